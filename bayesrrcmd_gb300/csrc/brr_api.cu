@@ -1,0 +1,926 @@
+// C ABI of libbrr_gpu.so and the host-side chain driver.
+//
+// The driver restates the per-iteration body of BayesRBase::runGibbs
+// (src/BayesRBase.cpp:186-247): updateMu, the per-marker draws, the shuffle,
+// the sweep (AnalysisGraph::exec -> processColumn for every marker), the
+// sigmaE draw and the per-group sigmaG / pi draws.  The sweep and all O(N) or
+// O(M) work run on the device; the handful of scalar draws per iteration run
+// on the host from the same counter-based stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <string>
+#include <vector>
+
+#include "brr_device.cuh"
+#include "brr_internal.h"
+#include "brr_stream.h"
+
+using namespace brr;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define BRR_CUDA(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(BRR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T **p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0)
+        n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T));
+}
+
+// Sweep permutation: Fisher-Yates from the counter-based stream.  The
+// reference shuffles with std::random_shuffle (src/BayesRBase.cpp:198); any
+// uniform permutation is equivalent in law, this one is replayable.
+void make_permutation(StreamKey key, uint32_t it, uint32_t M, uint32_t *perm)
+{
+    for (uint32_t i = 0; i < M; ++i)
+        perm[i] = i;
+    for (uint32_t i = M; i-- > 1;) {
+        const U4 b = stream_block(key, i, it, kPurposePerm, 0);
+        const uint64_t r = ((uint64_t)b.x << 32) | b.y;
+        const uint64_t j = (uint64_t)(((unsigned __int128)r * (uint64_t)(i + 1)) >> 64);
+        std::swap(perm[i], perm[j]);
+    }
+}
+
+}  // namespace
+
+struct brr_ctx {
+    brr_config cfg{};
+    int dev = 0;
+    int sms = 0;
+    cudaStream_t st = nullptr;
+    int G = 0;
+    int B = 16;
+    int64_t chunks = 0;
+    int64_t col_stride = 0;
+    int slice_max = 0;
+    int slot_bytes = 0;
+    std::vector<int32_t> slice_lo;
+    bool packed = false, pheno = false, inited = false;
+
+    // device buffers
+    int32_t *d_slice_lo = nullptr;
+    uint8_t *d_codes = nullptr;
+    int64_t *d_counts = nullptr;
+    double *d_table = nullptr;
+    double *d_scale = nullptr;
+    int32_t *d_roff = nullptr;          // 3 x (M*G+1)
+    uint16_t *d_ridx[3] = {nullptr, nullptr, nullptr};
+    int64_t rtot[3] = {0, 0, 0};
+    int32_t *d_group = nullptr;
+    double *d_ystd = nullptr;
+    double *d_beta = nullptr;
+    int32_t *d_comp = nullptr;
+    double *d_acum = nullptr;
+    double *d_eps = nullptr;
+    float *d_eps_hi = nullptr, *d_eps_lo = nullptr;
+    uint32_t *d_order = nullptr;
+    double *d_u = nullptr, *d_z = nullptr;
+    SweepRec *d_rec = nullptr;
+    unsigned long long *d_acc = nullptr;   // accumulators followed by the counter
+    double *d_gconst = nullptr;
+    int32_t *d_gK = nullptr;
+    double *d_stats = nullptr;
+    double *d_part = nullptr;
+    int *d_err = nullptr;
+    long long *d_rounds = nullptr;
+    uint32_t *d_nzj = nullptr;
+    double *d_nzb = nullptr;
+
+    // pinned host staging
+    uint32_t *h_order = nullptr;
+    double *h_stats = nullptr;
+    double *h_part = nullptr;
+
+    // host chain state
+    std::vector<int32_t> group;
+    std::vector<double> ystd;
+    double mu = 0.0, sigmaE = 0.0, epsSum = 0.0;
+    double sigmaG[BRR_MAX_GROUPS] = {};
+    double pi[BRR_MAX_GROUPS * BRR_MAX_K] = {};
+    uint32_t iteration = 0;
+    int64_t sweeps = 0;
+
+    // timing
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double last_sweep_ms = 0.0, last_total_ms = 0.0;
+    int64_t last_rounds = 0;
+
+    // permutation prepared one iteration ahead on a host thread
+    std::future<void> perm_future;
+    std::vector<uint32_t> perm_next;
+    uint32_t perm_next_it = UINT32_MAX;
+
+    StreamKey key() const { return StreamKey{cfg.seed, cfg.chain}; }
+};
+
+namespace {
+
+void free_all(brr_ctx *c)
+{
+    if (c->perm_future.valid())
+        c->perm_future.wait();
+    cudaFree(c->d_slice_lo);
+    cudaFree(c->d_codes);
+    cudaFree(c->d_counts);
+    cudaFree(c->d_table);
+    cudaFree(c->d_scale);
+    cudaFree(c->d_roff);
+    for (auto &p : c->d_ridx)
+        cudaFree(p);
+    cudaFree(c->d_group);
+    cudaFree(c->d_ystd);
+    cudaFree(c->d_beta);
+    cudaFree(c->d_comp);
+    cudaFree(c->d_acum);
+    cudaFree(c->d_eps);
+    cudaFree(c->d_eps_hi);
+    cudaFree(c->d_eps_lo);
+    cudaFree(c->d_order);
+    cudaFree(c->d_u);
+    cudaFree(c->d_z);
+    cudaFree(c->d_rec);
+    cudaFree(c->d_acc);
+    cudaFree(c->d_gconst);
+    cudaFree(c->d_gK);
+    cudaFree(c->d_stats);
+    cudaFree(c->d_part);
+    cudaFree(c->d_err);
+    cudaFree(c->d_rounds);
+    cudaFree(c->d_nzj);
+    cudaFree(c->d_nzb);
+    cudaFreeHost(c->h_order);
+    cudaFreeHost(c->h_stats);
+    cudaFreeHost(c->h_part);
+    for (auto &e : c->ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (c->st)
+        cudaStreamDestroy(c->st);
+}
+
+constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
+constexpr size_t kAccWords = 3 * kMaxSpec * 2;
+
+// Per-group sampler constants for the current sigmaE, sigmaG, pi
+// (src/BayesRBase.cpp:309-333): c_k = log(pi_k) - log(sigmaG/sigmaE*(N-1)*cVa_k + 1)/2,
+// invden_k = 1/denom_k with denom_k = N-1 + sigmaE/sigmaG/cVa_k,
+// h_k = invden_k/(2 sigmaE), sdk_k = sqrt(sigmaE/denom_k).
+void group_constants(const brr_ctx *c, std::vector<double> &gc, std::vector<int32_t> &gK)
+{
+    const int ng = c->cfg.n_groups;
+    gc.assign((size_t)ng * kMaxK * 4, 0.0);
+    gK.assign(ng, 0);
+    const double NM1 = (double)(c->cfg.N - 1);
+    for (int g = 0; g < ng; ++g) {
+        const int K = c->cfg.K[g];
+        gK[g] = K;
+        const double sigmaG = c->sigmaG[g];
+        const double sEsG = c->sigmaE / sigmaG;
+        const double logLScale = sigmaG / c->sigmaE * NM1;
+        double *row = gc.data() + (size_t)g * kMaxK * 4;
+        row[0] = std::log(c->pi[g * BRR_MAX_K]);
+        for (int k = 1; k < K; ++k) {
+            const double cVa = c->cfg.S[g * (BRR_MAX_K - 1) + (k - 1)];
+            const double cVaI = 1.0 / cVa;
+            const double denom = NM1 + sEsG * cVaI;
+            row[4 * k + 0] = std::log(c->pi[g * BRR_MAX_K + k]) - 0.5 * std::log(logLScale * cVa + 1.0);
+            row[4 * k + 1] = 1.0 / denom;
+            row[4 * k + 2] = 0.5 / denom / c->sigmaE;
+            row[4 * k + 3] = std::sqrt(c->sigmaE / denom);
+        }
+    }
+}
+
+int check_device_status(brr_ctx *c)
+{
+    int h = 0;
+    BRR_CUDA(cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    BRR_CUDA(cudaStreamSynchronize(c->st));
+    if (h == kDevTimeout)
+        return fail(BRR_ERR_TIMEOUT, "a grid barrier of the sweep exceeded its wait limit");
+    if (h == kDevRange)
+        return fail(BRR_ERR_RANGE, "a partial dot product left the fixed-point exchange range");
+    return BRR_OK;
+}
+
+int upload_state_eps(brr_ctx *c, const double *eps_host)
+{
+    const int64_t N = c->cfg.N;
+    if (c->cfg.form == BRR_FORM_FP64) {
+        BRR_CUDA(cudaMemcpy(c->d_eps, eps_host, sizeof(double) * N, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> h(N), l(N);
+        for (int64_t i = 0; i < N; ++i) {
+            h[i] = (float)eps_host[i];
+            l[i] = (float)(eps_host[i] - (double)h[i]);
+        }
+        BRR_CUDA(cudaMemcpy(c->d_eps_hi, h.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+        BRR_CUDA(cudaMemcpy(c->d_eps_lo, l.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    }
+    return BRR_OK;
+}
+
+int download_eps(brr_ctx *c, double *eps_host)
+{
+    const int64_t N = c->cfg.N;
+    if (c->cfg.form == BRR_FORM_FP64) {
+        BRR_CUDA(cudaMemcpy(eps_host, c->d_eps, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> h(N), l(N);
+        BRR_CUDA(cudaMemcpy(h.data(), c->d_eps_hi, sizeof(float) * N, cudaMemcpyDeviceToHost));
+        BRR_CUDA(cudaMemcpy(l.data(), c->d_eps_lo, sizeof(float) * N, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < N; ++i)
+            eps_host[i] = (double)h[i] + (double)l[i];
+    }
+    return BRR_OK;
+}
+
+// One sweep over the order already in d_order with draws in d_u/d_z.
+int run_sweep(brr_ctx *c, double mu_new, brr_sweep_out *out, float *sweep_ms)
+{
+    const brr_config &cf = c->cfg;
+    std::vector<double> gc;
+    std::vector<int32_t> gK;
+    group_constants(c, gc, gK);
+    BRR_CUDA(cudaMemcpyAsync(c->d_gconst, gc.data(), sizeof(double) * gc.size(), cudaMemcpyHostToDevice, c->st));
+    BRR_CUDA(cudaMemcpyAsync(c->d_gK, gK.data(), sizeof(int32_t) * gK.size(), cudaMemcpyHostToDevice, c->st));
+    BRR_CUDA(launch_gather(cf.form, cf.kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u, c->d_z,
+                           c->d_group, c->d_rec, c->st));
+    BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + 1), c->st));
+    BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+
+    SweepArgs a{};
+    a.N = cf.N;
+    a.M = cf.M;
+    a.G = c->G;
+    a.B = c->B;
+    a.n_groups = cf.n_groups;
+    a.slot_bytes = c->slot_bytes;
+    a.slice_max = c->slice_max;
+    a.slice_lo = c->d_slice_lo;
+    a.codes = c->d_codes;
+    a.col_stride = c->col_stride;
+    const int64_t MG1 = cf.M * (int64_t)c->G + 1;
+    for (int k = 0; k < 3; ++k) {
+        a.roff[k] = c->d_roff ? c->d_roff + k * MG1 : nullptr;
+        a.ridx[k] = c->d_ridx[k];
+    }
+    a.rec = c->d_rec;
+    a.gconst = c->d_gconst;
+    a.gK = c->d_gK;
+    a.beta = c->d_beta;
+    a.comp = c->d_comp;
+    a.acum = c->d_acum;
+    a.eps = c->d_eps;
+    a.eps_hi = c->d_eps_hi;
+    a.eps_lo = c->d_eps_lo;
+    a.mu_new = mu_new;
+    a.epsSum = c->epsSum;
+    a.acc = c->d_acc;
+    a.counter = c->d_acc + kAccWords;
+    a.stats_out = c->d_stats;
+    a.part = c->d_part;
+    a.err = c->d_err;
+    a.rounds_out = c->d_rounds;
+    a.timeout_ns = 2000000000ull;
+    const size_t smem = sweep_smem_bytes(cf.form, cf.kind, a);
+
+    BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
+    BRR_CUDA(launch_sweep(cf.form, cf.kind, a, smem, c->st));
+    BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
+
+    const int ng = cf.n_groups;
+    const size_t nstats = (size_t)ng * kMaxK + ng + 1;
+    BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double) * nstats, cudaMemcpyDeviceToHost, c->st));
+    BRR_CUDA(cudaMemcpyAsync(c->h_part, c->d_part, sizeof(double) * 2 * c->G, cudaMemcpyDeviceToHost, c->st));
+    long long rounds = 0;
+    BRR_CUDA(cudaMemcpyAsync(&rounds, c->d_rounds, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+    const int rc = check_device_status(c);
+    if (rc)
+        return rc;
+    BRR_CUDA(cudaEventElapsedTime(sweep_ms, c->ev[0], c->ev[1]));
+
+    for (int g = 0; g < ng; ++g)
+        for (int k = 0; k < BRR_MAX_K; ++k)
+            out->v[g * BRR_MAX_K + k] = k < kMaxK ? c->h_stats[g * kMaxK + k] : 0.0;
+    for (int g = 0; g < ng; ++g)
+        out->betasqnG[g] = c->h_stats[(size_t)ng * kMaxK + g];
+    double s1 = 0.0, s2 = 0.0;
+    for (int s = 0; s < c->G; ++s) {
+        s1 += c->h_part[2 * s];
+        s2 += c->h_part[2 * s + 1];
+    }
+    out->eps_sum = s1;
+    out->eps_sqnorm = s2;
+    out->rounds = rounds;
+    if (cf.kind == BRR_KIND_RAGGED)
+        c->epsSum = c->h_stats[(size_t)ng * kMaxK + ng];
+    c->sweeps += 1;
+    return BRR_OK;
+}
+
+int post_sweep_draws(brr_ctx *c, const brr_sweep_out &so, uint32_t it)
+{
+    const brr_config &cf = c->cfg;
+    const double Nd = (double)cf.N;
+    // sigmaE (src/BayesRBase.cpp:238-239)
+    if (!inv_scaled_chisq(c->key(), it, kPurposeSigmaE, 0, cf.v0E + Nd,
+                          (so.eps_sqnorm + cf.v0E * cf.s02E) / (cf.v0E + Nd), &c->sigmaE))
+        return fail(BRR_ERR_STREAM, "sigmaE gamma draw exceeded its attempt cap");
+    // sigmaG, pi per group (src/BayesRBase.cpp:243-247)
+    for (int g = 0; g < cf.n_groups; ++g) {
+        const int K = cf.K[g];
+        double vs = 0.0;
+        for (int k = 0; k < K; ++k)
+            vs += so.v[g * BRR_MAX_K + k];
+        const double m0 = vs - so.v[g * BRR_MAX_K];
+        if (!inv_scaled_chisq(c->key(), it, kPurposeSigmaG, (uint32_t)g, cf.v0G + m0,
+                              (so.betasqnG[g] * m0 + cf.v0G * cf.s02G) / (cf.v0G + m0), &c->sigmaG[g]))
+            return fail(BRR_ERR_STREAM, "sigmaG gamma draw exceeded its attempt cap");
+        double r[BRR_MAX_K], rs = 0.0;
+        for (int k = 0; k < K; ++k) {
+            double gk;
+            if (!gamma_draw(c->key(), it, kPurposePi, (uint32_t)(g * 256 + k), so.v[g * BRR_MAX_K + k] + 1.0, &gk))
+                return fail(BRR_ERR_STREAM, "Dirichlet gamma draw exceeded its attempt cap");
+            r[k] = 1.0 * gk;
+            rs += r[k];
+        }
+        for (int k = 0; k < K; ++k)
+            c->pi[g * BRR_MAX_K + k] = r[k] / rs;
+    }
+    return BRR_OK;
+}
+
+void schedule_permutation(brr_ctx *c, uint32_t it)
+{
+    if (c->perm_future.valid())
+        c->perm_future.wait();
+    c->perm_next.resize(c->cfg.M);
+    c->perm_next_it = it;
+    const StreamKey k = c->key();
+    const uint32_t M = (uint32_t)c->cfg.M;
+    uint32_t *dst = c->perm_next.data();
+    c->perm_future = std::async(std::launch::async, [k, it, M, dst]() { make_permutation(k, it, M, dst); });
+}
+
+int refresh_eps_impl(brr_ctx *c)
+{
+    const brr_config &cf = c->cfg;
+    std::vector<double> beta(cf.M);
+    BRR_CUDA(cudaMemcpy(beta.data(), c->d_beta, sizeof(double) * cf.M, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> nzj;
+    std::vector<double> nzb;
+    for (int64_t j = 0; j < cf.M; ++j)
+        if (beta[j] != 0.0) {
+            nzj.push_back((uint32_t)j);
+            nzb.push_back(beta[j]);
+        }
+    if (!nzj.empty()) {
+        BRR_CUDA(cudaMemcpy(c->d_nzj, nzj.data(), sizeof(uint32_t) * nzj.size(), cudaMemcpyHostToDevice));
+        BRR_CUDA(cudaMemcpy(c->d_nzb, nzb.data(), sizeof(double) * nzb.size(), cudaMemcpyHostToDevice));
+    }
+    BRR_CUDA(launch_refresh(cf.form, cf.kind, cf.N, c->d_ystd, c->mu, c->d_codes, c->col_stride, c->d_table, c->d_nzj,
+                            c->d_nzb, (int64_t)nzj.size(), c->d_eps, c->d_eps_hi, c->d_eps_lo, c->st));
+    BRR_CUDA(cudaStreamSynchronize(c->st));
+    return BRR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *brr_last_error(void) { return g_last_error.c_str(); }
+
+int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
+{
+    if (!cfg || !out)
+        return fail(BRR_ERR_ARG, "null argument");
+    *out = nullptr;
+    const brr_config &c = *cfg;
+    if (c.N < 2 || c.M < 1 || c.M > (int64_t)UINT32_MAX)
+        return fail(BRR_ERR_ARG, "need N >= 2 individuals and 1 <= M < 2^32 markers");
+    if (c.kind != BRR_KIND_DENSE && c.kind != BRR_KIND_RAGGED)
+        return fail(BRR_ERR_ARG, "unknown marker kind");
+    if (c.form != BRR_FORM_FP64 && c.form != BRR_FORM_FP32C)
+        return fail(BRR_ERR_ARG, "unknown sweep form");
+    if (c.n_groups < 1 || c.n_groups > BRR_MAX_GROUPS)
+        return fail(BRR_ERR_ARG, "n_groups must be in 1..64");
+    for (int g = 0; g < c.n_groups; ++g) {
+        if (c.K[g] < 2 || c.K[g] > BRR_MAX_K)
+            return fail(BRR_ERR_ARG, "every group needs 2..16 mixture components");
+        for (int k = 0; k + 1 < c.K[g]; ++k)
+            if (!(c.S[g * (BRR_MAX_K - 1) + k] > 0.0))
+                return fail(BRR_ERR_ARG, "variance ratios S must be positive");
+    }
+    int spec = c.spec_width ? c.spec_width : (c.form == BRR_FORM_FP64 ? 16 : 32);
+    if (spec != 8 && spec != 16 && spec != 32 && spec != 64)
+        return fail(BRR_ERR_ARG, "spec_width must be 8, 16, 32 or 64");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(BRR_ERR_DEVICE, "no CUDA device");
+    if (c.device < 0 || c.device >= ndev)
+        return fail(BRR_ERR_DEVICE, "device ordinal out of range");
+    cudaDeviceProp prop;
+    BRR_CUDA(cudaGetDeviceProperties(&prop, c.device));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(BRR_ERR_DEVICE, std::string("libbrr_gpu is built for sm_103a only; device is ") + prop.name);
+
+    brr_ctx *x = new brr_ctx();
+    x->cfg = c;
+    x->dev = c.device;
+    x->sms = prop.multiProcessorCount;
+    x->B = spec;
+    cudaError_t e = cudaSetDevice(c.device);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&x->st, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+        e = cudaEventCreate(&x->ev[i]);
+    if (e != cudaSuccess) {
+        free_all(x);
+        delete x;
+        return fail(BRR_ERR_CUDA, cudaGetErrorString(e));
+    }
+    // slices of individuals in 64-individual chunks (16 bytes of codes)
+    x->chunks = (c.N + kChunk - 1) / kChunk;
+    x->col_stride = x->chunks * 16;
+    int G = c.grid > 0 ? c.grid : x->sms;
+    G = (int)std::min<int64_t>(G, x->chunks);
+    x->G = G;
+    x->slice_lo.resize(G + 1);
+    int64_t maxch = 0;
+    for (int s = 0; s <= G; ++s) {
+        const int64_t ch = (int64_t)s * x->chunks / G;
+        x->slice_lo[s] = (int32_t)std::min<int64_t>(ch * kChunk, c.N);
+        if (s > 0)
+            maxch = std::max<int64_t>(maxch, ch - (int64_t)(s - 1) * x->chunks / G);
+    }
+    x->slice_max = (int)(maxch * kChunk);
+    x->slot_bytes = (int)(maxch * 16);
+    if (c.kind == BRR_KIND_RAGGED && x->slice_max > 65536) {
+        free_all(x);
+        delete x;
+        return fail(BRR_ERR_ARG, "ragged slices are limited to 65536 individuals; raise grid");
+    }
+    *out = x;
+    return BRR_OK;
+}
+
+int brr_ctx_destroy(brr_ctx *ctx)
+{
+    if (!ctx)
+        return BRR_OK;
+    cudaSetDevice(ctx->dev);
+    free_all(ctx);
+    delete ctx;
+    return BRR_OK;
+}
+
+int brr_pack_bed(brr_ctx *ctx, const uint8_t *bed, int64_t nbytes)
+{
+    if (!ctx || !bed)
+        return fail(BRR_ERR_ARG, "null argument");
+    const int64_t need = ctx->cfg.M * ((ctx->cfg.N + 3) / 4);
+    if (nbytes != need)
+        return fail(BRR_ERR_ARG, "BED payload size does not match M*ceil(N/4) (has the FAM/BIM been changed?)");
+    BRR_CUDA(cudaSetDevice(ctx->dev));
+    uint8_t *d = nullptr;
+    if (dalloc(&d, (size_t)nbytes) != cudaSuccess)
+        return fail(BRR_ERR_OOM, "device allocation of the BED payload failed");
+    cudaError_t e = cudaMemcpy(d, bed, (size_t)nbytes, cudaMemcpyHostToDevice);
+    int rc = e == cudaSuccess ? brr_pack_bed_device(ctx, d, nbytes) : fail(BRR_ERR_CUDA, cudaGetErrorString(e));
+    cudaFree(d);
+    return rc;
+}
+
+int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
+{
+    if (!ctx || !d_bed)
+        return fail(BRR_ERR_ARG, "null argument");
+    brr_ctx &c = *ctx;
+    const brr_config &cf = c.cfg;
+    if (nbytes != cf.M * ((cf.N + 3) / 4))
+        return fail(BRR_ERR_ARG, "BED payload size does not match M*ceil(N/4)");
+    BRR_CUDA(cudaSetDevice(c.dev));
+    const int64_t M = cf.M;
+    if (!c.d_codes) {
+        if (dalloc(&c.d_codes, (size_t)(M * c.col_stride)) != cudaSuccess || dalloc(&c.d_counts, (size_t)M * 4) ||
+            dalloc(&c.d_table, (size_t)M * 4) || dalloc(&c.d_scale, (size_t)M * 2) ||
+            dalloc(&c.d_slice_lo, (size_t)c.G + 1) || dalloc(&c.d_beta, (size_t)M) || dalloc(&c.d_comp, (size_t)M) ||
+            dalloc(&c.d_acum, (size_t)M) || dalloc(&c.d_order, (size_t)M) || dalloc(&c.d_u, (size_t)M) ||
+            dalloc(&c.d_z, (size_t)M) || dalloc(&c.d_rec, (size_t)M) || dalloc(&c.d_acc, kAccWords + 1) ||
+            dalloc(&c.d_gconst, (size_t)cf.n_groups * kMaxK * 4) || dalloc(&c.d_gK, (size_t)cf.n_groups) ||
+            dalloc(&c.d_stats, (size_t)cf.n_groups * kMaxK + cf.n_groups + 1) ||
+            dalloc(&c.d_part, (size_t)std::max(2 * c.G, kPartBlocks)) || dalloc(&c.d_err, 1) ||
+            dalloc(&c.d_rounds, 1) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
+            dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M))
+            return fail(BRR_ERR_OOM, "device allocation failed");
+        if (cf.form == BRR_FORM_FP64) {
+            if (dalloc(&c.d_eps, (size_t)cf.N))
+                return fail(BRR_ERR_OOM, "device allocation failed");
+        } else {
+            if (dalloc(&c.d_eps_hi, (size_t)cf.N) || dalloc(&c.d_eps_lo, (size_t)cf.N))
+                return fail(BRR_ERR_OOM, "device allocation failed");
+        }
+        if (cudaMallocHost((void **)&c.h_order, sizeof(uint32_t) * M) != cudaSuccess ||
+            cudaMallocHost((void **)&c.h_stats, sizeof(double) * ((size_t)cf.n_groups * kMaxK + cf.n_groups + 1)) !=
+                cudaSuccess ||
+            cudaMallocHost((void **)&c.h_part, sizeof(double) * std::max(2 * c.G, kPartBlocks)) != cudaSuccess)
+            return fail(BRR_ERR_OOM, "pinned host allocation failed");
+        BRR_CUDA(cudaMemset(c.d_group, 0, sizeof(int32_t) * M));
+        c.group.assign(M, 0);
+    }
+    BRR_CUDA(cudaMemcpy(c.d_slice_lo, c.slice_lo.data(), sizeof(int32_t) * (c.G + 1), cudaMemcpyHostToDevice));
+    BRR_CUDA(launch_pack_counts(d_bed, cf.N, M, c.d_codes, c.col_stride, c.d_counts, c.st));
+    int *d_bad = nullptr;
+    if (dalloc(&d_bad, 1))
+        return fail(BRR_ERR_OOM, "device allocation failed");
+    const int big = INT_MAX;
+    cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
+    if (cf.kind == BRR_KIND_DENSE) {
+        BRR_CUDA(launch_dense_tables(c.d_counts, cf.N, M, c.d_table, c.d_scale, d_bad, c.st));
+    } else {
+        BRR_CUDA(launch_ragged_stats(c.d_counts, cf.N, M, c.d_table, d_bad, c.st));
+    }
+    int bad = INT_MAX;
+    cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c.st);
+    cudaStreamSynchronize(c.st);
+    cudaFree(d_bad);
+    BRR_CUDA(cudaGetLastError());
+    if (bad != INT_MAX)
+        return fail(BRR_ERR_MARKER, "marker " + std::to_string(bad) +
+                                        " does not vary or is all missing; SNPs that do not vary should be "
+                                        "removed prior to analysis");
+    if (cf.kind == BRR_KIND_RAGGED) {
+        const int64_t MG1 = M * (int64_t)c.G + 1;
+        if (3 * MG1 > (int64_t)INT_MAX)
+            return fail(BRR_ERR_ARG, "ragged offset table too large for int32");
+        cudaFree(c.d_roff);
+        c.d_roff = nullptr;
+        if (dalloc(&c.d_roff, (size_t)(3 * MG1)))
+            return fail(BRR_ERR_OOM, "device allocation failed");
+        BRR_CUDA(cudaMemsetAsync(c.d_roff, 0, sizeof(int32_t) * 3 * MG1, c.st));
+        BRR_CUDA(launch_ragged_slice_counts(c.d_codes, c.col_stride, M, c.G, c.d_slice_lo, c.d_roff, c.st));
+        int32_t *tmp = nullptr;
+        if (dalloc(&tmp, (size_t)((MG1 + 1023) / 1024 + 1)))
+            return fail(BRR_ERR_OOM, "device allocation failed");
+        // totals must fit int32: the counts bound them by the genotype counts
+        std::vector<int64_t> cnt(M * 4);
+        BRR_CUDA(cudaMemcpyAsync(cnt.data(), c.d_counts, sizeof(int64_t) * M * 4, cudaMemcpyDeviceToHost, c.st));
+        BRR_CUDA(cudaStreamSynchronize(c.st));
+        int64_t tot[3] = {0, 0, 0};
+        for (int64_t j = 0; j < M; ++j) {
+            tot[0] += cnt[4 * j + 1];
+            tot[1] += cnt[4 * j + 2];
+            tot[2] += cnt[4 * j + 3];
+        }
+        for (int k = 0; k < 3; ++k) {
+            if (tot[k] > (int64_t)INT_MAX) {
+                cudaFree(tmp);
+                return fail(BRR_ERR_ARG, "ragged index list longer than 2^31 entries");
+            }
+            BRR_CUDA(launch_exclusive_scan_i32(c.d_roff + k * MG1, MG1, tmp, c.st));
+            cudaFree(c.d_ridx[k]);
+            c.d_ridx[k] = nullptr;
+            if (dalloc(&c.d_ridx[k], (size_t)tot[k] + 1)) {
+                cudaFree(tmp);
+                return fail(BRR_ERR_OOM, "device allocation failed");
+            }
+            c.rtot[k] = tot[k];
+        }
+        BRR_CUDA(cudaStreamSynchronize(c.st));
+        cudaFree(tmp);
+        BRR_CUDA(launch_ragged_fill(c.d_codes, c.col_stride, M, c.G, c.d_slice_lo, c.d_roff, c.d_roff + MG1,
+                                    c.d_roff + 2 * MG1, c.d_ridx[0], c.d_ridx[1], c.d_ridx[2], c.st));
+    }
+    BRR_CUDA(cudaStreamSynchronize(c.st));
+    // the sweep kernel must fit one CTA per slice on the GPU at once
+    SweepArgs a{};
+    a.B = c.B;
+    a.n_groups = cf.n_groups;
+    a.slice_max = c.slice_max;
+    a.slot_bytes = c.slot_bytes;
+    const size_t smem = sweep_smem_bytes(cf.form, cf.kind, a);
+    const int per_sm = sweep_max_ctas_per_sm(cf.form, cf.kind, smem);
+    if (per_sm < 1 || (int64_t)per_sm * c.sms < c.G)
+        return fail(BRR_ERR_ARG, "the sweep kernel does not fit " + std::to_string(c.G) +
+                                     " co-resident CTAs (shared memory " + std::to_string(smem) + " bytes)");
+    c.packed = true;
+    return BRR_OK;
+}
+
+int brr_get_marker_table(brr_ctx *ctx, double *table, int64_t *counts)
+{
+    if (!ctx || !ctx->packed)
+        return fail(BRR_ERR_ARG, "markers are not packed");
+    const int64_t M = ctx->cfg.M;
+    if (table)
+        BRR_CUDA(cudaMemcpy(table, ctx->d_table, sizeof(double) * M * 4, cudaMemcpyDeviceToHost));
+    if (counts)
+        BRR_CUDA(cudaMemcpy(counts, ctx->d_counts, sizeof(int64_t) * M * 4, cudaMemcpyDeviceToHost));
+    return BRR_OK;
+}
+
+int brr_get_ragged_lists(brr_ctx *ctx, int64_t *off_ones, int32_t *ones, int64_t *off_twos, int32_t *twos,
+                         int64_t *off_miss, int32_t *miss)
+{
+    if (!ctx || !ctx->packed || ctx->cfg.kind != BRR_KIND_RAGGED)
+        return fail(BRR_ERR_ARG, "no ragged markers packed");
+    const int64_t M = ctx->cfg.M, G = ctx->G, MG1 = M * G + 1;
+    std::vector<int32_t> off(3 * MG1);
+    BRR_CUDA(cudaMemcpy(off.data(), ctx->d_roff, sizeof(int32_t) * 3 * MG1, cudaMemcpyDeviceToHost));
+    int64_t *offs[3] = {off_ones, off_twos, off_miss};
+    int32_t *outs[3] = {ones, twos, miss};
+    for (int k = 0; k < 3; ++k) {
+        std::vector<uint16_t> idx(ctx->rtot[k] + 1);
+        BRR_CUDA(cudaMemcpy(idx.data(), ctx->d_ridx[k], sizeof(uint16_t) * (ctx->rtot[k] + 1), cudaMemcpyDeviceToHost));
+        const int32_t *o = off.data() + k * MG1;
+        for (int64_t j = 0; j < M; ++j) {
+            if (offs[k])
+                offs[k][j] = o[j * G];
+            for (int64_t s = 0; s < G; ++s)
+                for (int32_t e = o[j * G + s]; e < o[j * G + s + 1]; ++e)
+                    if (outs[k])
+                        outs[k][e] = ctx->slice_lo[s] + idx[e];
+        }
+        if (offs[k])
+            offs[k][M] = o[M * G];
+    }
+    return BRR_OK;
+}
+
+int brr_set_groups(brr_ctx *ctx, const int32_t *group)
+{
+    if (!ctx || !group || !ctx->packed)
+        return fail(BRR_ERR_ARG, "pack markers before setting groups");
+    for (int64_t j = 0; j < ctx->cfg.M; ++j)
+        if (group[j] < 0 || group[j] >= ctx->cfg.n_groups)
+            return fail(BRR_ERR_ARG, "group id out of range at marker " + std::to_string(j));
+    ctx->group.assign(group, group + ctx->cfg.M);
+    BRR_CUDA(cudaMemcpy(ctx->d_group, group, sizeof(int32_t) * ctx->cfg.M, cudaMemcpyHostToDevice));
+    return BRR_OK;
+}
+
+// y standardisation of BayesRBase::init (src/BayesRBase.cpp:85-86) on the
+// single-precision phenotype (src/data.cpp:348).
+int brr_set_phenotype(brr_ctx *ctx, const float *y)
+{
+    if (!ctx || !y || !ctx->packed)
+        return fail(BRR_ERR_ARG, "pack markers before setting the phenotype");
+    const int64_t N = ctx->cfg.N;
+    double ysum = 0.0;
+    for (int64_t i = 0; i < N; ++i) {
+        if (!std::isfinite(y[i]))
+            return fail(BRR_ERR_ARG, "phenotype value " + std::to_string(i) + " is not finite");
+        ysum += (double)y[i];
+    }
+    const double ymean = ysum / (double)N;
+    std::vector<double> d(N);
+    double sq = 0.0;
+    for (int64_t i = 0; i < N; ++i) {
+        d[i] = (double)y[i] - ymean;
+        sq += d[i] * d[i];
+    }
+    if (!(sq > 0.0))
+        return fail(BRR_ERR_ARG, "phenotype has zero variance");
+    const double scale = std::sqrt(sq / (double)(N - 1));
+    ctx->ystd.resize(N);
+    for (int64_t i = 0; i < N; ++i)
+        ctx->ystd[i] = d[i] / scale;
+    BRR_CUDA(cudaMemcpy(ctx->d_ystd, ctx->ystd.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    ctx->pheno = true;
+    return BRR_OK;
+}
+
+// BayesRBase::init (src/BayesRBase.cpp:39-99).
+int brr_init_chain(brr_ctx *ctx)
+{
+    if (!ctx || !ctx->packed || !ctx->pheno)
+        return fail(BRR_ERR_ARG, "pack markers and set the phenotype before init");
+    brr_ctx &c = *ctx;
+    const brr_config &cf = c.cfg;
+    const int64_t N = cf.N, M = cf.M;
+    for (int g = 0; g < cf.n_groups; ++g) {
+        const int K = cf.K[g];
+        for (int k = 0; k < BRR_MAX_K; ++k)
+            c.pi[g * BRR_MAX_K + k] = k < K ? 0.5 / (double)K : 0.0;
+        c.pi[g * BRR_MAX_K] = 0.5;
+        c.sigmaG[g] = uniform_init(c.key(), (uint32_t)g);
+    }
+    c.mu = 0.0;
+    std::vector<double> eps(N);
+    double esq = 0.0, esum = 0.0;
+    for (int64_t i = 0; i < N; ++i) {
+        eps[i] = c.ystd[i] - c.mu;
+        esq += eps[i] * eps[i];
+        esum += eps[i];
+    }
+    c.sigmaE = esq / (double)N * 0.5;
+    c.epsSum = esum;
+    BRR_CUDA(cudaMemset(c.d_beta, 0, sizeof(double) * M));
+    BRR_CUDA(cudaMemset(c.d_comp, 0, sizeof(int32_t) * M));
+    BRR_CUDA(cudaMemset(c.d_acum, 0, sizeof(double) * M));
+    int rc = upload_state_eps(&c, eps.data());
+    if (rc)
+        return rc;
+    c.iteration = 0;
+    c.sweeps = 0;
+    c.inited = true;
+    return BRR_OK;
+}
+
+int brr_iterate(brr_ctx *ctx, int32_t n_iter)
+{
+    if (!ctx || !ctx->inited)
+        return fail(BRR_ERR_ARG, "chain not initialised");
+    brr_ctx &c = *ctx;
+    const brr_config &cf = c.cfg;
+    BRR_CUDA(cudaSetDevice(c.dev));
+    const int64_t N = cf.N, M = cf.M;
+    const double Nd = (double)N;
+    double sweep_total = 0.0;
+    int64_t rounds_total = 0;
+    BRR_CUDA(cudaEventRecord(c.ev[2], c.st));
+    if (c.perm_next_it != c.iteration)
+        schedule_permutation(&c, c.iteration);
+    for (int32_t n = 0; n < n_iter; ++n) {
+        const uint32_t it = c.iteration;
+        if (cf.form == BRR_FORM_FP32C && cf.refresh_every > 0 && c.sweeps > 0 && c.sweeps % cf.refresh_every == 0) {
+            const int rc = refresh_eps_impl(&c);
+            if (rc)
+                return rc;
+        }
+        // updateMu (dense src/DenseBayesRRmz.cpp:36-42, ragged src/SparseBayesRRG.cpp:106-113)
+        const double old_mu = c.mu;
+        BRR_CUDA(launch_mu_prep(cf.form, N, old_mu, c.d_eps, c.d_eps_hi, c.d_eps_lo, c.d_part, kPartBlocks, c.st));
+        double mean;
+        if (cf.kind == BRR_KIND_DENSE) {
+            BRR_CUDA(cudaMemcpyAsync(c.h_part, c.d_part, sizeof(double) * kPartBlocks, cudaMemcpyDeviceToHost, c.st));
+            BRR_CUDA(cudaStreamSynchronize(c.st));
+            double s = 0.0;
+            for (int b = 0; b < kPartBlocks; ++b)
+                s += c.h_part[b];
+            mean = s / Nd;
+        } else {
+            c.epsSum += old_mu * Nd;
+            mean = c.epsSum / Nd;
+        }
+        c.mu = mean + std::sqrt(c.sigmaE / Nd) * normal_mu(c.key(), it);
+        if (cf.kind == BRR_KIND_RAGGED)
+            c.epsSum -= c.mu * Nd;
+
+        // per-marker draws and the permutation (src/BayesRBase.cpp:196-198)
+        BRR_CUDA(launch_draws(cf.seed, cf.chain, it, M, c.d_u, c.d_z, c.st));
+        c.perm_future.wait();
+        std::memcpy(c.h_order, c.perm_next.data(), sizeof(uint32_t) * M);
+        BRR_CUDA(cudaMemcpyAsync(c.d_order, c.h_order, sizeof(uint32_t) * M, cudaMemcpyHostToDevice, c.st));
+        schedule_permutation(&c, it + 1);
+
+        brr_sweep_out so{};
+        float ms = 0.f;
+        int rc = run_sweep(&c, c.mu, &so, &ms);
+        if (rc)
+            return rc;
+        sweep_total += ms;
+        rounds_total += so.rounds;
+        rc = post_sweep_draws(&c, so, it);
+        if (rc)
+            return rc;
+        c.iteration = it + 1;
+    }
+    BRR_CUDA(cudaEventRecord(c.ev[3], c.st));
+    BRR_CUDA(cudaEventSynchronize(c.ev[3]));
+    float tot = 0.f;
+    BRR_CUDA(cudaEventElapsedTime(&tot, c.ev[2], c.ev[3]));
+    c.last_sweep_ms = sweep_total;
+    c.last_total_ms = tot;
+    c.last_rounds = rounds_total;
+    return BRR_OK;
+}
+
+int brr_sweep(brr_ctx *ctx, const uint32_t *order, const double *u, const double *z, brr_sweep_out *out)
+{
+    if (!ctx || !ctx->inited || !order || !u || !z || !out)
+        return fail(BRR_ERR_ARG, "chain not initialised or null argument");
+    brr_ctx &c = *ctx;
+    const int64_t M = c.cfg.M;
+    std::vector<uint8_t> seen(M, 0);
+    for (int64_t q = 0; q < M; ++q) {
+        if (order[q] >= (uint32_t)M || seen[order[q]])
+            return fail(BRR_ERR_ARG, "order is not a permutation of 0..M-1");
+        seen[order[q]] = 1;
+    }
+    BRR_CUDA(cudaSetDevice(c.dev));
+    BRR_CUDA(cudaMemcpyAsync(c.d_order, order, sizeof(uint32_t) * M, cudaMemcpyHostToDevice, c.st));
+    BRR_CUDA(cudaMemcpyAsync(c.d_u, u, sizeof(double) * M, cudaMemcpyHostToDevice, c.st));
+    BRR_CUDA(cudaMemcpyAsync(c.d_z, z, sizeof(double) * M, cudaMemcpyHostToDevice, c.st));
+    BRR_CUDA(cudaEventRecord(c.ev[2], c.st));
+    float ms = 0.f;
+    const int rc = run_sweep(&c, 0.0, out, &ms);
+    if (rc)
+        return rc;
+    BRR_CUDA(cudaEventRecord(c.ev[3], c.st));
+    BRR_CUDA(cudaEventSynchronize(c.ev[3]));
+    float tot = 0.f;
+    BRR_CUDA(cudaEventElapsedTime(&tot, c.ev[2], c.ev[3]));
+    c.last_sweep_ms = ms;
+    c.last_total_ms = tot;
+    c.last_rounds = out->rounds;
+    return BRR_OK;
+}
+
+int brr_get_state(brr_ctx *ctx, brr_state *st)
+{
+    if (!ctx || !st || !ctx->inited)
+        return fail(BRR_ERR_ARG, "chain not initialised");
+    brr_ctx &c = *ctx;
+    const int64_t M = c.cfg.M;
+    BRR_CUDA(cudaStreamSynchronize(c.st));
+    if (st->beta)
+        BRR_CUDA(cudaMemcpy(st->beta, c.d_beta, sizeof(double) * M, cudaMemcpyDeviceToHost));
+    if (st->comp)
+        BRR_CUDA(cudaMemcpy(st->comp, c.d_comp, sizeof(int32_t) * M, cudaMemcpyDeviceToHost));
+    if (st->acum)
+        BRR_CUDA(cudaMemcpy(st->acum, c.d_acum, sizeof(double) * M, cudaMemcpyDeviceToHost));
+    if (st->eps) {
+        const int rc = download_eps(&c, st->eps);
+        if (rc)
+            return rc;
+    }
+    st->mu = c.mu;
+    st->sigmaE = c.sigmaE;
+    st->epsSum = c.epsSum;
+    std::memcpy(st->sigmaG, c.sigmaG, sizeof(c.sigmaG));
+    std::memcpy(st->pi, c.pi, sizeof(c.pi));
+    st->iteration = c.iteration;
+    return BRR_OK;
+}
+
+int brr_set_state(brr_ctx *ctx, const brr_state *st)
+{
+    if (!ctx || !st || !ctx->packed || !ctx->pheno || !st->beta || !st->comp || !st->acum || !st->eps)
+        return fail(BRR_ERR_ARG, "pack and set the phenotype first; all state arrays are required");
+    brr_ctx &c = *ctx;
+    const int64_t M = c.cfg.M;
+    BRR_CUDA(cudaStreamSynchronize(c.st));
+    BRR_CUDA(cudaMemcpy(c.d_beta, st->beta, sizeof(double) * M, cudaMemcpyHostToDevice));
+    BRR_CUDA(cudaMemcpy(c.d_comp, st->comp, sizeof(int32_t) * M, cudaMemcpyHostToDevice));
+    BRR_CUDA(cudaMemcpy(c.d_acum, st->acum, sizeof(double) * M, cudaMemcpyHostToDevice));
+    const int rc = upload_state_eps(&c, st->eps);
+    if (rc)
+        return rc;
+    c.mu = st->mu;
+    c.sigmaE = st->sigmaE;
+    c.epsSum = st->epsSum;
+    std::memcpy(c.sigmaG, st->sigmaG, sizeof(c.sigmaG));
+    std::memcpy(c.pi, st->pi, sizeof(c.pi));
+    c.iteration = st->iteration;
+    c.inited = true;
+    return BRR_OK;
+}
+
+int brr_refresh_eps(brr_ctx *ctx)
+{
+    if (!ctx || !ctx->inited)
+        return fail(BRR_ERR_ARG, "chain not initialised");
+    BRR_CUDA(cudaSetDevice(ctx->dev));
+    return refresh_eps_impl(ctx);
+}
+
+int brr_get_timing(brr_ctx *ctx, double *sweep_ms, double *total_ms, int64_t *rounds)
+{
+    if (!ctx)
+        return fail(BRR_ERR_ARG, "null context");
+    if (sweep_ms)
+        *sweep_ms = ctx->last_sweep_ms;
+    if (total_ms)
+        *total_ms = ctx->last_total_ms;
+    if (rounds)
+        *rounds = ctx->last_rounds;
+    return BRR_OK;
+}
+
+}  // extern "C"

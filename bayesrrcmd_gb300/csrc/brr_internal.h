@@ -1,0 +1,88 @@
+// Internal declarations shared by the translation units of libbrr_gpu.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/brr_gpu.h"
+
+namespace brr {
+
+// One record per sweep position, gathered before each sweep so that the
+// persistent kernel streams them contiguously.  t[] holds the marker table
+// in the layout the sweep form needs:
+//   FP64 dense : standardised value per 2-bit code (4 doubles)
+//   FP32C dense: {sigma, colmean, value of a missing genotype, 0}
+//   ragged     : {mean, sd, sqrdZ, Zsum}
+struct alignas(16) SweepRec {
+    double t[4];
+    double beta_old;
+    double u;
+    double z;
+    uint32_t j;
+    int32_t group;
+};
+static_assert(sizeof(SweepRec) == 64, "SweepRec must be 64 bytes");
+
+struct SweepArgs {
+    int64_t N, M;
+    int G;                       // CTAs (slices of individuals)
+    int B;                       // markers resolved per grid round
+    int n_groups;
+    int slot_bytes;              // bytes of one ring slot (max slice code bytes)
+    int slice_max;               // max individuals of a slice (multiple of 64)
+    const int32_t *slice_lo;     // G+1 slice boundaries in individuals
+    const uint8_t *codes;        // M x col_stride 2-bit codes
+    int64_t col_stride;
+    const int32_t *roff[3];      // ragged: (M*G+1) offsets of ones/twos/missing per (marker, slice)
+    const uint16_t *ridx[3];     // ragged: slice-local indices
+    const SweepRec *rec;         // M records in sweep order
+    const double *gconst;        // [n_groups][kMaxK][4] {c, invden, h, sdk}
+    const int32_t *gK;           // [n_groups]
+    double *beta;
+    int32_t *comp;
+    double *acum;
+    double *eps;                 // FP64 residual (FP64 form)
+    float *eps_hi, *eps_lo;      // double-float residual (FP32C form)
+    double mu_new;               // subtracted from eps while it is loaded (updateMu, second half)
+    double epsSum;               // ragged running sum at sweep start (after updateMu)
+    unsigned long long *acc;     // [3][kMaxSpec][2] fixed-point accumulators
+    unsigned long long *counter; // grid round counter, zero at launch
+    double *stats_out;           // v[n_groups*kMaxK], betasqnG[n_groups], epsSum_end
+    double *part;                // [G][2] per-slice sum(eps), sum(eps^2) after the sweep
+    int *err;                    // device status word
+    long long *rounds_out;
+    uint64_t timeout_ns;         // limit of any single wait
+};
+
+// Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).
+cudaError_t launch_pack_counts(const uint8_t *bed, int64_t N, int64_t M, uint8_t *codes,
+                               int64_t col_stride, int64_t *counts, cudaStream_t st);
+cudaError_t launch_dense_tables(const int64_t *counts, int64_t N, int64_t M, double *lut,
+                                double *scale, int *bad, cudaStream_t st);
+cudaError_t launch_ragged_stats(const int64_t *counts, int64_t N, int64_t M, double *stats,
+                                int *bad, cudaStream_t st);
+cudaError_t launch_ragged_slice_counts(const uint8_t *codes, int64_t col_stride, int64_t M, int G,
+                                       const int32_t *slice_lo, int32_t *cnt3, cudaStream_t st);
+cudaError_t launch_exclusive_scan_i32(int32_t *data, int64_t n, int32_t *tmp, cudaStream_t st);
+cudaError_t launch_ragged_fill(const uint8_t *codes, int64_t col_stride, int64_t M, int G,
+                               const int32_t *slice_lo, const int32_t *off0, const int32_t *off1,
+                               const int32_t *off2, uint16_t *idx0, uint16_t *idx1, uint16_t *idx2,
+                               cudaStream_t st);
+cudaError_t launch_draws(uint32_t seed, uint32_t chain, uint32_t it, int64_t M, double *u, double *z,
+                         cudaStream_t st);
+cudaError_t launch_gather(int form, int kind, const uint32_t *order, int64_t M, const double *table,
+                          const double *scale, const double *beta, const double *u, const double *z,
+                          const int32_t *group, SweepRec *rec, cudaStream_t st);
+cudaError_t launch_mu_prep(int form, int64_t N, double mu_old, double *eps, float *eps_hi,
+                           float *eps_lo, double *part, int nblocks, cudaStream_t st);
+cudaError_t launch_refresh(int form, int kind, int64_t N, const double *ystd, double mu,
+                           const uint8_t *codes, int64_t col_stride, const double *table,
+                           const uint32_t *nz_j, const double *nz_beta, int64_t n_nz, double *eps,
+                           float *eps_hi, float *eps_lo, cudaStream_t st);
+cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st);
+size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a);
+int sweep_max_ctas_per_sm(int form, int kind, size_t smem);
+
+}  // namespace brr

@@ -1,0 +1,265 @@
+"""ctypes binding of libbrr_gpu.so (the C ABI declared in include/brr_gpu.h).
+
+This is the Python mirror of the host interface the reference exposes for the
+BayesR path (src/analysis.h:25-52, src/markerbuilder.h:11-42): pack the
+markers, set groups and phenotype, initialise, run the Gibbs chain, read the
+state.  It is a thin binding: all compute runs in the CUDA library, and
+loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+MAX_GROUPS = 64
+MAX_K = 16
+
+KIND_DENSE, KIND_RAGGED = 0, 1
+FORM_FP64, FORM_FP32C = 0, 1
+
+ERRORS = {
+    -1: "BRR_ERR_ARG", -2: "BRR_ERR_CUDA", -3: "BRR_ERR_OOM", -4: "BRR_ERR_TIMEOUT",
+    -5: "BRR_ERR_MARKER", -6: "BRR_ERR_RANGE", -7: "BRR_ERR_STREAM", -8: "BRR_ERR_DEVICE",
+}
+
+
+class BrrConfig(C.Structure):
+    _fields_ = [
+        ("N", C.c_int64), ("M", C.c_int64), ("kind", C.c_int32), ("form", C.c_int32),
+        ("n_groups", C.c_int32), ("K", C.c_int32 * MAX_GROUPS),
+        ("S", C.c_double * (MAX_GROUPS * (MAX_K - 1))),
+        ("seed", C.c_uint32), ("chain", C.c_uint32),
+        ("v0E", C.c_double), ("s02E", C.c_double), ("v0G", C.c_double), ("s02G", C.c_double),
+        ("refresh_every", C.c_int32), ("spec_width", C.c_int32), ("grid", C.c_int32), ("device", C.c_int32),
+    ]
+
+
+class BrrState(C.Structure):
+    _fields_ = [
+        ("beta", C.POINTER(C.c_double)), ("comp", C.POINTER(C.c_int32)), ("acum", C.POINTER(C.c_double)),
+        ("eps", C.POINTER(C.c_double)), ("mu", C.c_double), ("sigmaE", C.c_double), ("epsSum", C.c_double),
+        ("sigmaG", C.c_double * MAX_GROUPS), ("pi", C.c_double * (MAX_GROUPS * MAX_K)), ("iteration", C.c_uint32),
+    ]
+
+
+class BrrSweepOut(C.Structure):
+    _fields_ = [
+        ("v", C.c_double * (MAX_GROUPS * MAX_K)), ("betasqnG", C.c_double * MAX_GROUPS),
+        ("eps_sqnorm", C.c_double), ("eps_sum", C.c_double), ("rounds", C.c_int64),
+    ]
+
+
+_LIB: Optional[C.CDLL] = None
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libbrr_gpu.so"
+
+EXPORTS = [
+    "brr_last_error", "brr_ctx_create", "brr_ctx_destroy", "brr_pack_bed", "brr_pack_bed_device",
+    "brr_get_marker_table", "brr_get_ragged_lists", "brr_set_groups", "brr_set_phenotype", "brr_init_chain",
+    "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing",
+]
+
+
+def load_library(path: Optional[Path] = None) -> C.CDLL:
+    """Load libbrr_gpu.so; raises if it has not been built (no fallback)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with `python -m bayesrrcmd_gb300.build` "
+                           "(the GPU path has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    P = C.c_void_p
+    lib.brr_last_error.restype = C.c_char_p
+    lib.brr_ctx_create.argtypes = [C.POINTER(BrrConfig), C.POINTER(P)]
+    lib.brr_ctx_destroy.argtypes = [P]
+    lib.brr_pack_bed.argtypes = [P, C.POINTER(C.c_uint8), C.c_int64]
+    lib.brr_pack_bed_device.argtypes = [P, P, C.c_int64]
+    lib.brr_get_marker_table.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.brr_get_ragged_lists.argtypes = [P] + [C.POINTER(C.c_int64), C.POINTER(C.c_int32)] * 3
+    lib.brr_set_groups.argtypes = [P, C.POINTER(C.c_int32)]
+    lib.brr_set_phenotype.argtypes = [P, C.POINTER(C.c_float)]
+    lib.brr_init_chain.argtypes = [P]
+    lib.brr_iterate.argtypes = [P, C.c_int32]
+    lib.brr_sweep.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                              C.POINTER(BrrSweepOut)]
+    lib.brr_get_state.argtypes = [P, C.POINTER(BrrState)]
+    lib.brr_set_state.argtypes = [P, C.POINTER(BrrState)]
+    lib.brr_refresh_eps.argtypes = [P]
+    lib.brr_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    for name in EXPORTS:
+        if name != "brr_last_error":
+            getattr(lib, name).restype = C.c_int
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+class BrrError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _ptr(a: np.ndarray, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+@dataclass
+class ChainConfig:
+    """Mirror of the reference Options used on this path (src/options.hpp:21-105)."""
+    N: int
+    M: int
+    kind: int = KIND_DENSE
+    form: int = FORM_FP64
+    S: Sequence[Sequence[float]] = field(default_factory=lambda: [[0.01, 0.001, 0.0001]])
+    seed: int = 1
+    chain: int = 0
+    v0E: float = 1e-4
+    s02E: float = 1e-4
+    v0G: float = 1e-4
+    s02G: float = 1e-4
+    refresh_every: int = 0
+    spec_width: int = 0
+    grid: int = 0
+    device: int = 0
+
+    def to_c(self) -> BrrConfig:
+        c = BrrConfig()
+        c.N, c.M, c.kind, c.form = self.N, self.M, self.kind, self.form
+        c.n_groups = len(self.S)
+        for g, row in enumerate(self.S):
+            c.K[g] = len(row) + 1
+            for k, v in enumerate(row):
+                c.S[g * (MAX_K - 1) + k] = float(v)
+        c.seed, c.chain = self.seed & 0xFFFFFFFF, self.chain & 0xFFFFFFFF
+        c.v0E, c.s02E, c.v0G, c.s02G = self.v0E, self.s02E, self.v0G, self.s02G
+        c.refresh_every, c.spec_width, c.grid, c.device = self.refresh_every, self.spec_width, self.grid, self.device
+        return c
+
+
+class Chain:
+    """One BayesR Markov chain on one GPU, behind the C ABI."""
+
+    def __init__(self, cfg: ChainConfig, lib: Optional[C.CDLL] = None):
+        self.cfg = cfg
+        self.lib = lib or load_library()
+        self._c = cfg.to_c()
+        h = C.c_void_p()
+        self._check(self.lib.brr_ctx_create(C.byref(self._c), C.byref(h)))
+        self.h = h
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise BrrError(rc, self.lib.brr_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.brr_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # preprocess ------------------------------------------------------------
+    def pack_bed(self, bed_payload: np.ndarray):
+        a = np.ascontiguousarray(bed_payload, dtype=np.uint8)
+        self._check(self.lib.brr_pack_bed(self.h, _ptr(a, C.c_uint8), a.size))
+
+    def pack_bed_device(self, dev_ptr: int, nbytes: int):
+        self._check(self.lib.brr_pack_bed_device(self.h, C.c_void_p(dev_ptr), nbytes))
+
+    def marker_table(self):
+        t = np.zeros((self.cfg.M, 4), np.float64)
+        n = np.zeros((self.cfg.M, 4), np.int64)
+        self._check(self.lib.brr_get_marker_table(self.h, _ptr(t, C.c_double), _ptr(n, C.c_int64)))
+        return t, n
+
+    def ragged_lists(self, counts: np.ndarray):
+        M = self.cfg.M
+        offs = [np.zeros(M + 1, np.int64) for _ in range(3)]
+        tot = [int(counts[:, 1].sum()), int(counts[:, 2].sum()), int(counts[:, 3].sum())]
+        idx = [np.zeros(max(t, 1), np.int32) for t in tot]
+        args = []
+        for k in range(3):
+            args += [_ptr(offs[k], C.c_int64), _ptr(idx[k], C.c_int32)]
+        self._check(self.lib.brr_get_ragged_lists(self.h, *args))
+        return [(offs[k], idx[k][:tot[k]]) for k in range(3)]
+
+    # chain -----------------------------------------------------------------
+    def set_groups(self, group: np.ndarray):
+        g = np.ascontiguousarray(group, dtype=np.int32)
+        self._check(self.lib.brr_set_groups(self.h, _ptr(g, C.c_int32)))
+
+    def set_phenotype(self, y: np.ndarray):
+        a = np.ascontiguousarray(y, dtype=np.float32)
+        self._check(self.lib.brr_set_phenotype(self.h, _ptr(a, C.c_float)))
+
+    def init(self):
+        self._check(self.lib.brr_init_chain(self.h))
+
+    def iterate(self, n: int = 1):
+        self._check(self.lib.brr_iterate(self.h, int(n)))
+
+    def sweep(self, order: np.ndarray, u: np.ndarray, z: np.ndarray) -> BrrSweepOut:
+        o = np.ascontiguousarray(order, dtype=np.uint32)
+        uu = np.ascontiguousarray(u, dtype=np.float64)
+        zz = np.ascontiguousarray(z, dtype=np.float64)
+        out = BrrSweepOut()
+        self._check(self.lib.brr_sweep(self.h, _ptr(o, C.c_uint32), _ptr(uu, C.c_double), _ptr(zz, C.c_double),
+                                       C.byref(out)))
+        return out
+
+    def refresh(self):
+        self._check(self.lib.brr_refresh_eps(self.h))
+
+    def state(self) -> dict:
+        M, N = self.cfg.M, self.cfg.N
+        beta = np.zeros(M, np.float64)
+        comp = np.zeros(M, np.int32)
+        acum = np.zeros(M, np.float64)
+        eps = np.zeros(N, np.float64)
+        st = BrrState()
+        st.beta, st.comp, st.acum, st.eps = (_ptr(beta, C.c_double), _ptr(comp, C.c_int32),
+                                             _ptr(acum, C.c_double), _ptr(eps, C.c_double))
+        self._check(self.lib.brr_get_state(self.h, C.byref(st)))
+        G = len(self.cfg.S)
+        return dict(beta=beta, comp=comp, acum=acum, eps=eps, mu=st.mu, sigmaE=st.sigmaE, epsSum=st.epsSum,
+                    sigmaG=np.array(st.sigmaG[:G]),
+                    pi=np.array(st.pi[:]).reshape(MAX_GROUPS, MAX_K)[:G].copy(), iteration=st.iteration)
+
+    def set_state(self, s: dict):
+        beta = np.ascontiguousarray(s["beta"], np.float64)
+        comp = np.ascontiguousarray(s["comp"], np.int32)
+        acum = np.ascontiguousarray(s["acum"], np.float64)
+        eps = np.ascontiguousarray(s["eps"], np.float64)
+        st = BrrState()
+        st.beta, st.comp, st.acum, st.eps = (_ptr(beta, C.c_double), _ptr(comp, C.c_int32),
+                                             _ptr(acum, C.c_double), _ptr(eps, C.c_double))
+        st.mu, st.sigmaE, st.epsSum = s["mu"], s["sigmaE"], s.get("epsSum", 0.0)
+        for g, v in enumerate(s["sigmaG"]):
+            st.sigmaG[g] = v
+        pi = np.asarray(s["pi"])
+        for g in range(pi.shape[0]):
+            for k in range(pi.shape[1]):
+                st.pi[g * MAX_K + k] = pi[g, k]
+        st.iteration = int(s.get("iteration", 0))
+        self._check(self.lib.brr_set_state(self.h, C.byref(st)))
+
+    def timing(self):
+        sw, tot, r = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self.lib.brr_get_timing(self.h, C.byref(sw), C.byref(tot), C.byref(r)))
+        return sw.value, tot.value, r.value

@@ -1,0 +1,158 @@
+/*
+ * libbrr_gpu.so — C ABI of the GB300 (sm_103a) BayesR Gibbs-sweep path.
+ *
+ * One context = one Markov chain on one GPU.  Calls on a context are not
+ * re-entrant; every function returns an int status (BRR_OK = 0, negative on
+ * error) and brr_last_error() returns a message for the calling thread.
+ * No C++ exception crosses this boundary and no torch type appears in it.
+ *
+ * Reference interfaces replaced (paths inside the BayesRRcmd project):
+ *   brr_pack_bed          PreprocessGraph::preprocessBedFile + the per-genotype
+ *                         MarkerBuilder::initialise/processAllele/endColumn/build
+ *                         calls (src/preprocessgraph.cpp:10-73, :152-244;
+ *                         src/markerbuilder.h:11-42;
+ *                         src/densemarkerbuilder.cpp:6-60;
+ *                         src/raggedsparsemarkerbuilder.cpp:5-55)
+ *   brr_get_marker_table  the per-marker statistics of the built Marker objects
+ *                         (DenseMarker::Cx values; SparseMarker mean/sd/sqrdZ/Zsum,
+ *                         src/densemarker.h:7-20, src/sparsemarker.h:6-18)
+ *   brr_get_ragged_lists  RaggedSparseMarker::Zones/Ztwos/Zmissing
+ *                         (src/raggedsparsemarker.h:7-23)
+ *   brr_set_phenotype     Data::readPhenotypeFile result + BayesRBase::init's
+ *                         standardisation (src/data.cpp:334-365,
+ *                         src/BayesRBase.cpp:85-90)
+ *   brr_set_groups        Data::readGroupFile result (src/data.cpp:424-453)
+ *   brr_init_chain        BayesRBase::init (src/BayesRBase.cpp:39-99)
+ *   brr_iterate           one pass of the BayesRBase::runGibbs chain loop body
+ *                         (src/BayesRBase.cpp:186-247), i.e. updateMu,
+ *                         prepareForAnylsis, the shuffle, AnalysisGraph::exec
+ *                         (-> BayesRBase::processColumn -> BayesRKernel::computeNum /
+ *                         calculateEpsilonChange for every marker) and the
+ *                         sigmaE / sigmaG / pi draws
+ *   brr_sweep             AnalysisGraph::exec(analysis, N, M, markerIndices)
+ *                         alone (src/analysisgraph.hpp:18-21,
+ *                         src/sequential.cpp:10-27, src/limitsequencegraph.cpp:79-106)
+ *                         with caller-supplied per-marker draws
+ *   brr_get_state /       the BayesRBase members written to the sample file
+ *   brr_set_state         (src/BayesRBase.hpp:63-96, src/BayesRBase.cpp:251)
+ */
+#ifndef BRR_GPU_H
+#define BRR_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BRR_OK 0
+#define BRR_ERR_ARG -1       /* invalid argument or call order */
+#define BRR_ERR_CUDA -2      /* CUDA runtime error */
+#define BRR_ERR_OOM -3       /* device or host allocation failed */
+#define BRR_ERR_TIMEOUT -4   /* a device-side wait exceeded its limit */
+#define BRR_ERR_MARKER -5    /* a marker does not vary or is all missing */
+#define BRR_ERR_RANGE -6     /* a device value left the exchange range */
+#define BRR_ERR_STREAM -7    /* a gamma draw exceeded its attempt cap */
+#define BRR_ERR_DEVICE -8    /* no usable sm_103 device */
+
+#define BRR_KIND_DENSE 0     /* 2-bit packed genotypes, standardised on the fly */
+#define BRR_KIND_RAGGED 1    /* index lists of ones / twos / missing */
+
+#define BRR_FORM_FP64 0      /* plain FP64 sweep: the drop-in */
+#define BRR_FORM_FP32C 1     /* FP32 compensated dots and residual, FP64 refresh */
+
+#define BRR_MAX_GROUPS 64
+#define BRR_MAX_K 16
+
+typedef struct brr_config {
+    int64_t N;                 /* individuals */
+    int64_t M;                 /* markers */
+    int32_t kind;              /* BRR_KIND_* */
+    int32_t form;              /* BRR_FORM_* */
+    int32_t n_groups;          /* marker groups (>= 1) */
+    int32_t K[BRR_MAX_GROUPS]; /* mixture components per group, incl. the zero component */
+    double S[BRR_MAX_GROUPS * (BRR_MAX_K - 1)]; /* S[g*(BRR_MAX_K-1)+k]: variance ratios */
+    uint32_t seed;
+    uint32_t chain;
+    double v0E, s02E, v0G, s02G;   /* priors (reference defaults 1e-4) */
+    int32_t refresh_every;     /* FP32C: FP64 residual refresh every this many sweeps (0: never) */
+    int32_t spec_width;        /* markers resolved per grid round (0: form default) */
+    int32_t grid;              /* CTAs of the persistent sweep (0: one per SM) */
+    int32_t device;            /* CUDA device ordinal */
+} brr_config;
+
+/* Chain state; arrays are caller-owned, sized M (beta, comp, acum) and N (eps).
+ * sigmaG[g] and pi[g*BRR_MAX_K+k] are filled for g < n_groups, k < K[g]. */
+typedef struct brr_state {
+    double *beta;
+    int32_t *comp;
+    double *acum;
+    double *eps;
+    double mu;
+    double sigmaE;
+    double epsSum;             /* ragged kind: the running residual sum */
+    double sigmaG[BRR_MAX_GROUPS];
+    double pi[BRR_MAX_GROUPS * BRR_MAX_K];
+    uint32_t iteration;        /* next iteration index */
+} brr_state;
+
+/* Per-sweep statistics returned by brr_sweep (src/BayesRBase.cpp:200-202, :238). */
+typedef struct brr_sweep_out {
+    double v[BRR_MAX_GROUPS * BRR_MAX_K];  /* component counts */
+    double betasqnG[BRR_MAX_GROUPS];       /* sum of squared non-zero betas */
+    double eps_sqnorm;                     /* ||eps||^2 after the sweep */
+    double eps_sum;                        /* sum(eps) after the sweep */
+    int64_t rounds;                        /* grid rounds used by the sweep */
+} brr_sweep_out;
+
+typedef struct brr_ctx brr_ctx;
+
+const char *brr_last_error(void);
+
+int brr_ctx_create(const brr_config *cfg, brr_ctx **out);
+int brr_ctx_destroy(brr_ctx *ctx);
+
+/* Pack a PLINK SNP-major BED payload (M columns of ceil(N/4) bytes, the 3-byte
+ * magic header already removed) from host memory; the decode, genotype counts,
+ * standardisation or ragged index lists all run on the device. */
+int brr_pack_bed(brr_ctx *ctx, const uint8_t *bed, int64_t nbytes);
+/* Same, from a device pointer. */
+int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes);
+
+/* Per-marker table, M x 4 doubles.  Dense: the standardised value of each
+ * 2-bit code {0: g=2, 1: missing, 2: g=1, 3: g=0}.  Ragged: {mean, sd, sqrdZ,
+ * Zsum}.  counts (optional): M x 4 int64 {n0, n1, n2, nmissing}. */
+int brr_get_marker_table(brr_ctx *ctx, double *table, int64_t *counts);
+/* Ragged index lists in ascending individual order.  off_*: M+1 offsets;
+ * ones/twos/miss sized from the counts. */
+int brr_get_ragged_lists(brr_ctx *ctx, int64_t *off_ones, int32_t *ones,
+                         int64_t *off_twos, int32_t *twos,
+                         int64_t *off_miss, int32_t *miss);
+
+int brr_set_groups(brr_ctx *ctx, const int32_t *group);      /* M ids in 0..n_groups-1 */
+int brr_set_phenotype(brr_ctx *ctx, const float *y);         /* N values */
+int brr_init_chain(brr_ctx *ctx);
+
+/* Run n_iter iterations of the chain. */
+int brr_iterate(brr_ctx *ctx, int32_t n_iter);
+
+/* One sweep over `order` (M marker ids) with per-marker draws u, z (indexed by
+ * marker id), using the context's current mu/sigmaE/sigmaG/pi.  Host arrays. */
+int brr_sweep(brr_ctx *ctx, const uint32_t *order, const double *u, const double *z,
+              brr_sweep_out *out);
+
+int brr_get_state(brr_ctx *ctx, brr_state *st);
+int brr_set_state(brr_ctx *ctx, const brr_state *st);
+
+/* FP64 residual refresh eps = y - mu - X beta (the FP32C form also runs it
+ * every refresh_every sweeps). */
+int brr_refresh_eps(brr_ctx *ctx);
+
+/* Device time of the last brr_iterate / brr_sweep call, split into the sweep
+ * kernels and everything else, in milliseconds; rounds = grid rounds. */
+int brr_get_timing(brr_ctx *ctx, double *sweep_ms, double *total_ms, int64_t *rounds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,39 @@
+"""The oracle reproduces the committed golden fixtures bit for bit (CPU)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+S2 = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
+
+
+def load(kind):
+    return dict(np.load(GOLDEN / ("synth_dense.npz" if kind == 0 else "synth_ragged.npz")))
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_oracle_reproduces_golden(kind):
+    d = load(kind)
+    N, bed = int(d["N"]), d["bed"]
+    np.testing.assert_array_equal(O.counts(bed, N), d["counts"])
+    if kind == 0:
+        rc, t = O.marker_table_dense(bed, N)
+    else:
+        rc, t = O.ragged_stats(bed, N)
+        for name, (off, idx) in zip(("ones", "twos", "miss"), O.ragged_lists(bed, N)):
+            np.testing.assert_array_equal(off, d[f"off_{name}"])
+            np.testing.assert_array_equal(idx, d[f"idx_{name}"])
+    assert rc == 0
+    assert np.array_equal(t.view(np.uint64), d["table"].view(np.uint64))
+    ch = O.OracleChain(bed, N, d["y"], S2, kind=kind, group=d["group"], seed=int(d["seed"]))
+    for it in range(d["trace_beta"].shape[0]):
+        ch.iterate(it)
+        s = ch.state()
+        np.testing.assert_array_equal(s["beta"], d["trace_beta"][it])
+        np.testing.assert_array_equal(s["comp"], d["trace_comp"][it])
+        assert s["sigmaE"] == d["trace_sigmaE"][it]
+        np.testing.assert_array_equal(s["sigmaG"], d["trace_sigmaG"][it])
+        assert s["mu"] == d["trace_mu"][it]
