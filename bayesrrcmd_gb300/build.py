@@ -66,5 +66,34 @@ def build_gpu(verbose: bool = False) -> Path:
     return LIB
 
 
+HOST = PKG / "host"
+BINDIR = PKG / "bin"
+CLI = BINDIR / "brr"
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """Compile the `brr` command-line host (C++17) against libbrr_gpu.so."""
+    lib = build_gpu(verbose)
+    BINDIR.mkdir(exist_ok=True)
+    srcs = sorted(HOST.glob("*.cpp"))
+    deps = srcs + sorted(HOST.glob("*.h")) + [PKG.parent / "include" / "brr_gpu.h", lib]
+    if _stale(CLI, deps):
+        cxx = shutil.which("g++") or shutil.which("c++")
+        if not cxx:
+            raise RuntimeError("no C++ compiler for the brr host")
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-o", str(CLI), *map(str, srcs),
+               f"-L{LIBDIR}", "-lbrr_gpu", "-Wl,-rpath,$ORIGIN/../lib"]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of brr failed:\n{r.stdout}\n{r.stderr}")
+    return CLI
+
+
+def build_all(verbose: bool = False):
+    return build_gpu(verbose), build_cli(verbose)
+
+
 if __name__ == "__main__":
-    print(build_gpu(verbose=True))
+    print(build_all(verbose=True))

@@ -86,6 +86,9 @@ struct brr_ctx {
     int64_t *d_counts = nullptr;
     double *d_table = nullptr;
     double *d_scale = nullptr;
+    double *d_colsum = nullptr;
+    uint8_t *d_chosen = nullptr;
+    unsigned long long *d_vstat = nullptr;   // sweep statistics: counts, fixed-point square sums
     int32_t *d_roff = nullptr;          // 3 x (M*G+1)
     uint16_t *d_ridx[3] = {nullptr, nullptr, nullptr};
     int64_t rtot[3] = {0, 0, 0};
@@ -106,6 +109,7 @@ struct brr_ctx {
     double *d_part = nullptr;
     int *d_err = nullptr;
     long long *d_rounds = nullptr;
+    long long *d_prof = nullptr;        // per-phase cycles of the last sweep (CTA 0)
     uint32_t *d_nzj = nullptr;
     double *d_nzb = nullptr;
 
@@ -127,6 +131,9 @@ struct brr_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
     int64_t last_rounds = 0;
+    long long phase[6] = {0, 0, 0, 0, 0, 0};   // summed over the sweeps of the last call
+    uint64_t wait_limit_ns = 2000000000ull;
+    int phantom = 0;
 
     // permutation prepared one iteration ahead on a host thread
     std::future<void> perm_future;
@@ -147,6 +154,9 @@ void free_all(brr_ctx *c)
     cudaFree(c->d_counts);
     cudaFree(c->d_table);
     cudaFree(c->d_scale);
+    cudaFree(c->d_colsum);
+    cudaFree(c->d_chosen);
+    cudaFree(c->d_vstat);
     cudaFree(c->d_roff);
     for (auto &p : c->d_ridx)
         cudaFree(p);
@@ -169,6 +179,7 @@ void free_all(brr_ctx *c)
     cudaFree(c->d_part);
     cudaFree(c->d_err);
     cudaFree(c->d_rounds);
+    cudaFree(c->d_prof);
     cudaFree(c->d_nzj);
     cudaFree(c->d_nzb);
     cudaFreeHost(c->h_order);
@@ -182,7 +193,7 @@ void free_all(brr_ctx *c)
 }
 
 constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
-constexpr size_t kAccWords = 3 * kMaxSpec * 2;
+constexpr size_t kAccWords = 3 * kMaxSpec * 4;
 
 // Per-group sampler constants for the current sigmaE, sigmaG, pi
 // (src/BayesRBase.cpp:309-333): c_k = log(pi_k) - log(sigmaG/sigmaE*(N-1)*cVa_k + 1)/2,
@@ -259,7 +270,7 @@ int download_eps(brr_ctx *c, double *eps_host)
 }
 
 // One sweep over the order already in d_order with draws in d_u/d_z.
-int run_sweep(brr_ctx *c, double mu_new, brr_sweep_out *out, float *sweep_ms)
+int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, float *sweep_ms)
 {
     const brr_config &cf = c->cfg;
     std::vector<double> gc;
@@ -268,7 +279,7 @@ int run_sweep(brr_ctx *c, double mu_new, brr_sweep_out *out, float *sweep_ms)
     BRR_CUDA(cudaMemcpyAsync(c->d_gconst, gc.data(), sizeof(double) * gc.size(), cudaMemcpyHostToDevice, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->d_gK, gK.data(), sizeof(int32_t) * gK.size(), cudaMemcpyHostToDevice, c->st));
     BRR_CUDA(launch_gather(cf.form, cf.kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u, c->d_z,
-                           c->d_group, c->d_rec, c->st));
+                           c->d_group, c->d_colsum, c->d_rec, c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + 1), c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
 
@@ -278,6 +289,9 @@ int run_sweep(brr_ctx *c, double mu_new, brr_sweep_out *out, float *sweep_ms)
     a.G = c->G;
     a.B = c->B;
     a.n_groups = cf.n_groups;
+    a.kmax = 0;
+    for (int g = 0; g < cf.n_groups; ++g)
+        a.kmax = std::max(a.kmax, cf.K[g]);
     a.slot_bytes = c->slot_bytes;
     a.slice_max = c->slice_max;
     a.slice_lo = c->d_slice_lo;
@@ -299,13 +313,17 @@ int run_sweep(brr_ctx *c, double mu_new, brr_sweep_out *out, float *sweep_ms)
     a.eps_lo = c->d_eps_lo;
     a.mu_new = mu_new;
     a.epsSum = c->epsSum;
+    a.eps_total = eps_total;
+    a.chosen = c->d_chosen;
     a.acc = c->d_acc;
     a.counter = c->d_acc + kAccWords;
     a.stats_out = c->d_stats;
     a.part = c->d_part;
     a.err = c->d_err;
     a.rounds_out = c->d_rounds;
-    a.timeout_ns = 2000000000ull;
+    a.prof = c->d_prof;
+    a.timeout_ns = c->wait_limit_ns;
+    a.phantom = c->phantom;
     const size_t smem = sweep_smem_bytes(cf.form, cf.kind, a);
 
     BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
@@ -313,21 +331,27 @@ int run_sweep(brr_ctx *c, double mu_new, brr_sweep_out *out, float *sweep_ms)
     BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
 
     const int ng = cf.n_groups;
-    const size_t nstats = (size_t)ng * kMaxK + ng + 1;
-    BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double) * nstats, cudaMemcpyDeviceToHost, c->st));
+    BRR_CUDA(launch_sweep_stats(cf.M, c->d_group, c->d_comp, c->d_chosen, c->d_beta, ng, c->d_vstat, c->st));
+    const size_t nv = (size_t)ng * kMaxK + 2 * ng;
+    std::vector<unsigned long long> vstat(nv);
+    BRR_CUDA(cudaMemcpyAsync(vstat.data(), c->d_vstat, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, c->st));
+    BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->h_part, c->d_part, sizeof(double) * 2 * c->G, cudaMemcpyDeviceToHost, c->st));
-    long long rounds = 0;
+    long long rounds = 0, prof[6];
     BRR_CUDA(cudaMemcpyAsync(&rounds, c->d_rounds, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+    BRR_CUDA(cudaMemcpyAsync(prof, c->d_prof, sizeof(prof), cudaMemcpyDeviceToHost, c->st));
     const int rc = check_device_status(c);
     if (rc)
         return rc;
     BRR_CUDA(cudaEventElapsedTime(sweep_ms, c->ev[0], c->ev[1]));
+    for (int k = 0; k < 6; ++k)
+        c->phase[k] += prof[k];
 
     for (int g = 0; g < ng; ++g)
         for (int k = 0; k < BRR_MAX_K; ++k)
-            out->v[g * BRR_MAX_K + k] = k < kMaxK ? c->h_stats[g * kMaxK + k] : 0.0;
+            out->v[g * BRR_MAX_K + k] = k < kMaxK ? (double)vstat[g * kMaxK + k] : 0.0;
     for (int g = 0; g < ng; ++g)
-        out->betasqnG[g] = c->h_stats[(size_t)ng * kMaxK + g];
+        out->betasqnG[g] = fx_join((long long)vstat[(size_t)ng * kMaxK + 2 * g], vstat[(size_t)ng * kMaxK + 2 * g + 1]);
     double s1 = 0.0, s2 = 0.0;
     for (int s = 0; s < c->G; ++s) {
         s1 += c->h_part[2 * s];
@@ -337,7 +361,7 @@ int run_sweep(brr_ctx *c, double mu_new, brr_sweep_out *out, float *sweep_ms)
     out->eps_sqnorm = s2;
     out->rounds = rounds;
     if (cf.kind == BRR_KIND_RAGGED)
-        c->epsSum = c->h_stats[(size_t)ng * kMaxK + ng];
+        c->epsSum = c->h_stats[0];
     c->sweeps += 1;
     return BRR_OK;
 }
@@ -529,13 +553,15 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     if (!c.d_codes) {
         if (dalloc(&c.d_codes, (size_t)(M * c.col_stride)) != cudaSuccess || dalloc(&c.d_counts, (size_t)M * 4) ||
             dalloc(&c.d_table, (size_t)M * 4) || dalloc(&c.d_scale, (size_t)M * 2) ||
+            dalloc(&c.d_colsum, (size_t)M) || dalloc(&c.d_chosen, (size_t)M) ||
+            dalloc(&c.d_vstat, (size_t)cf.n_groups * kMaxK + 2 * cf.n_groups) ||
             dalloc(&c.d_slice_lo, (size_t)c.G + 1) || dalloc(&c.d_beta, (size_t)M) || dalloc(&c.d_comp, (size_t)M) ||
             dalloc(&c.d_acum, (size_t)M) || dalloc(&c.d_order, (size_t)M) || dalloc(&c.d_u, (size_t)M) ||
             dalloc(&c.d_z, (size_t)M) || dalloc(&c.d_rec, (size_t)M) || dalloc(&c.d_acc, kAccWords + 1) ||
             dalloc(&c.d_gconst, (size_t)cf.n_groups * kMaxK * 4) || dalloc(&c.d_gK, (size_t)cf.n_groups) ||
             dalloc(&c.d_stats, (size_t)cf.n_groups * kMaxK + cf.n_groups + 1) ||
             dalloc(&c.d_part, (size_t)std::max(2 * c.G, kPartBlocks)) || dalloc(&c.d_err, 1) ||
-            dalloc(&c.d_rounds, 1) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
+            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 6) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
             dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M))
             return fail(BRR_ERR_OOM, "device allocation failed");
         if (cf.form == BRR_FORM_FP64) {
@@ -561,7 +587,7 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     const int big = INT_MAX;
     cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
     if (cf.kind == BRR_KIND_DENSE) {
-        BRR_CUDA(launch_dense_tables(c.d_counts, cf.N, M, c.d_table, c.d_scale, d_bad, c.st));
+        BRR_CUDA(launch_dense_tables(c.d_counts, cf.N, M, c.d_table, c.d_scale, c.d_colsum, d_bad, c.st));
     } else {
         BRR_CUDA(launch_ragged_stats(c.d_counts, cf.N, M, c.d_table, d_bad, c.st));
     }
@@ -763,6 +789,7 @@ int brr_iterate(brr_ctx *ctx, int32_t n_iter)
     const double Nd = (double)N;
     double sweep_total = 0.0;
     int64_t rounds_total = 0;
+    std::memset(c.phase, 0, sizeof(c.phase));
     BRR_CUDA(cudaEventRecord(c.ev[2], c.st));
     if (c.perm_next_it != c.iteration)
         schedule_permutation(&c, c.iteration);
@@ -776,14 +803,13 @@ int brr_iterate(brr_ctx *ctx, int32_t n_iter)
         // updateMu (dense src/DenseBayesRRmz.cpp:36-42, ragged src/SparseBayesRRG.cpp:106-113)
         const double old_mu = c.mu;
         BRR_CUDA(launch_mu_prep(cf.form, N, old_mu, c.d_eps, c.d_eps_hi, c.d_eps_lo, c.d_part, kPartBlocks, c.st));
-        double mean;
+        double mean, esum = 0.0;
         if (cf.kind == BRR_KIND_DENSE) {
             BRR_CUDA(cudaMemcpyAsync(c.h_part, c.d_part, sizeof(double) * kPartBlocks, cudaMemcpyDeviceToHost, c.st));
             BRR_CUDA(cudaStreamSynchronize(c.st));
-            double s = 0.0;
             for (int b = 0; b < kPartBlocks; ++b)
-                s += c.h_part[b];
-            mean = s / Nd;
+                esum += c.h_part[b];
+            mean = esum / Nd;
         } else {
             c.epsSum += old_mu * Nd;
             mean = c.epsSum / Nd;
@@ -801,7 +827,7 @@ int brr_iterate(brr_ctx *ctx, int32_t n_iter)
 
         brr_sweep_out so{};
         float ms = 0.f;
-        int rc = run_sweep(&c, c.mu, &so, &ms);
+        int rc = run_sweep(&c, c.mu, esum - c.mu * Nd, &so, &ms);
         if (rc)
             return rc;
         sweep_total += ms;
@@ -838,8 +864,18 @@ int brr_sweep(brr_ctx *ctx, const uint32_t *order, const double *u, const double
     BRR_CUDA(cudaMemcpyAsync(c.d_u, u, sizeof(double) * M, cudaMemcpyHostToDevice, c.st));
     BRR_CUDA(cudaMemcpyAsync(c.d_z, z, sizeof(double) * M, cudaMemcpyHostToDevice, c.st));
     BRR_CUDA(cudaEventRecord(c.ev[2], c.st));
+    std::memset(c.phase, 0, sizeof(c.phase));
+    double esum = 0.0;
+    if (c.cfg.kind == BRR_KIND_DENSE) {
+        // current residual total (adding zero leaves the residual unchanged)
+        BRR_CUDA(launch_mu_prep(c.cfg.form, c.cfg.N, 0.0, c.d_eps, c.d_eps_hi, c.d_eps_lo, c.d_part, kPartBlocks, c.st));
+        BRR_CUDA(cudaMemcpyAsync(c.h_part, c.d_part, sizeof(double) * kPartBlocks, cudaMemcpyDeviceToHost, c.st));
+        BRR_CUDA(cudaStreamSynchronize(c.st));
+        for (int b = 0; b < kPartBlocks; ++b)
+            esum += c.h_part[b];
+    }
     float ms = 0.f;
-    const int rc = run_sweep(&c, 0.0, out, &ms);
+    const int rc = run_sweep(&c, 0.0, esum, out, &ms);
     if (rc)
         return rc;
     BRR_CUDA(cudaEventRecord(c.ev[3], c.st));
@@ -920,6 +956,73 @@ int brr_get_timing(brr_ctx *ctx, double *sweep_ms, double *total_ms, int64_t *ro
         *total_ms = ctx->last_total_ms;
     if (rounds)
         *rounds = ctx->last_rounds;
+    return BRR_OK;
+}
+
+int brr_synth_bed_device(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
+                         double missing)
+{
+    if (!d_bed || N < 2 || M < 1 || !(p_lo > 0.0) || !(p_hi <= 0.5) || !(p_lo <= p_hi) || !(missing >= 0.0) ||
+        !(missing < 0.5))
+        return fail(BRR_ERR_ARG, "invalid synthetic genotype parameters");
+    BRR_CUDA(launch_synth_bed(d_bed, N, M, seed, p_lo, p_hi, missing, 0));
+    BRR_CUDA(cudaDeviceSynchronize());
+    return BRR_OK;
+}
+
+int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, double *out)
+{
+    if (!ctx || !ctx->packed || (n > 0 && (!idx || !b)) || !out || n < 0 || n > ctx->cfg.M)
+        return fail(BRR_ERR_ARG, "pack markers first; idx/b/out required");
+    brr_ctx &c = *ctx;
+    const int64_t N = c.cfg.N;
+    for (int64_t q = 0; q < n; ++q)
+        if (idx[q] >= (uint32_t)c.cfg.M)
+            return fail(BRR_ERR_ARG, "marker index out of range");
+    BRR_CUDA(cudaSetDevice(c.dev));
+    double *zero = nullptr, *res = nullptr;
+    if (dalloc(&zero, (size_t)N) || dalloc(&res, (size_t)N)) {
+        cudaFree(zero);
+        return fail(BRR_ERR_OOM, "device allocation failed");
+    }
+    int rc = BRR_OK;
+    cudaError_t e = cudaMemsetAsync(zero, 0, sizeof(double) * N, c.st);
+    if (e == cudaSuccess && n > 0)
+        e = cudaMemcpyAsync(c.d_nzj, idx, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c.st);
+    if (e == cudaSuccess && n > 0)
+        e = cudaMemcpyAsync(c.d_nzb, b, sizeof(double) * n, cudaMemcpyHostToDevice, c.st);
+    if (e == cudaSuccess)
+        e = launch_refresh(BRR_FORM_FP64, c.cfg.kind, N, zero, 0.0, c.d_codes, c.col_stride, c.d_table, c.d_nzj,
+                           c.d_nzb, n, res, nullptr, nullptr, c.st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, res, sizeof(double) * N, cudaMemcpyDeviceToHost, c.st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c.st);
+    if (e != cudaSuccess)
+        rc = fail(BRR_ERR_CUDA, cudaGetErrorString(e));
+    cudaFree(zero);
+    cudaFree(res);
+    if (rc == BRR_OK)
+        for (int64_t i = 0; i < N; ++i)
+            out[i] = -out[i];
+    return rc;
+}
+
+int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arrivals)
+{
+    if (!ctx || timeout_ns == 0 || phantom_arrivals < 0)
+        return fail(BRR_ERR_ARG, "invalid wait limit");
+    ctx->wait_limit_ns = timeout_ns;
+    ctx->phantom = phantom_arrivals;
+    return BRR_OK;
+}
+
+int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles)
+{
+    if (!ctx || !cycles)
+        return fail(BRR_ERR_ARG, "null argument");
+    for (int k = 0; k < 6; ++k)
+        cycles[k] = ctx->phase[k];
     return BRR_OK;
 }
 

@@ -65,24 +65,78 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Exact split of an FP64 value into two integers on fixed grids 2^-20 and
-// 2^-60, so that a sum over CTAs is an exact, order-independent integer sum.
-// Valid for |p| < 2^41; returns false otherwise.
-__device__ __forceinline__ bool fixed_split(double p, long long *hi, long long *lo)
+// Exact fixed-point exchange.  A partial sum is converted with integer
+// operations only into a 128-bit integer X = value * 2^60 (truncated below
+// 2^-60), split as X = hi * 2^56 + lo with 0 <= lo < 2^56, and the two words
+// are added with 64-bit integer atomics: the sum over CTAs is exact and does
+// not depend on the order of arrival.  Values must satisfy |value| < 2^41.
+struct Fx {
+    long long hi;
+    unsigned long long lo;
+};
+
+__device__ __forceinline__ bool fx_from_double(double p, __int128 &x)
 {
-    if (!(fabs(p) < 2199023255552.0))
+    const unsigned long long b = (unsigned long long)__double_as_longlong(p);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) {            // zero or subnormal: below the grid
+        x = 0;
+        return true;
+    }
+    if (e >= 1023 + 41)      // out of range (also inf / nan)
         return false;
-    const double ph = rint(p * 1048576.0);
-    const double rem = p - ph * (1.0 / 1048576.0);
-    const double pl = rint(rem * 1152921504606846976.0);
-    *hi = (long long)ph;
-    *lo = (long long)pl;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = e - 1015; // value * 2^60 = m * 2^(e - 1075 + 60)
+    __int128 v;
+    if (sh >= 0)
+        v = (__int128)m << sh;
+    else if (sh > -64)
+        v = (__int128)(m >> (-sh));
+    else
+        v = 0;
+    x = (b >> 63) ? -v : v;
     return true;
 }
 
-__device__ __forceinline__ double fixed_join(long long hi, long long lo)
+__device__ __forceinline__ bool fx_from_float(float f, __int128 &x)
 {
-    return (double)hi * (1.0 / 1048576.0) + (double)lo * (1.0 / 1152921504606846976.0);
+    const unsigned b = __float_as_uint(f);
+    const int e = (int)((b >> 23) & 0xFF);
+    if (e == 0) {
+        x = 0;
+        return true;
+    }
+    if (e >= 127 + 41)
+        return false;
+    const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
+    const int sh = e - 90;   // value * 2^60 = m * 2^(e - 150 + 60)
+    __int128 v;
+    if (sh >= 0)
+        v = (__int128)m << sh;
+    else if (sh > -64)
+        v = (__int128)(m >> (-sh));
+    else
+        v = 0;
+    x = (b >> 31) ? -v : v;
+    return true;
+}
+
+__device__ __forceinline__ Fx fx_split(__int128 x)
+{
+    Fx f;
+    f.lo = (unsigned long long)(x & (((__int128)1 << 56) - 1));
+    f.hi = (long long)(x >> 56);
+    return f;
+}
+
+// sum = hi * 2^-4 + lo * 2^-60 with lo < 2^64, evaluated with exact partial
+// conversions and two roundings.
+__host__ __device__ __forceinline__ double fx_join(long long hi, unsigned long long lo)
+{
+    const double a = (double)hi * 0.0625;
+    const double b = (double)(lo >> 32) * 3.7252902984619140625e-09;      // 2^-28
+    const double c = (double)(lo & 0xFFFFFFFFull) * 8.673617379884035e-19; // 2^-60
+    return a + (b + c);
 }
 
 // Error-free transformation a + b = s + e (Knuth TwoSum).

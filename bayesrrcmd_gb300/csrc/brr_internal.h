@@ -13,7 +13,7 @@ namespace brr {
 // persistent kernel streams them contiguously.  t[] holds the marker table
 // in the layout the sweep form needs:
 //   FP64 dense : standardised value per 2-bit code (4 doubles)
-//   FP32C dense: {sigma, colmean, value of a missing genotype, 0}
+//   FP32C dense: {sigma, colmean, value of a missing genotype, column sum}
 //   ragged     : {mean, sd, sqrdZ, Zsum}
 struct alignas(16) SweepRec {
     double t[4];
@@ -30,6 +30,7 @@ struct SweepArgs {
     int G;                       // CTAs (slices of individuals)
     int B;                       // markers resolved per grid round
     int n_groups;
+    int kmax;                    // largest mixture size over the groups
     int slot_bytes;              // bytes of one ring slot (max slice code bytes)
     int slice_max;               // max individuals of a slice (multiple of 64)
     const int32_t *slice_lo;     // G+1 slice boundaries in individuals
@@ -47,20 +48,24 @@ struct SweepArgs {
     float *eps_hi, *eps_lo;      // double-float residual (FP32C form)
     double mu_new;               // subtracted from eps while it is loaded (updateMu, second half)
     double epsSum;               // ragged running sum at sweep start (after updateMu)
-    unsigned long long *acc;     // [3][kMaxSpec][2] fixed-point accumulators
+    double eps_total;            // dense FP32C: sum of the residual at sweep start (after updateMu)
+    unsigned long long *acc;     // [3][kMaxSpec][4] fixed-point accumulators (sum, missing sum)
     unsigned long long *counter; // grid round counter, zero at launch
-    double *stats_out;           // v[n_groups*kMaxK], betasqnG[n_groups], epsSum_end
+    double *stats_out;           // [0]: ragged running sum at sweep end
+    uint8_t *chosen;             // M flags: marker chose a component in this sweep
     double *part;                // [G][2] per-slice sum(eps), sum(eps^2) after the sweep
     int *err;                    // device status word
     long long *rounds_out;
+    long long *prof;             // optional: cycles per round phase of CTA 0 (diagnostics), or null
     uint64_t timeout_ns;         // limit of any single wait
+    int phantom;                 // extra arrivals the barrier waits for (tests of the timeout path)
 };
 
 // Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).
 cudaError_t launch_pack_counts(const uint8_t *bed, int64_t N, int64_t M, uint8_t *codes,
                                int64_t col_stride, int64_t *counts, cudaStream_t st);
 cudaError_t launch_dense_tables(const int64_t *counts, int64_t N, int64_t M, double *lut,
-                                double *scale, int *bad, cudaStream_t st);
+                                double *scale, double *colsum, int *bad, cudaStream_t st);
 cudaError_t launch_ragged_stats(const int64_t *counts, int64_t N, int64_t M, double *stats,
                                 int *bad, cudaStream_t st);
 cudaError_t launch_ragged_slice_counts(const uint8_t *codes, int64_t col_stride, int64_t M, int G,
@@ -74,13 +79,17 @@ cudaError_t launch_draws(uint32_t seed, uint32_t chain, uint32_t it, int64_t M, 
                          cudaStream_t st);
 cudaError_t launch_gather(int form, int kind, const uint32_t *order, int64_t M, const double *table,
                           const double *scale, const double *beta, const double *u, const double *z,
-                          const int32_t *group, SweepRec *rec, cudaStream_t st);
+                          const int32_t *group, const double *colsum, SweepRec *rec, cudaStream_t st);
+cudaError_t launch_sweep_stats(int64_t M, const int32_t *group, const int32_t *comp, const uint8_t *chosen,
+                               const double *beta, int n_groups, unsigned long long *out, cudaStream_t st);
 cudaError_t launch_mu_prep(int form, int64_t N, double mu_old, double *eps, float *eps_hi,
                            float *eps_lo, double *part, int nblocks, cudaStream_t st);
 cudaError_t launch_refresh(int form, int kind, int64_t N, const double *ystd, double mu,
                            const uint8_t *codes, int64_t col_stride, const double *table,
                            const uint32_t *nz_j, const double *nz_beta, int64_t n_nz, double *eps,
                            float *eps_hi, float *eps_lo, cudaStream_t st);
+cudaError_t launch_synth_bed(uint8_t *out, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
+                             double miss, cudaStream_t st);
 cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st);
 size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a);
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem);

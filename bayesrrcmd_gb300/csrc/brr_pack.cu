@@ -8,6 +8,7 @@
 // the standardisation table or ragged statistics are derived from the counts.
 #include "brr_device.cuh"
 #include "brr_internal.h"
+#include "brr_stream.h"
 
 namespace brr {
 
@@ -77,7 +78,8 @@ __global__ void __launch_bounds__(kThreads) k_pack_counts(const uint8_t *__restr
 // squared norm follow from the counts; every operation is a separately rounded
 // IEEE operation so the table is bit-identical to the CPU restatement.
 __global__ void k_dense_tables(const int64_t *__restrict__ counts, int64_t N, int64_t M,
-                               double *__restrict__ lut, double *__restrict__ scale, int *bad)
+                               double *__restrict__ lut, double *__restrict__ scale, double *__restrict__ colsum,
+                               int *bad)
 {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= M)
@@ -107,6 +109,9 @@ __global__ void k_dense_tables(const int64_t *__restrict__ counts, int64_t N, in
     lut[4 * j + 3] = __dmul_rn(c0, sigma);
     scale[2 * j + 0] = sigma;
     scale[2 * j + 1] = colmean;
+    // sum of the standardised column (zero up to rounding)
+    colsum[j] = (double)n0 * lut[4 * j + 3] + (double)n1 * lut[4 * j + 2] + (double)n2 * lut[4 * j + 0] +
+                (double)nm * lut[4 * j + 1];
 }
 
 // Ragged statistics (src/sparsemarker.cpp:8-19, src/raggedsparsemarkerbuilder.cpp:43-55):
@@ -266,10 +271,10 @@ cudaError_t launch_pack_counts(const uint8_t *bed, int64_t N, int64_t M, uint8_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_dense_tables(const int64_t *counts, int64_t N, int64_t M, double *lut, double *scale, int *bad,
-                                cudaStream_t st)
+cudaError_t launch_dense_tables(const int64_t *counts, int64_t N, int64_t M, double *lut, double *scale,
+                                double *colsum, int *bad, cudaStream_t st)
 {
-    k_dense_tables<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(counts, N, M, lut, scale, bad);
+    k_dense_tables<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(counts, N, M, lut, scale, colsum, bad);
     return cudaGetLastError();
 }
 
@@ -304,6 +309,61 @@ cudaError_t launch_ragged_fill(const uint8_t *codes, int64_t col_stride, int64_t
     const int blocks = (int)imin64(M, 152 * 16);
     k_ragged_fill<<<blocks, kThreads, 0, st>>>(codes, col_stride, M, G, slice_lo, off0, off1, off2, idx0, idx1,
                                                idx2);
+    return cudaGetLastError();
+}
+
+}  // namespace brr
+
+namespace brr {
+
+// Seeded synthetic genotypes written directly as a BED payload: marker j has
+// allele frequency p_j = p_lo + (p_hi - p_lo) * U, genotypes are two
+// Bernoulli(p_j) draws, missing at rate `miss`.  Every byte is a function of
+// (seed, j, byte index) through the same Philox stream as the sampler.
+__global__ void k_synth_bed(uint8_t *__restrict__ out, int64_t N, int64_t M, uint32_t seed, double p_lo,
+                            double p_hi, double miss)
+{
+    const int64_t cb = (N + 3) >> 2;
+    for (int64_t j = blockIdx.x; j < M; j += gridDim.x) {
+        const U4 pb = philox4x32_10((uint32_t)j, 0u, 9u, 0u, seed, 0x5EEDu);
+        const float p = (float)(p_lo + (p_hi - p_lo) * u53(pb.x, pb.y));
+        const uint32_t t1 = (uint32_t)fminf(4294967040.f, p * 4294967296.f);
+        const uint32_t tm = (uint32_t)fminf(4294967040.f, (float)miss * 4294967296.f);
+        for (int64_t b = threadIdx.x; b < cb; b += blockDim.x) {
+            const U4 r = philox4x32_10((uint32_t)j, (uint32_t)b, 10u, 0u, seed, 0x5EEDu);
+            const U4 q = philox4x32_10((uint32_t)j, (uint32_t)b, 11u, 0u, seed, 0x5EEDu);
+            const uint32_t ra[4] = {r.x, r.y, r.z, r.w};
+            const uint32_t qa[4] = {q.x, q.y, q.z, q.w};
+            unsigned byte = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                // two allele draws from the two halves of one 32-bit word (16 bits each)
+                const unsigned a1 = (ra[k] & 0xFFFFu) < (t1 >> 16);
+                const unsigned a2 = (ra[k] >> 16) < (t1 >> 16);
+                const unsigned gv = a1 + a2;
+                unsigned code = gv == 2 ? 0u : (gv == 1 ? 2u : 3u);
+                if (qa[k] < tm)
+                    code = 1u;
+                if (b * 4 + k >= N)
+                    code = 0u;
+                byte |= code << (2 * k);
+            }
+            out[j * cb + b] = (uint8_t)byte;
+        }
+        // keep every marker polymorphic: individual 0 heterozygous, 1 homozygous
+        if (threadIdx.x == 0 && N >= 2) {
+            unsigned v = out[j * cb];
+            v = (v & ~0x0Fu) | 2u | (3u << 2);
+            out[j * cb] = (uint8_t)v;
+        }
+    }
+}
+
+cudaError_t launch_synth_bed(uint8_t *out, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
+                             double miss, cudaStream_t st)
+{
+    const int blocks = (int)imin64(M, 152 * 32);
+    k_synth_bed<<<blocks, kThreads, 0, st>>>(out, N, M, seed, p_lo, p_hi, miss);
     return cudaGetLastError();
 }
 

@@ -40,7 +40,8 @@ __global__ void k_draws(uint32_t seed, uint32_t chain, uint32_t it, int64_t M, d
 __global__ void k_gather(int form, int kind, const uint32_t *__restrict__ order, int64_t M,
                          const double *__restrict__ table, const double *__restrict__ scale,
                          const double *__restrict__ beta, const double *__restrict__ u,
-                         const double *__restrict__ z, const int32_t *__restrict__ group, SweepRec *rec)
+                         const double *__restrict__ z, const int32_t *__restrict__ group,
+                         const double *__restrict__ colsum, SweepRec *rec)
 {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= M)
@@ -57,7 +58,7 @@ __global__ void k_gather(int form, int kind, const uint32_t *__restrict__ order,
             r.t[0] = scale[2 * j];       // sigma
             r.t[1] = scale[2 * j + 1];   // column mean
             r.t[2] = table[4 * j + 1];   // value of a missing genotype
-            r.t[3] = 0.0;
+            r.t[3] = colsum[j];          // sum of the column
         }
     } else {
         r.t[0] = table[4 * j];           // mean
@@ -211,7 +212,7 @@ __host__ __device__ inline SmemPlan make_plan(int form, int kind, int slice_max,
     return p;
 }
 
-// Team of LPM lanes inside a warp.
+// Team of LPM lanes inside a warp that computes one marker's partial dot product.
 struct Team {
     unsigned mask;
     int lane;      // lane within the team
@@ -222,31 +223,13 @@ __device__ __forceinline__ Team make_team(int lpm)
 {
     Team t;
     const int wl = threadIdx.x & 31;
-    t.lane = wl % lpm;
+    t.lane = wl & (lpm - 1);
     t.base = wl - t.lane;
     t.mask = lpm == 32 ? 0xffffffffu : (((1u << lpm) - 1u) << t.base);
     return t;
 }
 
 __device__ __forceinline__ double team_sum_d(double v, const Team &t, int lpm)
-{
-    for (int o = lpm >> 1; o > 0; o >>= 1)
-        v += __shfl_xor_sync(t.mask, v, o);
-    return v;
-}
-__device__ __forceinline__ double team_max_d(double v, const Team &t, int lpm)
-{
-    for (int o = lpm >> 1; o > 0; o >>= 1)
-        v = fmax(v, __shfl_xor_sync(t.mask, v, o));
-    return v;
-}
-__device__ __forceinline__ double team_min_d(double v, const Team &t, int lpm)
-{
-    for (int o = lpm >> 1; o > 0; o >>= 1)
-        v = fmin(v, __shfl_xor_sync(t.mask, v, o));
-    return v;
-}
-__device__ __forceinline__ float team_sum_f(float v, const Team &t, int lpm)
 {
     for (int o = lpm >> 1; o > 0; o >>= 1)
         v += __shfl_xor_sync(t.mask, v, o);
@@ -266,120 +249,104 @@ __device__ __forceinline__ double lut_select(unsigned c, double l0, double l1, d
     return (c & 2u) ? ((c & 1u) ? l3 : l2) : ((c & 1u) ? l1 : l0);
 }
 
-// Component selection for one marker by a team (src/BayesRBase.cpp:309-366).
-// Lane l evaluates components k = l, l+lpm, ...; lane 0 returns the result.
+// Component selection for one marker by one thread (src/BayesRBase.cpp:309-366).
 // logL_k = c_k + h_k*num^2 with c_k = log(pi_k) - log(sigmaG/sigmaE*(N-1)*cVa_k + 1)/2
-// and h_k = 1/(2*denom_k*sigmaE); P_k = exp(logL_k - max)/sum, zeroed where the
-// reference's 700 guards fire (any |logL_q - logL_k| > 700 over q >= 1).
+// and h_k = 1/(2*denom_k*sigmaE).  P(k) = exp(logL_k - max)/sum, zeroed where the
+// reference's 700 guards fire (any |logL_q - logL_k| > 700 over q >= 1); the
+// walk picks the first k whose cumulative probability reaches u.
+// FP32 = true evaluates the exponentials in single precision from the FP64
+// log-likelihood differences and keeps the decision only when u is further
+// than 2e-5 from every cumulative bound it was compared with (the FP32 error
+// is below 5e-6); otherwise the FP64 evaluation decides.
 struct Pick {
     int comp;       // chosen component, -1 if none
     double beta;    // new beta (beta_old when none)
     double acum0;   // P(component 0) as stored in acum
 };
 
-template <bool FP32>
-__device__ Pick pick_component(const Team &tm, int lpm, double num, double u, double z, double beta_old,
-                               const double *__restrict__ gc, int K)
+template <bool FP32, int KM>
+__device__ __forceinline__ Pick pick_marker(double num, double u, double z, double beta_old,
+                                            const double *__restrict__ gc, int K)
 {
-    constexpr int kPer = kMaxK / 4;   // components per lane when lpm >= 4
-    double L[kPer];
-    double lmax = -INFINITY, lmax1 = -INFINITY, lmin1 = INFINITY;
+    double L[KM];
     const double n2 = num * num;
 #pragma unroll
-    for (int i = 0; i < kPer; ++i) {
-        const int k = tm.lane + i * lpm;
-        L[i] = -INFINITY;
+    for (int k = 0; k < KM; ++k)
+        L[k] = k < K ? (k == 0 ? gc[0] : fma(gc[4 * k + 2], n2, gc[4 * k])) : -INFINITY;
+    double lmax = L[0], lmax1 = L[1], lmin1 = L[1];
+#pragma unroll
+    for (int k = 1; k < KM; ++k) {
         if (k < K) {
-            const double c = gc[4 * k + 0], h = gc[4 * k + 2];
-            L[i] = k == 0 ? c : fma(h, n2, c);
-            lmax = fmax(lmax, L[i]);
-            if (k >= 1) {
-                lmax1 = fmax(lmax1, L[i]);
-                lmin1 = fmin(lmin1, L[i]);
-            }
+            lmax = fmax(lmax, L[k]);
+            lmax1 = fmax(lmax1, L[k]);
+            lmin1 = fmin(lmin1, L[k]);
         }
     }
-    lmax = team_max_d(lmax, tm, lpm);
-    lmax1 = team_max_d(lmax1, tm, lpm);
-    lmin1 = team_min_d(lmin1, tm, lpm);
-
-    // probabilities
-    float pf[kPer];
-    double pd[kPer];
-    bool fallback = false;
+    // the guards of components q >= 1 can only fire when the log-likelihoods of
+    // components 1..K-1 span more than 700
+    const bool wide = lmax1 - lmin1 > 700.0;
+    const bool guard0 = (lmax1 - L[0] > 700.0) || (L[0] - lmin1 > 700.0);
+    auto guarded = [&](int k) -> bool {
+        return k == 0 ? guard0 : (wide && ((lmax1 - L[k] > 700.0) || (L[k] - lmin1 > 700.0)));
+    };
     Pick res;
     res.comp = -1;
     res.beta = beta_old;
     res.acum0 = 0.0;
+    bool decided = false;
     if (FP32) {
-        float e[kPer];
+        float e[KM];
         float es = 0.f;
 #pragma unroll
-        for (int i = 0; i < kPer; ++i) {
-            const int k = tm.lane + i * lpm;
-            e[i] = k < K ? expf((float)(L[i] - lmax)) : 0.f;
-            es += e[i];
+        for (int k = 0; k < KM; ++k) {
+            e[k] = k < K ? __expf((float)(L[k] - lmax)) : 0.f;
+            es += e[k];
         }
-        es = team_sum_f(es, tm, lpm);
-#pragma unroll
-        for (int i = 0; i < kPer; ++i) {
-            const int k = tm.lane + i * lpm;
-            const bool guard = (lmax1 - L[i] > 700.0) || (L[i] - lmin1 > 700.0);
-            pf[i] = (k < K && !guard) ? e[i] / es : 0.f;
-        }
-        // walk in FP32 on lane 0; certify the decision against the FP32 error
+        const float ies = __frcp_rn(es);
         int chosen = -1;
-        float acum = 0.f, prev = 0.f;
-        float a0 = 0.f;
-        for (int k = 0; k < K; ++k) {
-            const float pk = __shfl_sync(tm.mask, pf[k / lpm], tm.base + (k % lpm));
-            if (k == 0)
-                a0 = pk;
-            prev = acum;
-            acum = k == 0 ? pk : acum + pk;
-            if (chosen < 0 && (double)u <= (double)acum)
-                chosen = k;
-            if (chosen >= 0 && k == chosen)
-                break;
+        float acum = 0.f, prev = 0.f, a0 = 0.f;
+        const float uf = (float)u;
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+            if (k < K && chosen < 0) {
+                const float pk = guarded(k) ? 0.f : e[k] * ies;
+                if (k == 0)
+                    a0 = pk;
+                prev = acum;
+                acum += pk;
+                if (uf <= acum)
+                    chosen = k;
+            }
         }
         const float tol = 2e-5f;
-        bool close;
-        if (chosen >= 0)
-            close = ((float)u > acum - tol) || (chosen > 0 && (float)u < prev + tol);
-        else
-            close = (float)u < acum + tol;
-        fallback = __shfl_sync(tm.mask, close ? 1 : 0, tm.base) != 0;
-        if (!fallback) {
+        const bool close = chosen >= 0 ? ((uf > acum - tol) || (chosen > 0 && uf < prev + tol)) : (uf < acum + tol);
+        if (!close) {
             res.comp = chosen;
             res.acum0 = (double)a0;
+            decided = true;
         }
     }
-    if (!FP32 || fallback) {
-        double e[kPer];
+    if (!decided) {
+        double e[KM];
         double es = 0.0;
 #pragma unroll
-        for (int i = 0; i < kPer; ++i) {
-            const int k = tm.lane + i * lpm;
-            e[i] = k < K ? exp(L[i] - lmax) : 0.0;
-            es += e[i];
+        for (int k = 0; k < KM; ++k) {
+            e[k] = k < K ? exp(L[k] - lmax) : 0.0;
+            es += e[k];
         }
-        es = team_sum_d(es, tm, lpm);
         const double ies = 1.0 / es;
-#pragma unroll
-        for (int i = 0; i < kPer; ++i) {
-            const int k = tm.lane + i * lpm;
-            const bool guard = (lmax1 - L[i] > 700.0) || (L[i] - lmin1 > 700.0);
-            pd[i] = (k < K && !guard) ? e[i] * ies : 0.0;
-        }
         int chosen = -1;
         double acum = 0.0, a0 = 0.0;
-        for (int k = 0; k < K; ++k) {
-            const double pk = __shfl_sync(tm.mask, pd[k / lpm], tm.base + (k % lpm));
-            if (k == 0)
-                a0 = pk;
-            acum = k == 0 ? pk : acum + pk;
-            if (chosen < 0 && u <= acum)
-                chosen = k;
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+            if (k < K && chosen < 0) {
+                const double pk = guarded(k) ? 0.0 : e[k] * ies;
+                if (k == 0)
+                    a0 = pk;
+                acum += pk;
+                if (u <= acum)
+                    chosen = k;
+            }
         }
         res.comp = chosen;
         res.acum0 = a0;
@@ -394,21 +361,18 @@ __device__ Pick pick_component(const Team &tm, int lpm, double num, double u, do
 }
 
 // --------------------------------------------------------------------------
-template <int FORM, int KIND>
+template <int FORM, int KIND, int KM>
 __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double s_num[kMaxSpec];
     __shared__ double s_beta[kMaxSpec];
     __shared__ double s_acum[kMaxSpec];
     __shared__ int s_comp[kMaxSpec];
     __shared__ int s_first;
     __shared__ int s_abort;
-    __shared__ double s_scal[8];          // ragged: shift, epsSum; dense FP32C: slice sum
-    __shared__ double s_delta[8];         // update coefficients of the current round
+    __shared__ double s_scal[4];          // ragged: shift, epsSum; dense FP32C: residual total
+    __shared__ double s_delta[4];         // update coefficients of the current round
     __shared__ float s_dfl[8];            // double-float split of the update coefficients
-    __shared__ unsigned long long s_bsq[kMaxGroups][2];
-    __shared__ int s_v[kMaxGroups * kMaxK];
     __shared__ double s_red[kThreads / 32][2];
 
     const int B = a.B;
@@ -468,110 +432,113 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
             mtab[v] = (uint8_t)m;
         }
     }
-    for (int i = tid; i < kMaxGroups * kMaxK; i += kThreads)
-        s_v[i] = 0;
-    if (tid < kMaxGroups) {
-        s_bsq[tid][0] = 0ull;
-        s_bsq[tid][1] = 0ull;
-    }
     if (tid == 0) {
         s_abort = 0;
-        s_scal[0] = 0.0;        // ragged shift
-        s_scal[1] = a.epsSum;   // ragged running sum
-        s_scal[2] = 0.0;        // dense FP32C slice sum
+        s_scal[0] = 0.0;          // ragged shift
+        s_scal[1] = a.epsSum;     // ragged running sum
+        s_scal[2] = a.eps_total;  // dense FP32C: sum of the residual
     }
     __syncthreads();
 
-    // dense FP32C: slice sum of the residual (kept current across updates)
-    auto slice_sum = [&]() {
-        double s = 0.0;
-        if (FORM != kFormFP64 && KIND == kKindDense) {
-            for (int i = tid; i < ns; i += kThreads)
-                s += (double)eh[i] + (double)el[i];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                s += __shfl_xor_sync(0xffffffffu, s, o);
-            if ((tid & 31) == 0)
-                s_red[tid >> 5][0] = s;
-            __syncthreads();
-            if (tid == 0) {
-                double t = 0.0;
-                for (int q = 0; q < kThreads / 32; ++q)
-                    t += s_red[q][0];
-                s_scal[2] = t;
-            }
-            __syncthreads();
-        }
-    };
-    slice_sum();
-
-    // ---- prefetch machinery
-    int64_t rec_issued = 0, code_issued = 0;
-    auto issue_recs = [&](int64_t upto) {
-        upto = imin64(upto, a.M);
-        const int64_t n = upto - rec_issued;
-        for (int64_t e = tid; e < n * 4; e += kThreads) {
-            const int64_t q = rec_issued + e / 4;
-            const int c = (int)(e % 4);
-            cp_async16(reinterpret_cast<unsigned char *>(&ring_rec[q % R]) + 16 * c,
+    // ---- prefetch machinery (ring slots are positions modulo R, a power of two)
+    const unsigned M32 = (unsigned)a.M;
+    const unsigned Rm = (unsigned)R - 1u;
+    unsigned rec_issued = 0, code_issued = 0;
+    auto issue_recs = [&](unsigned upto) {
+        upto = min(upto, M32);
+        if (upto <= rec_issued)
+            return;
+        const unsigned n = (upto - rec_issued) * 4u;
+        for (unsigned e = tid; e < n; e += kThreads) {
+            const unsigned q = rec_issued + (e >> 2);
+            const unsigned c = e & 3u;
+            cp_async16(reinterpret_cast<unsigned char *>(&ring_rec[q & Rm]) + 16 * c,
                        reinterpret_cast<const unsigned char *>(&a.rec[q]) + 16 * c);
         }
-        rec_issued = imax64(rec_issued, upto);
+        rec_issued = upto;
     };
-    auto issue_codes = [&](int64_t upto) {
-        upto = imin64(upto, a.M);
-        const int64_t n = upto - code_issued;
+    // each thread owns one 16-byte chunk of codes of one marker per pass
+    const unsigned chunks = (unsigned)nbytes / 16u;
+    const unsigned per_pass = chunks ? (unsigned)kThreads / chunks : 0u;
+    const unsigned my_q = chunks ? (unsigned)tid / chunks : 0u;
+    const unsigned my_c = chunks ? (unsigned)tid - my_q * chunks : 0u;
+    auto issue_codes = [&](unsigned upto) {
+        upto = min(upto, M32);
+        if (upto <= code_issued)
+            return;
         if (KIND == kKindDense) {
-            const int chunks = nbytes / 16;
-            for (int64_t e = tid; e < n * chunks; e += kThreads) {
-                const int64_t q = code_issued + e / chunks;
-                const int c = (int)(e % chunks);
-                const uint32_t j = ring_rec[q % R].j;
-                cp_async16(ring_codes + (q % R) * a.slot_bytes + 16 * c,
-                           a.codes + (int64_t)j * a.col_stride + byte_lo + 16 * c);
+            if (my_q < per_pass) {
+                for (unsigned q = code_issued + my_q; q < upto; q += per_pass) {
+                    const uint32_t j = ring_rec[q & Rm].j;
+                    cp_async16(ring_codes + (q & Rm) * a.slot_bytes + 16 * my_c,
+                               a.codes + (int64_t)j * a.col_stride + byte_lo + 16 * my_c);
+                }
             }
         } else {
             // offsets of the slice's sub-lists, copied asynchronously into the ring
-            for (int64_t e = tid; e < n * 6; e += kThreads) {
-                const int64_t q = code_issued + e / 6;
-                const int k = (int)(e % 6);
-                const uint32_t j = ring_rec[q % R].j;
-                const int64_t base = (int64_t)j * a.G + sidx;
-                cp_async4(&ring_roff[(q % R) * 8 + k], &a.roff[k >> 1][base + (k & 1)]);
+            const unsigned n = (upto - code_issued) * 8u;
+            for (unsigned e = tid; e < n; e += kThreads) {
+                const unsigned q = code_issued + (e >> 3);
+                const unsigned k = e & 7u;
+                if (k < 6u) {
+                    const uint32_t j = ring_rec[q & Rm].j;
+                    const int64_t base = (int64_t)j * a.G + sidx;
+                    cp_async4(&ring_roff[(q & Rm) * 8 + k], &a.roff[k >> 1][base + (k & 1)]);
+                }
             }
         }
-        code_issued = imax64(code_issued, upto);
+        code_issued = upto;
     };
 
-    issue_recs(3 * (int64_t)B);
+    issue_recs(3u * B);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
-    issue_codes(2 * (int64_t)B);
+    issue_codes(2u * B);
     cp_async_commit();
 
+    int lpm_log2 = 0;
+    while ((1 << lpm_log2) < lpm)
+        ++lpm_log2;
     const Team tm = make_team(lpm);
-    const int team = tid / lpm;
+    const int team = tid >> lpm_log2;
     const double Nm1 = (double)(a.N - 1);
+    const bool prof = a.prof != nullptr && blockIdx.x == 0 && tid == 0;
+    long long ph[6] = {0, 0, 0, 0, 0, 0};
+    long long tp = prof ? clock64() : 0;
+    auto mark = [&](int k) {
+        if (prof) {
+            const long long t = clock64();
+            ph[k] += t - tp;
+            tp = t;
+        }
+    };
+    auto publish = [&](unsigned long long *acc, __int128 x) {
+        const Fx f = fx_split(x);
+        red_add_u64(acc, (unsigned long long)f.hi);
+        red_add_u64(acc + 1, f.lo);
+    };
 
-    int64_t start = 0;
+    unsigned start = 0;
     long long r = 0;
-    while (start < a.M) {
+    int rb = 0;   // r % 3
+    while (start < M32) {
         cp_async_wait_all();
         __syncthreads();
-        issue_codes(start + 2 * (int64_t)B);
-        issue_recs(start + 3 * (int64_t)B);
+        issue_codes(start + 2u * B);
+        issue_recs(start + 3u * B);
         cp_async_commit();
-        const int nb = (int)imin64(B, a.M - start);
+        const int nb = (int)min((unsigned)B, M32 - start);
         if (tid == 0)
             s_first = kMaxSpec;
+        mark(0);
 
-        // ---- partial dot products of this slice
+        // ---- partial dot products of this slice, published as exact fixed point
         if (team < nb) {
-            const int64_t q = start + team;
-            const int slot = (int)(q % R);
+            const unsigned slot = (start + team) & Rm;
             const SweepRec &rc = ring_rec[slot];
-            double part = 0.0;
+            unsigned long long *acc = a.acc + (rb * kMaxSpec + team) * 4;
+            bool ok = true;
             if (KIND == kKindDense) {
                 const uint8_t *cb = ring_codes + slot * a.slot_bytes;
                 if (FORM == kFormFP64) {
@@ -586,26 +553,30 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                         p = fma(lut_select((v >> 4) & 3u, l0, l1, l2, l3), e23.x, p);
                         p = fma(lut_select((v >> 6) & 3u, l0, l1, l2, l3), e23.y, p);
                     }
-                    part = team_sum_d(p, tm, lpm);
+                    p = team_sum_d(p, tm, lpm);
+                    if (tm.lane == 0) {
+                        __int128 x;
+                        ok = fx_from_double(p, x);
+                        if (ok)
+                            publish(acc, x);
+                    }
                 } else {
-                    // sum g*eps exactly per product, pairwise over the four
-                    // genotypes of a byte, Kahan across bytes; lo parts plain.
-                    float A = 0.f, cA = 0.f, sl = 0.f, mh = 0.f, ml = 0.f;
+                    // A = sum over non-missing of g*eps in double-float: the
+                    // products g*hi are exact, each is added with an
+                    // error-free TwoSum into one of two interleaved chains and
+                    // the rounding errors plus the g*lo terms are accumulated
+                    // in the low words.  Sm = sum of eps over missing genotypes.
+                    float A0 = 0.f, L0 = 0.f, A1 = 0.f, L1 = 0.f, mh = 0.f, ml = 0.f;
                     for (int b = tm.lane; b < nbytes; b += lpm) {
                         const unsigned v = cb[b];
                         const float4 g = gtab[v];
                         const float4 h = reinterpret_cast<const float4 *>(eh)[b];
                         const float4 l = reinterpret_cast<const float4 *>(el)[b];
-                        const float s4 = __fadd_rn(__fadd_rn(__fmul_rn(g.x, h.x), __fmul_rn(g.y, h.y)),
-                                                   __fadd_rn(__fmul_rn(g.z, h.z), __fmul_rn(g.w, h.w)));
-                        const float y = __fsub_rn(s4, cA);
-                        const float t2 = __fadd_rn(A, y);
-                        cA = __fsub_rn(__fsub_rn(t2, A), y);
-                        A = t2;
-                        sl = fmaf(g.x, l.x, sl);
-                        sl = fmaf(g.y, l.y, sl);
-                        sl = fmaf(g.z, l.z, sl);
-                        sl = fmaf(g.w, l.w, sl);
+                        float s, e;
+                        two_sum(A0, __fmul_rn(g.x, h.x), s, e); A0 = s; L0 = __fmaf_rn(g.x, l.x, __fadd_rn(L0, e));
+                        two_sum(A1, __fmul_rn(g.y, h.y), s, e); A1 = s; L1 = __fmaf_rn(g.y, l.y, __fadd_rn(L1, e));
+                        two_sum(A0, __fmul_rn(g.z, h.z), s, e); A0 = s; L0 = __fmaf_rn(g.z, l.z, __fadd_rn(L0, e));
+                        two_sum(A1, __fmul_rn(g.w, h.w), s, e); A1 = s; L1 = __fmaf_rn(g.w, l.w, __fadd_rn(L1, e));
                         const unsigned mm = mtab[v];
                         if (mm) {
                             if (mm & 1u) df_add(mh, ml, h.x, l.x);
@@ -614,13 +585,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                             if (mm & 8u) df_add(mh, ml, h.w, l.w);
                         }
                     }
-                    float Al = __fsub_rn(sl, cA);
-                    team_df_sum(A, Al, tm, lpm);
+                    float Ah = A0, Al = L0;
+                    df_add(Ah, Al, A1, L1);
+                    team_df_sum(Ah, Al, tm, lpm);
                     team_df_sum(mh, ml, tm, lpm);
-                    const double Ad = (double)A + (double)Al;
-                    const double Sm = (double)mh + (double)ml;
-                    const double sigma = rc.t[0], cm = rc.t[1], xm = rc.t[2];
-                    part = sigma * (Ad - cm * (s_scal[2] - Sm)) + xm * Sm;
+                    if (tm.lane == 0) {
+                        __int128 x1, x2, m1, m2;
+                        ok = fx_from_float(Ah, x1) && fx_from_float(Al, x2) && fx_from_float(mh, m1) &&
+                             fx_from_float(ml, m2);
+                        if (ok) {
+                            publish(acc, x1 + x2);
+                            if (mh != 0.f || ml != 0.f)
+                                publish(acc + 2, m1 + m2);
+                        }
+                    }
                 }
             } else {
                 const int32_t *ro = ring_roff + slot * 8;
@@ -631,7 +609,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                     double p2 = 0.0;
                     for (int e = ro[2] + tm.lane; e < ro[3]; e += lpm)
                         p2 += eps64[a.ridx[1][e]];
-                    part = team_sum_d(p + 2.0 * p2, tm, lpm);
+                    p = team_sum_d(p + 2.0 * p2, tm, lpm);
+                    if (tm.lane == 0) {
+                        __int128 x;
+                        ok = fx_from_double(p, x);
+                        if (ok)
+                            publish(acc, x);
+                    }
                 } else {
                     float h = 0.f, l = 0.f;
                     for (int e = ro[0] + tm.lane; e < ro[1]; e += lpm) {
@@ -643,28 +627,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                         df_add(h, l, 2.f * eh[i], 2.f * el[i]);
                     }
                     team_df_sum(h, l, tm, lpm);
-                    part = (double)h + (double)l;
+                    if (tm.lane == 0) {
+                        __int128 x1, x2;
+                        ok = fx_from_float(h, x1) && fx_from_float(l, x2);
+                        if (ok)
+                            publish(acc, x1 + x2);
+                    }
                 }
             }
-            if (tm.lane == 0) {
-                long long ph, pl;
-                if (!fixed_split(part, &ph, &pl)) {
-                    atomicCAS(a.err, kDevOk, kDevRange);
-                    ph = 0;
-                    pl = 0;
-                }
-                unsigned long long *acc = a.acc + ((r % 3) * kMaxSpec + team) * 2;
-                red_add_u64(acc, (unsigned long long)ph);
-                red_add_u64(acc + 1, (unsigned long long)pl);
-            }
+            if (!ok)
+                atomicCAS(a.err, kDevOk, kDevRange);
         }
         __syncthreads();
+        mark(1);
 
-        // ---- grid barrier: one counter, bounded wait
+        // ---- grid barrier: one counter; release orders this CTA's
+        // accumulator updates (ordered before it by bar.sync), acquire orders
+        // the reads below.  The wait is bounded.
         if (tid == 0) {
-            __threadfence();
             red_release_add_u64(a.counter, 1ull);
-            const unsigned long long target = (unsigned long long)a.G * (unsigned long long)(r + 1);
+            const unsigned long long target = (unsigned long long)(a.G + a.phantom) * (unsigned long long)(r + 1);
             const uint64_t t0 = global_timer_ns();
             unsigned spins = 0;
             while (ld_acquire_u64(a.counter) < target) {
@@ -676,71 +658,63 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                     }
                 }
             }
-            __threadfence();
         }
         __syncthreads();
+        mark(2);
         if (s_abort)
             break;
 
-        // ---- redundant sampling of the round's markers in every CTA
-        if (team < nb) {
-            const int64_t q = start + team;
-            const SweepRec &rc = ring_rec[q % R];
-            double tot = 0.0;
-            if (tm.lane == 0) {
-                const unsigned long long *acc = a.acc + ((r % 3) * kMaxSpec + team) * 2;
-                tot = fixed_join((long long)ld_relaxed_u64(acc), (long long)ld_relaxed_u64(acc + 1));
-            }
-            tot = __shfl_sync(tm.mask, tot, tm.base);
+        // ---- redundant sampling of the round's markers in every CTA, one thread per marker
+        if (tid < nb) {
+            const SweepRec &rc = ring_rec[(start + tid) & Rm];
+            const unsigned long long *acc = a.acc + (rb * kMaxSpec + tid) * 4;
+            const double tot = fx_join((long long)ld_relaxed_u64(acc), ld_relaxed_u64(acc + 1));
             double num;
             if (KIND == kKindDense) {
-                num = tot + rc.beta_old * Nm1;
+                if (FORM == kFormFP64) {
+                    num = tot + rc.beta_old * Nm1;
+                } else {
+                    const double sm = fx_join((long long)ld_relaxed_u64(acc + 2), ld_relaxed_u64(acc + 3));
+                    const double sigma = rc.t[0], cm = rc.t[1], xm = rc.t[2];
+                    num = (sigma * (tot - cm * (s_scal[2] - sm)) + xm * sm) + rc.beta_old * Nm1;
+                }
             } else {
                 const double mean = rc.t[0], isd = rc.t[2], Zsum = rc.t[3];
                 num = (rc.beta_old * ((double)a.N - 1.0) - mean * s_scal[1] * isd) + (tot + s_scal[0] * Zsum) * isd;
             }
             const int g = rc.group;
-            const Pick pk = pick_component<FORM != kFormFP64>(tm, lpm, num, rc.u, rc.z, rc.beta_old,
-                                                              gconst + (size_t)g * kMaxK * 4, gk[g]);
-            if (tm.lane == 0) {
-                s_num[team] = num;
-                s_beta[team] = pk.beta;
-                s_acum[team] = pk.acum0;
-                s_comp[team] = pk.comp;
-                if (rc.beta_old != 0.0 || pk.beta != 0.0)
-                    atomicMin(&s_first, team);
-            }
+            const Pick pk = pick_marker<FORM != kFormFP64, KM>(num, rc.u, rc.z, rc.beta_old,
+                                                           gconst + (size_t)g * kMaxK * 4, gk[g]);
+            s_beta[tid] = pk.beta;
+            s_acum[tid] = pk.acum0;
+            s_comp[tid] = pk.comp;
+            if (rc.beta_old != 0.0 || pk.beta != 0.0)
+                atomicMin(&s_first, tid);
         }
         __syncthreads();
+        mark(3);
 
         const int first = s_first;
         const int last = first < nb ? first : nb - 1;
         if (blockIdx.x == 0) {
-            // outputs and sweep statistics, only from CTA 0
-            if (team <= last && tm.lane == 0) {
-                const SweepRec &rc = ring_rec[(start + team) % R];
-                const int c = s_comp[team];
-                a.beta[rc.j] = s_beta[team];
-                a.acum[rc.j] = s_acum[team];
-                if (c >= 0) {
+            // outputs of the resolved markers, only from CTA 0
+            if (tid <= last) {
+                const SweepRec &rc = ring_rec[(start + tid) & Rm];
+                const int c = s_comp[tid];
+                a.beta[rc.j] = s_beta[tid];
+                a.acum[rc.j] = s_acum[tid];
+                a.chosen[rc.j] = c >= 0 ? 1 : 0;
+                if (c >= 0)
                     a.comp[rc.j] = c;
-                    atomicAdd(&s_v[rc.group * kMaxK + c], 1);
-                    if (c >= 1) {
-                        long long ph, pl;
-                        const double b = s_beta[team];
-                        fixed_split(b * b, &ph, &pl);
-                        atomicAdd(&s_bsq[rc.group][0], (unsigned long long)ph);
-                        atomicAdd(&s_bsq[rc.group][1], (unsigned long long)pl);
-                    }
-                }
             }
-            if (tid < 2 * kMaxSpec)
-                a.acc[((r + 2) % 3) * kMaxSpec * 2 + tid] = 0ull;
+            // all CTAs have read the accumulators of round r-1: recycle them
+            if (tid < 4 * kMaxSpec)
+                a.acc[((rb + 2) % 3) * kMaxSpec * 4 + tid] = 0ull;
         }
 
         // ---- apply the residual update of the first changing marker
         if (first < nb) {
-            const int slot = (int)((start + first) % R);
+            const unsigned slot = (start + first) & Rm;
             const SweepRec &rc = ring_rec[slot];
             const double dBeta = rc.beta_old - s_beta[first];
             if (KIND == kKindDense) {
@@ -761,6 +735,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                         df_from_double(d, h, l);
                         s_dfl[2 * tid] = h;
                         s_dfl[2 * tid + 1] = l;
+                    } else if (tid == 32) {
+                        // the residual total moves by dBeta times the column sum
+                        s_scal[2] = s_scal[2] + dBeta * rc.t[3];
                     }
                     __syncthreads();
                     for (int i = tid; i < ns; i += kThreads) {
@@ -770,8 +747,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                         eh[i] = h;
                         el[i] = l;
                     }
-                    __syncthreads();
-                    slice_sum();
                 }
             } else {
                 const int32_t *ro = ring_roff + slot * 8;
@@ -809,13 +784,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
             }
         }
         __syncthreads();
-        start += last + 1;
+        mark(4);
+        start += (unsigned)(last + 1);
         ++r;
+        rb = rb == 2 ? 0 : rb + 1;
+    }
+    if (prof) {
+        for (int k = 0; k < 5; ++k)
+            a.prof[k] = ph[k];
+        a.prof[5] = r;
     }
     cp_async_wait_all();
     __syncthreads();
 
-    // ---- epilogue: residual back to HBM, per-slice sums, sweep statistics
+    // ---- epilogue: residual back to HBM, per-slice sums
     double s1 = 0.0, s2 = 0.0;
     const double shift = (KIND == kKindRagged) ? s_scal[0] : 0.0;
     float shh, shl;
@@ -854,16 +836,53 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
         }
         a.part[2 * sidx] = t1;
         a.part[2 * sidx + 1] = t2;
-    }
-    if (blockIdx.x == 0) {
-        for (int i = tid; i < a.n_groups * kMaxK; i += kThreads)
-            a.stats_out[i] = (double)s_v[i];
-        if (tid < a.n_groups)
-            a.stats_out[a.n_groups * kMaxK + tid] = fixed_join((long long)s_bsq[tid][0], (long long)s_bsq[tid][1]);
-        if (tid == 0) {
-            a.stats_out[a.n_groups * kMaxK + a.n_groups] = s_scal[1];
+        if (blockIdx.x == 0) {
+            a.stats_out[0] = s_scal[1];
             *a.rounds_out = r;
         }
+    }
+}
+
+// Sweep statistics from the resolved markers (src/BayesRBase.cpp:353-355):
+// v[g][k] counts the markers that chose component k, betasqnG[g] sums the
+// squares of the non-zero betas.  Counts and the fixed-point square sums are
+// integer atomics, so the result does not depend on the order of summation.
+__global__ void __launch_bounds__(kThreads) k_sweep_stats(int64_t M, const int32_t *__restrict__ group,
+                                                          const int32_t *__restrict__ comp,
+                                                          const uint8_t *__restrict__ chosen,
+                                                          const double *__restrict__ beta, int n_groups,
+                                                          unsigned long long *__restrict__ out)
+{
+    // out: [n_groups*kMaxK] counts, then [n_groups][2] fixed-point sums
+    __shared__ unsigned long long sv[kMaxGroups * kMaxK];
+    __shared__ unsigned long long sb[kMaxGroups][2];
+    for (int i = threadIdx.x; i < n_groups * kMaxK; i += blockDim.x)
+        sv[i] = 0ull;
+    for (int i = threadIdx.x; i < n_groups; i += blockDim.x) {
+        sb[i][0] = 0ull;
+        sb[i][1] = 0ull;
+    }
+    __syncthreads();
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
+        if (!chosen[j])
+            continue;
+        const int g = group[j], c = comp[j];
+        atomicAdd(&sv[g * kMaxK + c], 1ull);
+        if (c >= 1) {
+            __int128 x;
+            fx_from_double(beta[j] * beta[j], x);
+            const Fx f = fx_split(x);
+            atomicAdd(&sb[g][0], (unsigned long long)f.hi);
+            atomicAdd(&sb[g][1], f.lo);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_groups * kMaxK; i += blockDim.x)
+        if (sv[i])
+            atomicAdd(&out[i], sv[i]);
+    for (int i = threadIdx.x; i < n_groups; i += blockDim.x) {
+        atomicAdd(&out[n_groups * kMaxK + 2 * i], sb[i][0]);
+        atomicAdd(&out[n_groups * kMaxK + 2 * i + 1], sb[i][1]);
     }
 }
 
@@ -878,9 +897,10 @@ cudaError_t launch_draws(uint32_t seed, uint32_t chain, uint32_t it, int64_t M, 
 
 cudaError_t launch_gather(int form, int kind, const uint32_t *order, int64_t M, const double *table,
                           const double *scale, const double *beta, const double *u, const double *z,
-                          const int32_t *group, SweepRec *rec, cudaStream_t st)
+                          const int32_t *group, const double *colsum, SweepRec *rec, cudaStream_t st)
 {
-    k_gather<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(form, kind, order, M, table, scale, beta, u, z, group, rec);
+    k_gather<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(form, kind, order, M, table, scale, beta, u, z, group,
+                                                          colsum, rec);
     return cudaGetLastError();
 }
 
@@ -901,44 +921,73 @@ cudaError_t launch_refresh(int form, int kind, int64_t N, const double *ystd, do
     return cudaGetLastError();
 }
 
+cudaError_t launch_sweep_stats(int64_t M, const int32_t *group, const int32_t *comp, const uint8_t *chosen,
+                               const double *beta, int n_groups, unsigned long long *out, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long) * (n_groups * kMaxK + 2 * n_groups), st);
+    if (e != cudaSuccess)
+        return e;
+    const int blocks = (int)imin64((M + kThreads - 1) / kThreads, 152);
+    k_sweep_stats<<<blocks, kThreads, 0, st>>>(M, group, comp, chosen, beta, n_groups, out);
+    return cudaGetLastError();
+}
+
 size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a)
 {
     return make_plan(form, kind, a.slice_max, a.slot_bytes, a.B, a.n_groups).total;
 }
 
-template <int FORM, int KIND>
+template <int FORM, int KIND, int KM>
 static cudaError_t launch_one(const SweepArgs &a, size_t smem, cudaStream_t st)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_sweep<FORM, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_sweep<FORM, KIND, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     SweepArgs args = a;
     void *params[] = {&args};
-    return cudaLaunchCooperativeKernel((const void *)k_sweep<FORM, KIND>, dim3(a.G), dim3(kThreads), params, smem, st);
+    return cudaLaunchCooperativeKernel((const void *)k_sweep<FORM, KIND, KM>, dim3(a.G), dim3(kThreads), params, smem,
+                                       st);
 }
 
-cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st)
+template <int KM>
+static const void *sweep_fn(int form, int kind)
+{
+    if (form == kFormFP64)
+        return kind == kKindDense ? (const void *)k_sweep<kFormFP64, kKindDense, KM>
+                                  : (const void *)k_sweep<kFormFP64, kKindRagged, KM>;
+    return kind == kKindDense ? (const void *)k_sweep<kFormFP32C, kKindDense, KM>
+                              : (const void *)k_sweep<kFormFP32C, kKindRagged, KM>;
+}
+
+template <int KM>
+static cudaError_t launch_km(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st)
 {
     if (form == kFormFP64 && kind == kKindDense)
-        return launch_one<kFormFP64, kKindDense>(a, smem, st);
+        return launch_one<kFormFP64, kKindDense, KM>(a, smem, st);
     if (form == kFormFP32C && kind == kKindDense)
-        return launch_one<kFormFP32C, kKindDense>(a, smem, st);
+        return launch_one<kFormFP32C, kKindDense, KM>(a, smem, st);
     if (form == kFormFP64 && kind == kKindRagged)
-        return launch_one<kFormFP64, kKindRagged>(a, smem, st);
-    return launch_one<kFormFP32C, kKindRagged>(a, smem, st);
+        return launch_one<kFormFP64, kKindRagged, KM>(a, smem, st);
+    return launch_one<kFormFP32C, kKindRagged, KM>(a, smem, st);
+}
+
+// Components per group up to 4 (the reference default S has three variance
+// ratios) use the 4-wide sampler; larger mixtures the 16-wide one.
+cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st)
+{
+    return a.kmax <= 4 ? launch_km<4>(form, kind, a, smem, st) : launch_km<kMaxK>(form, kind, a, smem, st);
 }
 
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem)
 {
-    int n = 0;
-    const void *f = form == kFormFP64 ? (kind == kKindDense ? (const void *)k_sweep<kFormFP64, kKindDense>
-                                                             : (const void *)k_sweep<kFormFP64, kKindRagged>)
-                                      : (kind == kKindDense ? (const void *)k_sweep<kFormFP32C, kKindDense>
-                                                            : (const void *)k_sweep<kFormFP32C, kKindRagged>);
-    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kThreads, smem) != cudaSuccess)
+    int n = 0, m = 0;
+    const void *f4 = sweep_fn<4>(form, kind), *f16 = sweep_fn<kMaxK>(form, kind);
+    cudaFuncSetAttribute(f4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(f16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f4, kThreads, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, f16, kThreads, smem) != cudaSuccess)
         return 0;
-    return n;
+    return n < m ? n : m;
 }
 
 }  // namespace brr

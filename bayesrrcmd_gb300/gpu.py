@@ -59,7 +59,8 @@ LIB_PATH = Path(__file__).resolve().parent / "lib" / "libbrr_gpu.so"
 EXPORTS = [
     "brr_last_error", "brr_ctx_create", "brr_ctx_destroy", "brr_pack_bed", "brr_pack_bed_device",
     "brr_get_marker_table", "brr_get_ragged_lists", "brr_set_groups", "brr_set_phenotype", "brr_init_chain",
-    "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing",
+    "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing", "brr_get_phase_cycles",
+    "brr_set_wait_limit", "brr_xbeta", "brr_synth_bed_device",
 ]
 
 
@@ -91,12 +92,25 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_set_state.argtypes = [P, C.POINTER(BrrState)]
     lib.brr_refresh_eps.argtypes = [P]
     lib.brr_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.brr_get_phase_cycles.argtypes = [P, C.POINTER(C.c_int64)]
+    lib.brr_set_wait_limit.argtypes = [P, C.c_uint64, C.c_int32]
+    lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
+    lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
     for name in EXPORTS:
         if name != "brr_last_error":
             getattr(lib, name).restype = C.c_int
     if path is None:
         _LIB = lib
     return lib
+
+
+def synth_bed_device(dev_ptr: int, N: int, M: int, seed: int, p_lo: float, p_hi: float, missing: float = 0.0,
+                     lib: Optional[C.CDLL] = None):
+    """Fill a device buffer of M*ceil(N/4) bytes with a seeded synthetic BED payload."""
+    lib = lib or load_library()
+    rc = lib.brr_synth_bed_device(C.c_void_p(dev_ptr), N, M, seed & 0xFFFFFFFF, p_lo, p_hi, missing)
+    if rc != 0:
+        raise BrrError(rc, lib.brr_last_error().decode())
 
 
 class BrrError(RuntimeError):
@@ -258,6 +272,22 @@ class Chain:
                 st.pi[g * MAX_K + k] = pi[g, k]
         st.iteration = int(s.get("iteration", 0))
         self._check(self.lib.brr_set_state(self.h, C.byref(st)))
+
+    def xbeta(self, idx: np.ndarray, b: np.ndarray) -> np.ndarray:
+        i = np.ascontiguousarray(idx, np.uint32)
+        bb = np.ascontiguousarray(b, np.float64)
+        out = np.zeros(self.cfg.N, np.float64)
+        self._check(self.lib.brr_xbeta(self.h, _ptr(i, C.c_uint32), _ptr(bb, C.c_double), i.size,
+                                       _ptr(out, C.c_double)))
+        return out
+
+    def set_wait_limit(self, timeout_ns: int, phantom_arrivals: int = 0):
+        self._check(self.lib.brr_set_wait_limit(self.h, int(timeout_ns), int(phantom_arrivals)))
+
+    def phase_cycles(self) -> np.ndarray:
+        out = np.zeros(6, np.int64)
+        self._check(self.lib.brr_get_phase_cycles(self.h, _ptr(out, C.c_int64)))
+        return out
 
     def timing(self):
         sw, tot, r = C.c_double(), C.c_double(), C.c_int64()

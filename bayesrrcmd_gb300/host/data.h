@@ -1,0 +1,46 @@
+// PLINK metadata, phenotype and group readers and the preprocessed-file
+// formats of the reference, for the host side of `brr`.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace brr {
+
+struct IndexEntry {          // src/common.h:57-61: one per marker in the index file
+    uint64_t pos = 0;
+    uint64_t compressedSize = 0;
+    uint64_t originalSize = 0;
+};
+
+struct Data {
+    std::vector<std::string> indIds;     // "FID:IID", src/data.cpp:85-107
+    std::vector<std::string> snpIds;     // src/data.cpp:109-133
+    std::vector<float> y;                // src/data.cpp:334-365 (NA skipped, packed)
+    std::vector<int32_t> G;              // group per marker, default 0
+    unsigned numGroups = 1;
+    int64_t numInds() const { return (int64_t)indIds.size(); }
+    int64_t numSnps() const { return (int64_t)snpIds.size(); }
+
+    void readFamFile(const std::string &famFile);        // throws std::string
+    void readBimFile(const std::string &bimFile);        // throws std::string
+    void readPhenotypeFile(const std::string &phenFile); // throws std::string
+    void readGroupFile(const std::string &groupFile);    // throws std::string
+};
+
+// SNP-major BED payload without the 3-byte magic; throws on a bad magic or size
+// (src/preprocessgraph.cpp:195-200, :36-41).
+std::vector<uint8_t> readBedPayload(const std::string &bedFile, int64_t N, int64_t M);
+
+// Preprocessed marker files (uncompressed layout of src/preprocessgraph.cpp:92-126):
+// dense records are N doubles (src/densemarker.cpp:34-49); ragged records are
+// {mean, sd, sqrdZ, Zsum} doubles then three (u64 count, int32[count]) lists
+// (src/sparsemarker.cpp:43-58, src/raggedsparsemarker.cpp:43-66).
+void writeDensePreprocessed(const std::string &ppFile, const std::string &indexFile, int64_t N, int64_t M,
+                            const double *lut, const uint8_t *bedPayload);
+void writeRaggedPreprocessed(const std::string &ppFile, const std::string &indexFile, int64_t M,
+                             const double *stats, const int64_t *off[3], const int32_t *idx[3]);
+std::vector<IndexEntry> readIndex(const std::string &indexFile, int64_t M);
+
+}  // namespace brr

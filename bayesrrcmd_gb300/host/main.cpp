@@ -1,0 +1,299 @@
+// `brr`: command-line entry of the GB300 BayesR path (the reference's
+// src/main.cpp:8-48 + AnalysisRunner::run, src/analysisrunner.cpp:278-306,
+// restricted to --preprocess and --analysis-type ppbayes over PLINK BED).
+// Compute runs in libbrr_gpu.so through the C ABI of include/brr_gpu.h.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <sstream>
+#include <vector>
+
+#include "../../include/brr_gpu.h"
+#include "data.h"
+#include "options.h"
+
+using namespace brr;
+
+namespace {
+
+void check(int rc, const char *what)
+{
+    if (rc != BRR_OK)
+        throw std::string("Error: ") + what + " failed (" + std::to_string(rc) + "): " + brr_last_error();
+}
+
+// src/analysisrunner.cpp:20-45
+void readMetaData(Data &data, const Options &opt)
+{
+    if (opt.inputType != InputType::BED)
+        throw std::string("Error: the GB300 path reads PLINK BED input (--bfile PREFIX or --data-file X.bed)");
+    data.readFamFile(fileWithSuffix(opt.dataFile, ".fam"));
+    data.readBimFile(fileWithSuffix(opt.dataFile, ".bim"));
+    if (!opt.phenotypeFile.empty())
+        data.readPhenotypeFile(opt.phenotypeFile);
+    if (!opt.groupFile.empty()) {
+        data.readGroupFile(opt.groupFile);
+        if (opt.S.size() != data.numGroups)
+            std::cerr << "Number of groups " << data.numGroups << " does not match the number of variance sets: "
+                      << opt.S.size() << std::endl;
+    }
+}
+
+brr_config makeConfig(const Options &opt, const Data &data)
+{
+    brr_config c{};
+    c.N = data.numInds();
+    c.M = data.numSnps();
+    c.kind = opt.preprocessDataType == PreprocessDataType::SparseRagged ? BRR_KIND_RAGGED : BRR_KIND_DENSE;
+    c.form = opt.form == "fp32c" ? BRR_FORM_FP32C : BRR_FORM_FP64;
+    c.n_groups = (int)opt.S.size();
+    if (c.n_groups < 1 || c.n_groups > BRR_MAX_GROUPS)
+        throw std::string("Error: the variance components could not be parsed (--S)");
+    for (int g = 0; g < c.n_groups; ++g) {
+        c.K[g] = (int)opt.S[g].size() + 1;
+        for (std::size_t k = 0; k < opt.S[g].size() && k < BRR_MAX_K - 1; ++k)
+            c.S[g * (BRR_MAX_K - 1) + k] = opt.S[g][k];
+    }
+    c.seed = opt.seed;
+    c.chain = 0;
+    c.v0E = opt.v0E;
+    c.s02E = opt.s02E;
+    c.v0G = opt.v0G;
+    c.s02G = opt.s02G;
+    c.refresh_every = opt.refreshEvery;
+    c.spec_width = opt.specWidth;
+    c.device = opt.device;
+    return c;
+}
+
+struct Ctx {
+    brr_ctx *h = nullptr;
+    ~Ctx() { brr_ctx_destroy(h); }
+};
+
+void packFromBed(Ctx &ctx, const Options &opt, const Data &data, const brr_config &cfg, std::vector<uint8_t> &bed)
+{
+    check(brr_ctx_create(&cfg, &ctx.h), "brr_ctx_create");
+    bed = readBedPayload(opt.dataFile, cfg.N, cfg.M);
+    check(brr_pack_bed(ctx.h, bed.data(), (int64_t)bed.size()), "brr_pack_bed");
+}
+
+// src/analysisrunner.cpp:47-78 + src/preprocessgraph.cpp:152-244
+bool preprocess(const Options &opt)
+{
+    if (opt.preprocessDataType != PreprocessDataType::Dense && opt.preprocessDataType != PreprocessDataType::SparseRagged)
+        throw std::string("Error: the GB300 path preprocesses dense and ragged markers (--sparse-data ragged)");
+    if (opt.compress)
+        std::cout << "Note: --compress is not applied; preprocessed files are written uncompressed" << std::endl;
+    const auto t0 = std::chrono::steady_clock::now();
+    Data data;
+    readMetaData(data, opt);
+    const brr_config cfg = makeConfig(opt, data);
+    Ctx ctx;
+    std::vector<uint8_t> bed;
+    packFromBed(ctx, opt, data, cfg, bed);
+    const int64_t M = cfg.M;
+    std::vector<double> table((size_t)M * 4);
+    std::vector<int64_t> counts((size_t)M * 4);
+    check(brr_get_marker_table(ctx.h, table.data(), counts.data()), "brr_get_marker_table");
+    const std::string pp = ppFileForType(opt.preprocessDataType, opt.dataFile);
+    const std::string ix = ppIndexFileForType(opt.preprocessDataType, opt.dataFile);
+    if (cfg.kind == BRR_KIND_DENSE) {
+        writeDensePreprocessed(pp, ix, cfg.N, M, table.data(), bed.data());
+    } else {
+        int64_t tot[3] = {0, 0, 0};
+        for (int64_t j = 0; j < M; ++j) {
+            tot[0] += counts[4 * j + 1];
+            tot[1] += counts[4 * j + 2];
+            tot[2] += counts[4 * j + 3];
+        }
+        std::vector<int64_t> off[3];
+        std::vector<int32_t> idx[3];
+        for (int k = 0; k < 3; ++k) {
+            off[k].resize(M + 1);
+            idx[k].resize(tot[k] + 1);
+        }
+        check(brr_get_ragged_lists(ctx.h, off[0].data(), idx[0].data(), off[1].data(), idx[1].data(), off[2].data(),
+                                   idx[2].data()),
+              "brr_get_ragged_lists");
+        const int64_t *offs[3] = {off[0].data(), off[1].data(), off[2].data()};
+        const int32_t *idxs[3] = {idx[0].data(), idx[1].data(), idx[2].data()};
+        writeRaggedPreprocessed(pp, ix, M, table.data(), offs, idxs);
+    }
+    const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::printf("Finished preprocessing the bed file in %.3f sec.\n\n", s);
+    return true;
+}
+
+// Sample file of SampleWriter::openGroups / Writer::write
+// (src/samplewriter.cpp:82-118, src/writer.cpp:9-22): header with ',' and rows
+// with ", " in the stream's default precision.
+struct SampleWriter {
+    std::ofstream out;
+    void open(const std::string &file, int64_t M, int64_t N, int G)
+    {
+        std::cout << "Opening results file " << file << std::endl;
+        out.open(file);
+        if (!out)
+            throw("Error: can not open the sample file [" + file + "] for writing.");
+        out << "iteration," << "mu,";
+        for (int64_t i = 0; i < M; ++i)
+            out << "beta[" << (i + 1) << "],";
+        out << "sigmaE,";
+        for (int g = 0; g < G; ++g)
+            out << "sigmaG[" << (g + 1) << "],";
+        for (int64_t i = 0; i < M; ++i)
+            out << "comp[" << (i + 1) << "],";
+        for (int64_t i = 0; i < M; ++i)
+            out << "acum[" << (i + 1) << "],";
+        int64_t i;
+        for (i = 0; i < N - 1; ++i)
+            out << "epsilon[" << (i + 1) << "],";
+        out << "epsilon[" << (i + 1) << "]" << std::endl;
+    }
+    void write(unsigned iteration, const brr_state &st, int64_t M, int64_t N, int G)
+    {
+        std::ostringstream row;
+        auto put = [&](double v) { row << v << ", "; };
+        put(iteration);
+        put(st.mu);
+        for (int64_t j = 0; j < M; ++j)
+            put(st.beta[j]);
+        put(st.sigmaE);
+        for (int g = 0; g < G; ++g)
+            put(st.sigmaG[g]);
+        for (int64_t j = 0; j < M; ++j)
+            put((double)st.comp[j]);
+        for (int64_t j = 0; j < M; ++j)
+            put(st.acum[j]);
+        for (int64_t i = 0; i < N - 1; ++i)
+            put(st.eps[i]);
+        row << st.eps[N - 1];
+        out << row.str() << std::endl;
+    }
+};
+
+// runBayesRAnalysis + BayesRBase::runGibbs (src/analysisrunner.cpp:123-152,
+// src/BayesRBase.cpp:130-285)
+bool ppbayes(const Options &opt)
+{
+    Data data;
+    readMetaData(data, opt);
+    if (opt.S.empty())
+        throw std::string("Error: variance components must be given for ppbayes (--S)");
+    if ((int64_t)data.y.size() != data.numInds())
+        throw std::string("Error: " + std::to_string(data.y.size()) + " phenotype values for " +
+                          std::to_string(data.numInds()) + " individuals (missing phenotypes must be removed)");
+    if ((int64_t)data.G.size() != data.numSnps())
+        throw std::string("Error: the group file lists " + std::to_string(data.G.size()) + " SNPs, the BIM " +
+                          std::to_string(data.numSnps()));
+    const brr_config cfg = makeConfig(opt, data);
+    Ctx ctx;
+    std::vector<uint8_t> bed;
+    packFromBed(ctx, opt, data, cfg, bed);
+    check(brr_set_groups(ctx.h, data.G.data()), "brr_set_groups");
+    check(brr_set_phenotype(ctx.h, data.y.data()), "brr_set_phenotype");
+    check(brr_init_chain(ctx.h), "brr_init_chain");
+
+    const int64_t M = cfg.M, N = cfg.N;
+    const int G = cfg.n_groups;
+    SampleWriter writer;
+    writer.open(opt.mcmcSampleFile, M, N, G);
+    std::ofstream iterLog;
+    if (opt.iterLog)
+        iterLog.open(opt.iterLogFile);
+    std::vector<double> beta(M), acum(M), eps(N);
+    std::vector<int32_t> comp(M);
+    brr_state st{};
+    st.beta = beta.data();
+    st.comp = comp.data();
+    st.acum = acum.data();
+    st.eps = eps.data();
+    std::cout << "Number of groups: " << G << std::endl << "Running Gibbs sampling" << std::endl;
+    double meanIter = 0.0, meanSweep = 0.0;
+    const auto t1 = std::chrono::steady_clock::now();
+    for (unsigned it = 0; it < opt.chainLength; ++it) {
+        const auto s0 = std::chrono::steady_clock::now();
+        std::cout << "iteration " << it << ": ";
+        check(brr_iterate(ctx.h, 1), "brr_iterate");
+        double sweep_ms = 0, total_ms = 0;
+        int64_t rounds = 0;
+        brr_get_timing(ctx.h, &sweep_ms, &total_ms, &rounds);
+        if (it >= opt.burnin && it % opt.thin == 0) {
+            check(brr_get_state(ctx.h, &st), "brr_get_state");
+            writer.write(it, st, M, N, G);
+        }
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - s0).count();
+        std::cout << secs << "s (" << sweep_ms / 1000.0 << "s)" << std::endl;
+        meanIter += secs;
+        meanSweep += sweep_ms / 1000.0;
+        if (opt.iterLog) {
+            brr_state sc{};
+            check(brr_get_state(ctx.h, &sc), "brr_get_state");
+            iterLog << it << ", " << sc.mu << ", " << sc.sigmaE;
+            for (int g = 0; g < G; ++g)
+                iterLog << ", " << sc.sigmaG[g];
+            iterLog << ", " << sweep_ms << ", " << total_ms << ", " << rounds << std::endl;
+        }
+    }
+    const double dur = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+    std::cout << "duration: " << (long)dur << "s" << std::endl;
+    const double n = opt.chainLength ? (double)opt.chainLength : 1.0;
+    std::cout << "mean iteration duration: " << meanIter / n << "s" << std::endl
+              << "mean flowgraph duration: " << meanSweep / n << "s" << std::endl;
+    return true;
+}
+
+void printOptions(const Options &o)
+{
+    std::cout << "{\"analysis\": " << (int)o.analysisType << ", \"input\": " << (int)o.inputType
+              << ", \"data\": \"" << o.dataFile << "\", \"pheno\": \"" << o.phenotypeFile << "\", \"chain\": "
+              << o.chainLength << ", \"burnin\": " << o.burnin << ", \"thin\": " << o.thin << ", \"seed\": " << o.seed
+              << ", \"samples\": \"" << o.mcmcSampleFile << "\", \"sparse\": " << (int)o.preprocessDataType
+              << ", \"form\": \"" << o.form << "\", \"S\": [";
+    for (std::size_t g = 0; g < o.S.size(); ++g) {
+        std::cout << (g ? ", " : "") << "[";
+        for (std::size_t k = 0; k < o.S[g].size(); ++k)
+            std::cout << (k ? ", " : "") << std::setprecision(17) << o.S[g][k];
+        std::cout << "]";
+    }
+    std::cout << "]}" << std::endl;
+}
+
+}  // namespace
+
+int main(int argc, const char *argv[])
+{
+    std::cout << "***********************************************\n"
+              << "* brr (GB300 sm_103a BayesR Gibbs sampler)    *\n"
+              << "***********************************************" << std::endl;
+    try {
+        Options opt;
+        opt.inputOptions(argc, argv);
+        if (opt.printOptions) {
+            printOptions(opt);
+            return 0;
+        }
+        switch (opt.analysisType) {
+        case AnalysisType::Preprocess:
+            return preprocess(opt) ? 0 : 1;
+        case AnalysisType::PpBayes:
+            if (opt.S.empty()) {
+                std::cerr << "Variance components `--S` are missing or could not be parsed!" << std::endl;
+                return 1;
+            }
+            return ppbayes(opt) ? 0 : 1;
+        default:
+            std::cerr << "unknown analysis type" << std::endl;
+            return 1;
+        }
+    } catch (const std::string &err) {
+        std::cerr << err << std::endl;
+    } catch (const char *err) {
+        std::cerr << err << std::endl;
+    }
+    return 1;
+}

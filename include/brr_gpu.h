@@ -152,6 +152,33 @@ int brr_refresh_eps(brr_ctx *ctx);
  * kernels and everything else, in milliseconds; rounds = grid rounds. */
 int brr_get_timing(brr_ctx *ctx, double *sweep_ms, double *total_ms, int64_t *rounds);
 
+/* Genetic values out[i] = sum_q b[q] * x[i, idx[q]] of the packed, standardised
+ * markers (dense: the DenseMarker column; ragged: the column its residual
+ * update uses, missing = 0).  out: N doubles on the host.  Used to simulate
+ * phenotypes and to predict from posterior-mean effects. */
+int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, double *out);
+
+/* Seeded synthetic genotypes written as a BED payload (M x ceil(N/4) bytes,
+ * no header) into a device buffer: allele frequency of marker j uniform in
+ * [p_lo, p_hi], genotypes Binomial(2, p_j), missing at rate `missing`.  A data
+ * source for benchmarks at sizes where host generation is too slow. */
+int brr_synth_bed_device(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
+                         double missing);
+
+/* Limit of every device-side wait of the sweep (default 2 s); a wait that
+ * runs out makes the call return BRR_ERR_TIMEOUT and leaves the context
+ * usable (re-initialise or set the state before continuing).
+ * phantom_arrivals > 0 makes the grid barrier wait for that many CTAs more
+ * than exist, so that tests can exercise the timeout path without a fault. */
+int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arrivals);
+
+/* Per-phase SM cycles of the sweeps of the last brr_iterate / brr_sweep call,
+ * measured on the first CTA (the counterpart of the reference's per-column
+ * timing log, src/BayesRBase.cpp:381-389): [0] ring prefetch and wait,
+ * [1] partial dot products, [2] grid barrier, [3] component sampling,
+ * [4] outputs and residual update, [5] grid rounds. */
+int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles);
+
 #ifdef __cplusplus
 }
 #endif
