@@ -230,7 +230,13 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: N=100,000 x M=8,192 (200 MB of codes, above L2), same settings")
     args = ap.parse_args()
+    if args.small:
+        global M_SNP, N_CAUSAL, WORKLOAD
+        M_SNP, N_CAUSAL = 8192, 82
+        WORKLOAD = WORKLOAD.replace("M=100,000", "M=8,192").replace("1,000 causal", "82 causal")
 
     rank, world, dist = dist_setup(args.gpus)
     if args.impl == "reference":

@@ -1,0 +1,123 @@
+"""`brr` end to end on the GPU: preprocess files and a ppbayes run.
+
+The ppbayes sample file has 1 + ceil(chain/thin) lines (the reference's
+smoke invariant, test/ppbayestest.cpp:138-149) and its rows hold the same
+chain as the oracle (values as printed with 6 significant digits).
+"""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from bayesrrcmd_gb300 import plink
+from bayesrrcmd_gb300.build import build_cli
+
+pytestmark = pytest.mark.gpu
+S2 = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
+
+
+@pytest.fixture(scope="module")
+def brr(gpu_lib):
+    return str(build_cli())
+
+
+@pytest.fixture
+def dataset(tmp_path):
+    N, M = 509, 120
+    g, _ = plink.synth_genotypes(N, M, seed=4, missing=0.01)
+    payload = plink.encode_bed(g)
+    prefix = tmp_path / "toy"
+    plink.write_plink(prefix, payload, N)
+    y, _, _ = plink.synth_phenotype(g, 4, 6, 0.5)
+    plink.write_phen(tmp_path / "toy.phen", y)
+    group = (np.arange(M) % 2).astype(np.int32)
+    plink.write_groups(tmp_path / "toy.group", group)
+    return dict(N=N, M=M, g=g, payload=payload, prefix=prefix, y=plink.read_phen(tmp_path / "toy.phen",
+                plink.read_fam(prefix.with_suffix(".fam"))), group=group, dir=tmp_path)
+
+
+def run(brr, *args):
+    r = subprocess.run([brr, *args], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    return r.stdout
+
+
+@pytest.mark.parametrize("sparse", [None, "ragged"])
+def test_preprocess_writes_reference_formats(brr, dataset, sparse):
+    d = dataset
+    args = ["--preprocess", "--bfile", str(d["prefix"]), "--pheno", str(d["dir"] / "toy.phen")]
+    if sparse:
+        args += ["--sparse-data", sparse]
+    run(brr, *args)
+    N, M = d["N"], d["M"]
+    if sparse is None:
+        data = np.fromfile(d["dir"] / "toy.ppbed", np.float64).reshape(M, N)
+        idx = np.fromfile(d["dir"] / "toy.ppbedindex", np.uint64).reshape(M, 3)
+        np.testing.assert_array_equal(data, O.dense_columns(d["payload"], N))
+        np.testing.assert_array_equal(idx[:, 0], np.arange(M) * N * 8)
+        np.testing.assert_array_equal(idx[:, 1], N * 8)
+    else:
+        raw = (d["dir"] / "toy.ragged.sparsebed").read_bytes()
+        idx = np.fromfile(d["dir"] / "toy.ragged.sparsebedindex", np.uint64).reshape(M, 3)
+        rc, st = O.ragged_stats(d["payload"], N)
+        lists = O.ragged_lists(d["payload"], N)
+        for j in range(M):
+            pos = int(idx[j, 0])
+            stats = np.frombuffer(raw, np.float64, 4, pos)
+            np.testing.assert_array_equal(stats, st[j])
+            pos += 32
+            for off, ix in lists:
+                n = int(np.frombuffer(raw, np.uint64, 1, pos)[0])
+                pos += 8
+                got = np.frombuffer(raw, np.int32, n, pos)
+                pos += 4 * n
+                np.testing.assert_array_equal(got, ix[off[j]:off[j + 1]])
+            assert pos == int(idx[j, 0] + idx[j, 1])
+
+
+@pytest.mark.parametrize("chain,thin,burn", [(10, 1, 0), (7, 3, 0), (6, 2, 2)])
+def test_ppbayes_sample_file(brr, dataset, chain, thin, burn):
+    d = dataset
+    out = d["dir"] / "samples.csv"
+    run(brr, "--analysis-type", "ppbayes", "--bfile", str(d["prefix"]), "--pheno", str(d["dir"] / "toy.phen"),
+        "--group", str(d["dir"] / "toy.group"), "--S", "0.01,0.001,0.0001;0.1,0.01",
+        "--chain-length", str(chain), "--burn-in", str(burn), "--thin", str(thin), "--seed", "11",
+        "--mcmc-samples", str(out))
+    lines = out.read_text().splitlines()
+    kept = [it for it in range(chain) if it >= burn and it % thin == 0]
+    assert len(lines) == 1 + len(kept)
+    if burn == 0:
+        assert len(lines) == 1 + int(np.ceil(chain / thin))
+    M, N = d["M"], d["N"]
+    header = lines[0].split(",")
+    assert header[:3] == ["iteration", "mu", "beta[1]"] and header[-1] == f"epsilon[{N}]"
+    assert len(header) == 2 + M + 1 + 2 + M + M + N
+    oc = O.OracleChain(d["payload"], N, d["y"], S2, kind=0, group=d["group"], seed=11)
+    rows = {}
+    for it in range(chain):
+        oc.iterate(it)
+        if it in kept:
+            rows[it] = oc.state()
+    for line in lines[1:]:
+        v = np.array([float(t) for t in line.split(", ")])
+        it = int(v[0])
+        s = rows[it]
+        np.testing.assert_allclose(v[1], s["mu"], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(v[2:2 + M], s["beta"], rtol=1e-5, atol=1e-9)
+        np.testing.assert_allclose(v[2 + M], s["sigmaE"], rtol=1e-5)
+        np.testing.assert_array_equal(v[5 + M:5 + 2 * M], s["comp"])
+
+
+def test_ppbayes_missing_phenotypes_are_an_error(brr, dataset):
+    d = dataset
+    phen = d["dir"] / "toy.phen"
+    lines = phen.read_text().splitlines()
+    t = lines[3].split()
+    lines[3] = f"{t[0]} {t[1]} NA"
+    phen.write_text("\n".join(lines) + "\n")
+    r = subprocess.run([brr, "--analysis-type", "ppbayes", "--bfile", str(d["prefix"]), "--pheno", str(phen),
+                        "--chain-length", "2", "--mcmc-samples", str(d["dir"] / "x.csv")],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "phenotype" in r.stderr
