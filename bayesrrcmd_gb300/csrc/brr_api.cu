@@ -1008,6 +1008,27 @@ int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, dou
     return rc;
 }
 
+// Allocation-free variant of brr_xbeta for callers that cannot allocate
+// device memory; the term list goes through the static array of
+// brr_noalloc.cu and the result into the caller's device buffer.
+int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, double *d_out)
+{
+    if (!ctx || !ctx->packed || !d_out || n < 0 || (n > 0 && (!idx || !b)))
+        return fail(BRR_ERR_ARG, "pack markers first; idx/b (host) and d_out (device, N doubles) required");
+    if (n > BRR_NOALLOC_MAX_TERMS)
+        return fail(BRR_ERR_ARG, "brr_xbeta_noalloc takes at most " + std::to_string(BRR_NOALLOC_MAX_TERMS) +
+                                     " terms (the size of its static device array); got " + std::to_string(n));
+    for (int64_t q = 0; q < n; ++q)
+        if (idx[q] >= (uint32_t)ctx->cfg.M)
+            return fail(BRR_ERR_ARG, "marker index out of range");
+    BRR_CUDA(cudaSetDevice(ctx->dev));
+    std::string why;
+    if (noalloc_xbeta(ctx->dev, ctx->st, ctx->cfg.kind, ctx->cfg.N, ctx->d_codes, ctx->col_stride, ctx->d_table, idx, b,
+                      n, d_out, why) != cudaSuccess)
+        return fail(BRR_ERR_CUDA, why);
+    return BRR_OK;
+}
+
 int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arrivals)
 {
     if (!ctx || timeout_ns == 0 || phantom_arrivals < 0)

@@ -60,7 +60,7 @@ EXPORTS = [
     "brr_last_error", "brr_ctx_create", "brr_ctx_destroy", "brr_pack_bed", "brr_pack_bed_device",
     "brr_get_marker_table", "brr_get_ragged_lists", "brr_set_groups", "brr_set_phenotype", "brr_init_chain",
     "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing", "brr_get_phase_cycles",
-    "brr_set_wait_limit", "brr_xbeta", "brr_synth_bed_device",
+    "brr_set_wait_limit", "brr_xbeta", "brr_synth_bed_device", "brr_xbeta_noalloc",
 ]
 
 
@@ -95,6 +95,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_get_phase_cycles.argtypes = [P, C.POINTER(C.c_int64)]
     lib.brr_set_wait_limit.argtypes = [P, C.c_uint64, C.c_int32]
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
+    lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
     lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
     for name in EXPORTS:
         if name != "brr_last_error":

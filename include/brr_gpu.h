@@ -165,6 +165,20 @@ int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, dou
 int brr_synth_bed_device(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
                          double missing);
 
+/* Allocation-free genetic values.  No counterpart in the reference: it serves
+ * callers that cannot allocate device memory when they need the values (a
+ * host runtime that owns the whole GPU through its own pool and forbids
+ * further cudaMalloc, a serving loop that must not block on the allocator or
+ * synchronise the device).  Computes the same d_out[i] = sum_q b[q] *
+ * x[i, idx[q]] as brr_xbeta, but into a caller-owned device buffer of N
+ * doubles, with idx/b (host arrays) staged in a fixed static device array
+ * of BRR_NOALLOC_MAX_TERMS terms; n above that limit is rejected with
+ * BRR_ERR_ARG.  Calls no cudaMalloc/cudaFree.  The first call on a device
+ * looks up the array's device address, so make it before any stream
+ * capture; calls that overlap on the GPU share the array and race. */
+#define BRR_NOALLOC_MAX_TERMS 65536
+int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, double *d_out);
+
 /* Limit of every device-side wait of the sweep (default 2 s); a wait that
  * runs out makes the call return BRR_ERR_TIMEOUT and leaves the context
  * usable (re-initialise or set the state before continuing).
