@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "lib"
 BUILD = PKG / "_build"
 LIB = LIBDIR / "libbrr_gpu.so"
-SOURCES = ["brr_pack.cu", "brr_sweep.cu", "brr_api.cu", "brr_noalloc.cu"]
+SOURCES = ["brr_pack.cu", "brr_sweep.cu", "brr_api.cu", "brr_noalloc.cu", "brr_gram.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
 
@@ -59,7 +59,7 @@ def build_gpu(verbose: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     if _stale(LIB, objs):
-        cmd = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
+        cmd = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libbrr_gpu.so failed:\n{r.stdout}\n{r.stderr}")

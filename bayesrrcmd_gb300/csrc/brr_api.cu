@@ -112,6 +112,11 @@ struct brr_ctx {
     long long *d_prof = nullptr;        // per-phase cycles of the last sweep (CTA 0)
     uint32_t *d_nzj = nullptr;
     double *d_nzb = nullptr;
+    double *d_gram = nullptr;           // blocked FP32C: packed marker Gram
+    double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries of two blocks
+    bool blocked = false;
+    bool has_missing = false;
+    double gram_ms = 0.0;
 
     // pinned host staging
     uint32_t *h_order = nullptr;
@@ -131,7 +136,7 @@ struct brr_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
     int64_t last_rounds = 0;
-    long long phase[6] = {0, 0, 0, 0, 0, 0};   // summed over the sweeps of the last call
+    long long phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // summed over the sweeps of the last call
     uint64_t wait_limit_ns = 2000000000ull;
     int phantom = 0;
 
@@ -182,6 +187,8 @@ void free_all(brr_ctx *c)
     cudaFree(c->d_prof);
     cudaFree(c->d_nzj);
     cudaFree(c->d_nzb);
+    cudaFree(c->d_gram);
+    cudaFree(c->d_gstage);
     cudaFreeHost(c->h_order);
     cudaFreeHost(c->h_stats);
     cudaFreeHost(c->h_part);
@@ -324,10 +331,16 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     a.prof = c->d_prof;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
-    const size_t smem = sweep_smem_bytes(cf.form, cf.kind, a);
+    a.gram = c->d_gram;
+    a.gstage = c->d_gstage;
+    BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 8, c->st));
+    const size_t smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, cf.kind, a);
 
     BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
-    BRR_CUDA(launch_sweep(cf.form, cf.kind, a, smem, c->st));
+    if (c->blocked)
+        BRR_CUDA(launch_sweep_block(a, smem, c->st));
+    else
+        BRR_CUDA(launch_sweep(cf.form, cf.kind, a, smem, c->st));
     BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
 
     const int ng = cf.n_groups;
@@ -337,14 +350,14 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     BRR_CUDA(cudaMemcpyAsync(vstat.data(), c->d_vstat, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->h_part, c->d_part, sizeof(double) * 2 * c->G, cudaMemcpyDeviceToHost, c->st));
-    long long rounds = 0, prof[6];
+    long long rounds = 0, prof[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     BRR_CUDA(cudaMemcpyAsync(&rounds, c->d_rounds, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(prof, c->d_prof, sizeof(prof), cudaMemcpyDeviceToHost, c->st));
     const int rc = check_device_status(c);
     if (rc)
         return rc;
     BRR_CUDA(cudaEventElapsedTime(sweep_ms, c->ev[0], c->ev[1]));
-    for (int k = 0; k < 6; ++k)
+    for (int k = 0; k < 8; ++k)
         c->phase[k] += prof[k];
 
     for (int g = 0; g < ng; ++g)
@@ -408,6 +421,72 @@ void schedule_permutation(brr_ctx *c, uint32_t it)
     const uint32_t M = (uint32_t)c->cfg.M;
     uint32_t *dst = c->perm_next.data();
     c->perm_future = std::async(std::launch::async, [k, it, M, dst]() { make_permutation(k, it, M, dst); });
+}
+
+// The FP32C dense form resolves whole blocks of markers per grid round with
+// the precomputed marker Gram when it fits in device memory (2 GB left free).
+int prepare_blocked(brr_ctx *c)
+{
+    const brr_config &cf = c->cfg;
+    if (cf.form != BRR_FORM_FP32C || cf.kind != BRR_KIND_DENSE || cf.gram < 0 || cf.M < 2) {
+        c->blocked = false;
+        if (cf.gram > 0)
+            return fail(BRR_ERR_ARG, "the Gram-blocked sweep needs the FP32C form, dense markers and M >= 2");
+        return BRR_OK;
+    }
+    if (c->d_gram) {
+        c->blocked = true;
+        return BRR_OK;
+    }
+    size_t gram_bytes = 0, work = 0, free_b = 0, total_b = 0;
+    gram_bytes_needed(cf.N, cf.M, c->has_missing, &gram_bytes, &work);
+    BRR_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t margin = (size_t)2 << 30;
+    if (gram_bytes + work + margin > free_b) {
+        if (cf.gram > 0)
+            return fail(BRR_ERR_OOM, "the marker Gram (" + std::to_string(gram_bytes >> 20) + " MiB) does not fit");
+        c->blocked = false;
+        return BRR_OK;
+    }
+    if (cf.spec_width == 0)
+        c->B = 64;
+    SweepArgs a{};
+    a.B = c->B;
+    a.n_groups = cf.n_groups;
+    a.slice_max = c->slice_max;
+    a.slot_bytes = c->slot_bytes;
+    const size_t smem = sweep_block_smem_bytes(a);
+    const int per_sm = sweep_block_max_ctas_per_sm(smem);
+    if (per_sm < 1 || (int64_t)per_sm * c->sms < c->G) {
+        if (cf.gram > 0)
+            return fail(BRR_ERR_ARG, "the blocked sweep does not fit its CTAs");
+        c->blocked = false;
+        return BRR_OK;
+    }
+    if (cudaMalloc((void **)&c->d_gram, gram_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        c->d_gram = nullptr;
+        if (cf.gram > 0)
+            return fail(BRR_ERR_OOM, "allocation of the marker Gram failed");
+        c->blocked = false;
+        return BRR_OK;
+    }
+    BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
+    std::string why;
+    if (build_gram(c->d_codes, c->col_stride, cf.N, cf.M, c->d_scale, c->d_counts, c->has_missing, c->d_gram, c->st,
+                   why) != 0) {
+        cudaFree(c->d_gram);
+    cudaFree(c->d_gstage);
+        c->d_gram = nullptr;
+        return fail(BRR_ERR_CUDA, "building the marker Gram failed: " + why);
+    }
+    BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
+    BRR_CUDA(cudaEventSynchronize(c->ev[1]));
+    float ms = 0.f;
+    BRR_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    c->gram_ms = ms;
+    c->blocked = true;
+    return BRR_OK;
 }
 
 int refresh_eps_impl(brr_ctx *c)
@@ -561,7 +640,7 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
             dalloc(&c.d_gconst, (size_t)cf.n_groups * kMaxK * 4) || dalloc(&c.d_gK, (size_t)cf.n_groups) ||
             dalloc(&c.d_stats, (size_t)cf.n_groups * kMaxK + cf.n_groups + 1) ||
             dalloc(&c.d_part, (size_t)std::max(2 * c.G, kPartBlocks)) || dalloc(&c.d_err, 1) ||
-            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 6) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
+            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 8) || dalloc(&c.d_gstage, (size_t)kMaxSpec * (kMaxSpec - 1)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
             dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M))
             return fail(BRR_ERR_OOM, "device allocation failed");
         if (cf.form == BRR_FORM_FP64) {
@@ -600,6 +679,13 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
         return fail(BRR_ERR_MARKER, "marker " + std::to_string(bad) +
                                         " does not vary or is all missing; SNPs that do not vary should be "
                                         "removed prior to analysis");
+    {
+        std::vector<int64_t> cnt(M * 4);
+        BRR_CUDA(cudaMemcpy(cnt.data(), c.d_counts, sizeof(int64_t) * M * 4, cudaMemcpyDeviceToHost));
+        c.has_missing = false;
+        for (int64_t j = 0; j < M && !c.has_missing; ++j)
+            c.has_missing = cnt[4 * j + 3] != 0;
+    }
     if (cf.kind == BRR_KIND_RAGGED) {
         const int64_t MG1 = M * (int64_t)c.G + 1;
         if (3 * MG1 > (int64_t)INT_MAX)
@@ -772,6 +858,9 @@ int brr_init_chain(brr_ctx *ctx)
     int rc = upload_state_eps(&c, eps.data());
     if (rc)
         return rc;
+    rc = prepare_blocked(&c);
+    if (rc)
+        return rc;
     c.iteration = 0;
     c.sweeps = 0;
     c.inited = true;
@@ -934,6 +1023,9 @@ int brr_set_state(brr_ctx *ctx, const brr_state *st)
     std::memcpy(c.sigmaG, st->sigmaG, sizeof(c.sigmaG));
     std::memcpy(c.pi, st->pi, sizeof(c.pi));
     c.iteration = st->iteration;
+    const int rb = prepare_blocked(&c);
+    if (rb)
+        return rb;
     c.inited = true;
     return BRR_OK;
 }
@@ -1038,11 +1130,24 @@ int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arriva
     return BRR_OK;
 }
 
+int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes)
+{
+    if (!ctx)
+        return fail(BRR_ERR_ARG, "null context");
+    if (blocked)
+        *blocked = ctx->blocked ? 1 : 0;
+    if (build_ms)
+        *build_ms = ctx->gram_ms;
+    if (bytes)
+        *bytes = ctx->d_gram ? (int64_t)(ctx->cfg.M * (ctx->cfg.M - 1) / 2) * (int64_t)sizeof(double) : 0;
+    return BRR_OK;
+}
+
 int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles)
 {
     if (!ctx || !cycles)
         return fail(BRR_ERR_ARG, "null argument");
-    for (int k = 0; k < 6; ++k)
+    for (int k = 0; k < 8; ++k)
         cycles[k] = ctx->phase[k];
     return BRR_OK;
 }

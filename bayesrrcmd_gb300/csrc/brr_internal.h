@@ -59,6 +59,8 @@ struct SweepArgs {
     long long *prof;             // optional: cycles per round phase of CTA 0 (diagnostics), or null
     uint64_t timeout_ns;         // limit of any single wait
     int phantom;                 // extra arrivals the barrier waits for (tests of the timeout path)
+    const double *gram;          // blocked FP32C sweep: packed lower-triangle marker Gram (FP64)
+    double *gstage;              // blocked FP32C sweep: 2 x B(B-1)/2 staged Gram entries
 };
 
 // Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).
@@ -96,5 +98,11 @@ cudaError_t noalloc_xbeta(int dev, cudaStream_t st, int kind, int64_t N, const u
                           const double *table, const uint32_t *idx, const double *b, int64_t n, double *d_out,
                           std::string &why);
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem);
+size_t sweep_block_smem_bytes(const SweepArgs &a);
+cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st);
+int sweep_block_max_ctas_per_sm(size_t smem);
+cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work);
+int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
+               const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why);
 
 }  // namespace brr

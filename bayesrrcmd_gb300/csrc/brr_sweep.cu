@@ -843,6 +843,581 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
     }
 }
 
+// --------------------------------------------------------------------------
+// Blocked sweep of the FP32C form over dense markers, with the precomputed
+// marker Gram matrix (packed lower triangle, FP64).  Every grid round
+// resolves exactly B consecutive markers of the sweep order: the B dot
+// products against the residual at the start of the block are exchanged as in
+// k_sweep; then, in every CTA, all markers of the block are sampled in
+// parallel, the first one that changes the residual (p) is kept, the dot
+// products of the later markers are moved by dBeta_p * G[p, t], and the later
+// markers are sampled again, until no later marker changes the residual.  This
+// is the sequential chain exactly (up to rounding): marker t sees
+// x_t . (eps + sum_{p<t} dBeta_p x_p).  The rank-U residual update of the block
+// follows.  Genotype slices, records and the block's Gram entries are
+// prefetched with cp.async one round ahead.
+struct BlockPlan {
+    SmemPlan base;
+    size_t gram;    // 2 x npairs doubles
+    size_t pairs;   // npairs x 2 bytes (positions a < b)
+    size_t gcf;     // n_groups x kMaxK x 2 floats: FP32 log-likelihood constants
+    size_t total;
+};
+
+__host__ __device__ inline BlockPlan make_block_plan(int slice_max, int slot_bytes, int B, int n_groups)
+{
+    BlockPlan p;
+    p.base = make_plan(kFormFP32C, kKindDense, slice_max, slot_bytes, B, n_groups);
+    const size_t npairs = (size_t)B * (B - 1) / 2;
+    size_t o = p.base.total;
+    p.gram = o;
+    o += align16(2 * npairs * sizeof(double));
+    p.pairs = o;
+    o += align16(npairs * 2);
+    p.gcf = o;
+    o += align16((size_t)n_groups * kMaxK * 2 * sizeof(float));
+    p.total = align16(o);
+    return p;
+}
+
+// FP32 component selection with a rigorous error bound, falling back to the
+// FP64 evaluation of pick_marker when the bound cannot certify the decision.
+// With D_k = logL_k - logL_0 = dc_k + h_k*num^2 (dc_0 = h_0 = 0) evaluated by one
+// FMA from rounded inputs, |error(D_k)| <= 3u(|dc_k| + |h_k num^2|) with
+// u = 2^-24.  The 700 guards compare differences of D (the logL_0 offset
+// cancels); a guard whose difference lies within the error band of 700
+// falls back.  Probabilities then carry at most 2*max_err + 2^-21 relative
+// error, so a u within tol = 4e-5 + 4*max_err of a cumulative bound falls back.
+template <int KM>
+__device__ __forceinline__ Pick pick_fast(double num, double u, double z, double beta_old,
+                                          const float *__restrict__ gcf, const double *__restrict__ gc, int K)
+{
+    const float n2 = (float)(num * num);
+    float D[KM];
+    float maxerr = 0.f;
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+        if (k == 0 || k >= K) {
+            D[k] = k == 0 ? 0.f : -INFINITY;
+        } else {
+            const float dc = gcf[2 * k], h = gcf[2 * k + 1];
+            D[k] = __fmaf_rn(h, n2, dc);
+            maxerr = fmaxf(maxerr, 1.8e-7f * (fabsf(dc) + fabsf(h * n2)));
+        }
+    }
+    float dmax = 0.f, dmax1 = D[1], dmin1 = D[1];
+#pragma unroll
+    for (int k = 1; k < KM; ++k) {
+        if (k < K) {
+            dmax = fmaxf(dmax, D[k]);
+            dmax1 = fmaxf(dmax1, D[k]);
+            dmin1 = fminf(dmin1, D[k]);
+        }
+    }
+    const float band = 2.f * maxerr + 1e-3f;
+    const float spread = dmax1 - dmin1;
+    bool unsure = fabsf(spread - 700.f) < band || fabsf(dmax1 - 700.f) < band || fabsf(-dmin1 - 700.f) < band;
+    const bool wide = spread > 700.f;
+    const bool guard0 = (dmax1 > 700.f) || (-dmin1 > 700.f);
+    float e[KM];
+    float es = 0.f;
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+        e[k] = k < K ? __expf(D[k] - dmax) : 0.f;
+        es += e[k];
+    }
+    const float ies = __frcp_rn(es);
+    int chosen = -1;
+    float acum = 0.f, prev = 0.f, a0 = 0.f;
+    const float uf = (float)u;
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+        if (k < K && chosen < 0) {
+            bool guard;
+            if (k == 0) {
+                guard = guard0;
+            } else {
+                const float d1 = dmax1 - D[k], d2 = D[k] - dmin1;
+                if (wide && (fabsf(d1 - 700.f) < band || fabsf(d2 - 700.f) < band))
+                    unsure = true;
+                guard = wide && (d1 > 700.f || d2 > 700.f);
+            }
+            const float pk = guard ? 0.f : e[k] * ies;
+            if (k == 0)
+                a0 = pk;
+            prev = acum;
+            acum += pk;
+            if (uf <= acum)
+                chosen = k;
+        }
+    }
+    const float tol = 4e-5f + 4.f * maxerr;
+    const bool close = chosen >= 0 ? ((uf > acum - tol) || (chosen > 0 && uf < prev + tol)) : (uf < acum + tol);
+    if (unsure || close)
+        return pick_marker<false, KM>(num, u, z, beta_old, gc, K);
+    Pick res;
+    res.comp = chosen;
+    res.acum0 = (double)a0;
+    res.beta = beta_old;
+    if (chosen == 0) {
+        res.beta = 0.0;
+    } else if (chosen > 0) {
+        const double sdk = gc[4 * chosen + 3], invden = gc[4 * chosen + 1];
+        res.beta = __dadd_rn(__dmul_rn(z, sdk), __dmul_rn(num, invden));
+    }
+    return res;
+}
+
+template <int KM>
+__global__ void __launch_bounds__(kThreads, 1) k_sweep_block(SweepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_num0[kMaxSpec];
+    __shared__ double s_corr[kMaxSpec];
+    __shared__ double s_beta[kMaxSpec];
+    __shared__ double s_acum[kMaxSpec];
+    __shared__ int s_comp[kMaxSpec];
+    __shared__ int s_upd[kMaxSpec];
+    __shared__ float s_dfl[kMaxSpec][8];
+    __shared__ int s_first[2], s_abort, s_nupd;
+    __shared__ double s_scal[2];
+
+    const int B = a.B;
+    const int lpm = kThreads / B;
+    const int R = 4 * B;
+    const int sidx = blockIdx.x;
+    const int tid = threadIdx.x;
+    const int lo = a.slice_lo[sidx];
+    const int ns = a.slice_lo[sidx + 1] - lo;
+    const int nbytes = ((ns + kChunk - 1) / kChunk) * 16;
+    const int64_t byte_lo = lo / 4;
+    const BlockPlan bp = make_block_plan(a.slice_max, a.slot_bytes, B, a.n_groups);
+    const SmemPlan &plan = bp.base;
+    const int npairs = B * (B - 1) / 2;
+
+    float *eh = reinterpret_cast<float *>(smem + plan.eps0);
+    float *el = reinterpret_cast<float *>(smem + plan.eps1);
+    uint8_t *ring_codes = smem + plan.ring_codes;
+    SweepRec *ring_rec = reinterpret_cast<SweepRec *>(smem + plan.ring_rec);
+    double *gconst = reinterpret_cast<double *>(smem + plan.gconst);
+    int32_t *gk = reinterpret_cast<int32_t *>(smem + plan.gk);
+    float4 *gtab = reinterpret_cast<float4 *>(smem + plan.gtab);
+    uint8_t *mtab = smem + plan.gtab + 256 * 16;
+    double *gbuf = reinterpret_cast<double *>(smem + bp.gram);
+    uint8_t *pair_ab = smem + bp.pairs;
+    float *gcf = reinterpret_cast<float *>(smem + bp.gcf);
+
+    // ---- prologue
+    float muh, mul;
+    df_from_double(-a.mu_new, muh, mul);
+    for (int i = tid; i < a.slice_max; i += kThreads) {
+        float h = 0.f, l = 0.f;
+        if (i < ns) {
+            h = a.eps_hi[lo + i];
+            l = a.eps_lo[lo + i];
+            df_add(h, l, muh, mul);
+        }
+        eh[i] = h;
+        el[i] = l;
+    }
+    for (int i = tid; i < a.n_groups * kMaxK * 4; i += kThreads)
+        gconst[i] = a.gconst[i];
+    for (int i = tid; i < a.n_groups; i += kThreads)
+        gk[i] = a.gK[i];
+    for (int i = tid; i < a.n_groups * kMaxK; i += kThreads) {
+        const int g = i / kMaxK, k = i - g * kMaxK;
+        const double *row = a.gconst + (size_t)g * kMaxK * 4;
+        gcf[2 * i] = k == 0 ? 0.f : (float)(row[4 * k] - row[0]);
+        gcf[2 * i + 1] = k == 0 ? 0.f : (float)row[4 * k + 2];
+    }
+    for (int v = tid; v < 256; v += kThreads) {
+        float g[4];
+        unsigned m = 0;
+        for (int k = 0; k < 4; ++k) {
+            const unsigned c = (v >> (2 * k)) & 3u;
+            g[k] = c == 0u ? 2.f : (c == 2u ? 1.f : 0.f);
+            if (c == 1u)
+                m |= 1u << k;
+        }
+        gtab[v] = make_float4(g[0], g[1], g[2], g[3]);
+        mtab[v] = (uint8_t)m;
+    }
+    for (int pb = 1 + tid; pb < B; pb += kThreads)
+        for (int pa = 0; pa < pb; ++pa) {
+            const int p = pb * (pb - 1) / 2 + pa;
+            pair_ab[2 * p] = (uint8_t)pa;
+            pair_ab[2 * p + 1] = (uint8_t)pb;
+        }
+    if (tid == 0) {
+        s_abort = 0;
+        s_scal[0] = a.eps_total;
+        s_first[0] = kMaxSpec;
+        s_first[1] = kMaxSpec;
+    }
+    __syncthreads();
+
+    const unsigned M32 = (unsigned)a.M;
+    const unsigned Rm = (unsigned)R - 1u;
+    unsigned rec_issued = 0, code_issued = 0;
+    auto issue_recs = [&](unsigned upto) {
+        upto = min(upto, M32);
+        if (upto <= rec_issued)
+            return;
+        const unsigned n = (upto - rec_issued) * 4u;
+        for (unsigned e = tid; e < n; e += kThreads) {
+            const unsigned q = rec_issued + (e >> 2);
+            const unsigned c = e & 3u;
+            cp_async16(reinterpret_cast<unsigned char *>(&ring_rec[q & Rm]) + 16 * c,
+                       reinterpret_cast<const unsigned char *>(&a.rec[q]) + 16 * c);
+        }
+        rec_issued = upto;
+    };
+    const unsigned chunks = (unsigned)nbytes / 16u;
+    const unsigned per_pass = chunks ? (unsigned)kThreads / chunks : 0u;
+    const unsigned my_q = chunks ? (unsigned)tid / chunks : 0u;
+    const unsigned my_c = chunks ? (unsigned)tid - my_q * chunks : 0u;
+    auto issue_codes = [&](unsigned upto) {
+        upto = min(upto, M32);
+        if (upto <= code_issued)
+            return;
+        if (my_q < per_pass) {
+            for (unsigned q = code_issued + my_q; q < upto; q += per_pass) {
+                const uint32_t j = ring_rec[q & Rm].j;
+                cp_async16(ring_codes + (q & Rm) * a.slot_bytes + 16 * my_c,
+                           a.codes + (int64_t)j * a.col_stride + byte_lo + 16 * my_c);
+            }
+        }
+        code_issued = upto;
+    };
+    // Cooperative Gram gather: CTA s loads pairs p = s, s+G, ... of the block
+    // starting at q0 (issued early into registers, stored to the global staging
+    // buffer before the CTA arrives at the round barrier, which publishes them).
+    // Thread t of CTA s owns pairs p = s + (t + k*kThreads)*G; the first one is
+    // loaded ahead into a register, any further ones (small grids only) at store time.
+    double gval = 0.0;
+    int gpair = -1;
+    unsigned gq0 = 0;
+    auto gram_entry = [&](unsigned q0, int p, unsigned nb, double *out) -> bool {
+        const unsigned pa = pair_ab[2 * p], pb = pair_ab[2 * p + 1];
+        if (pb >= nb)
+            return false;
+        const int64_t ja = ring_rec[(q0 + pa) & Rm].j, jb = ring_rec[(q0 + pb) & Rm].j;
+        const int64_t hi = ja > jb ? ja : jb, lw = ja > jb ? jb : ja;
+        *out = __ldg(&a.gram[hi * (hi - 1) / 2 + lw]);
+        return true;
+    };
+    auto gather_load = [&](unsigned q0) {
+        gpair = -1;
+        gq0 = q0;
+        if (q0 >= M32)
+            return;
+        const int p = sidx + tid * a.G;
+        if (p < npairs && gram_entry(q0, p, min((unsigned)B, M32 - q0), &gval))
+            gpair = p;
+    };
+    auto gather_store = [&](int buf) {
+        if (gpair >= 0)
+            a.gstage[(size_t)buf * npairs + gpair] = gval;
+        if (gq0 >= M32)
+            return;
+        const unsigned nb = min((unsigned)B, M32 - gq0);
+        for (int p = sidx + (tid + kThreads) * a.G; p < npairs; p += kThreads * a.G) {
+            double v;
+            if (gram_entry(gq0, p, nb, &v))
+                a.gstage[(size_t)buf * npairs + p] = v;
+        }
+    };
+    auto copy_stage = [&](int buf) {
+        const unsigned n16 = (unsigned)(npairs * 8 + 15) / 16u;
+        for (unsigned e = tid; e < n16; e += kThreads)
+            cp_async16(reinterpret_cast<unsigned char *>(gbuf + (size_t)buf * npairs) + 16 * e,
+                       reinterpret_cast<const unsigned char *>(a.gstage + (size_t)buf * npairs) + 16 * e);
+    };
+
+    issue_recs(3u * B);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    issue_codes(2u * B);
+    cp_async_commit();
+    gather_load(0u);
+    gather_store(0);   // block 0's entries, published by the first round barrier
+
+    int lpm_log2 = 0;
+    while ((1 << lpm_log2) < lpm)
+        ++lpm_log2;
+    const Team tm = make_team(lpm);
+    const int team = tid >> lpm_log2;
+    const double Nm1 = (double)(a.N - 1);
+    const bool prof = a.prof != nullptr && blockIdx.x == 0 && tid == 0;
+    long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long tp = prof ? clock64() : 0;
+    auto mark = [&](int k) {
+        if (prof) {
+            const long long t = clock64();
+            ph[k] += t - tp;
+            tp = t;
+        }
+    };
+    auto publish = [&](unsigned long long *acc, __int128 x) {
+        const Fx f = fx_split(x);
+        red_add_u64(acc, (unsigned long long)f.hi);
+        red_add_u64(acc + 1, f.lo);
+    };
+
+    unsigned start = 0;
+    long long r = 0, steps = 0;
+    int rb = 0;
+    while (start < M32) {
+        cp_async_wait_all();
+        __syncthreads();
+        issue_codes(start + 2u * B);
+        issue_recs(start + 3u * B);
+        cp_async_commit();
+        gather_load(start + (unsigned)B);   // next block's Gram entries, in flight during the dots
+        const int nb = (int)min((unsigned)B, M32 - start);
+        const double *gcur = gbuf + (size_t)(r & 1) * npairs;
+        mark(0);
+
+        // ---- partial dot products (double-float, exact integer genotypes);
+        // per byte the four products are combined by error-free TwoSums before
+        // the one TwoSum into the running sum, so the dependent chain per lane
+        // is one TwoSum per byte
+        if (team < nb) {
+            const unsigned slot = (start + team) & Rm;
+            const uint8_t *cb = ring_codes + slot * a.slot_bytes;
+            unsigned long long *acc = a.acc + (rb * kMaxSpec + team) * 4;
+            float A0 = 0.f, L0 = 0.f, A1 = 0.f, L1 = 0.f, mh = 0.f, ml = 0.f;
+            int par = 0;
+            for (int b = tm.lane; b < nbytes; b += lpm) {
+                const unsigned v = cb[b];
+                const float4 g = gtab[v];
+                const float4 h = reinterpret_cast<const float4 *>(eh)[b];
+                const float4 l = reinterpret_cast<const float4 *>(el)[b];
+                float s01, e01, s23, e23, s4, e4;
+                two_sum(__fmul_rn(g.x, h.x), __fmul_rn(g.y, h.y), s01, e01);
+                two_sum(__fmul_rn(g.z, h.z), __fmul_rn(g.w, h.w), s23, e23);
+                two_sum(s01, s23, s4, e4);
+                const float lo4 = __fadd_rn(__fadd_rn(e01, e23), e4) +
+                                  __fmaf_rn(g.x, l.x, __fmaf_rn(g.y, l.y, __fmaf_rn(g.z, l.z, __fmul_rn(g.w, l.w))));
+                float sa, ea;
+                if (par == 0) {
+                    two_sum(A0, s4, sa, ea);
+                    A0 = sa;
+                    L0 = __fadd_rn(L0, __fadd_rn(ea, lo4));
+                } else {
+                    two_sum(A1, s4, sa, ea);
+                    A1 = sa;
+                    L1 = __fadd_rn(L1, __fadd_rn(ea, lo4));
+                }
+                par ^= 1;
+                const unsigned mm = mtab[v];
+                if (mm) {
+                    if (mm & 1u) df_add(mh, ml, h.x, l.x);
+                    if (mm & 2u) df_add(mh, ml, h.y, l.y);
+                    if (mm & 4u) df_add(mh, ml, h.z, l.z);
+                    if (mm & 8u) df_add(mh, ml, h.w, l.w);
+                }
+            }
+            float Ah = A0, Al = L0;
+            df_add(Ah, Al, A1, L1);
+            team_df_sum(Ah, Al, tm, lpm);
+            team_df_sum(mh, ml, tm, lpm);
+            if (tm.lane == 0) {
+                __int128 x1, x2, m1, m2;
+                const bool ok = fx_from_float(Ah, x1) && fx_from_float(Al, x2) && fx_from_float(mh, m1) &&
+                                fx_from_float(ml, m2);
+                if (ok) {
+                    publish(acc, x1 + x2);
+                    if (mh != 0.f || ml != 0.f)
+                        publish(acc + 2, m1 + m2);
+                } else {
+                    atomicCAS(a.err, kDevOk, kDevRange);
+                }
+            }
+        }
+        gather_store((int)((r + 1) & 1));
+        __syncthreads();
+        mark(1);
+
+        // ---- grid barrier
+        if (tid == 0) {
+            red_release_add_u64(a.counter, 1ull);
+            const unsigned long long target = (unsigned long long)(a.G + a.phantom) * (unsigned long long)(r + 1);
+            const uint64_t t0 = global_timer_ns();
+            unsigned spins = 0;
+            while (ld_acquire_u64(a.counter) < target) {
+                if ((++spins & 255u) == 0) {
+                    if (*(volatile int *)a.err != kDevOk || global_timer_ns() - t0 > a.timeout_ns) {
+                        atomicCAS(a.err, kDevOk, kDevTimeout);
+                        s_abort = 1;
+                        break;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        mark(2);
+        if (s_abort)
+            break;
+        if (r == 0) {
+            // block 0's entries were staged before the first barrier
+            copy_stage(0);
+            cp_async_commit();
+            cp_async_wait_all();
+        }
+        copy_stage((int)((r + 1) & 1));   // next block's entries: complete before the next round
+        cp_async_commit();
+
+        // ---- resolve the block: dot products at the block start, then exact
+        // Gram corrections after every residual-changing marker
+        if (tid < nb) {
+            const SweepRec &rc = ring_rec[(start + tid) & Rm];
+            const unsigned long long *acc = a.acc + (rb * kMaxSpec + tid) * 4;
+            const double tot = fx_join((long long)ld_relaxed_u64(acc), ld_relaxed_u64(acc + 1));
+            const double sm = fx_join((long long)ld_relaxed_u64(acc + 2), ld_relaxed_u64(acc + 3));
+            const double sigma = rc.t[0], cm = rc.t[1], xm = rc.t[2];
+            s_num0[tid] = (sigma * (tot - cm * (s_scal[0] - sm)) + xm * sm) + rc.beta_old * Nm1;
+            s_corr[tid] = 0.0;
+        }
+        if (tid == 0)
+            s_nupd = 0;
+        __syncthreads();
+        mark(5);
+        int next = 0, fb = 0;
+        while (true) {
+            if (tid >= next && tid < nb) {
+                const SweepRec &rc = ring_rec[(start + tid) & Rm];
+                const int g = rc.group;
+                const Pick pk = pick_fast<KM>(s_num0[tid] + s_corr[tid], rc.u, rc.z, rc.beta_old,
+                                              gcf + (size_t)g * kMaxK * 2, gconst + (size_t)g * kMaxK * 4, gk[g]);
+                s_beta[tid] = pk.beta;
+                s_acum[tid] = pk.acum0;
+                s_comp[tid] = pk.comp;
+                if (rc.beta_old != 0.0 || pk.beta != 0.0)
+                    atomicMin(&s_first[fb], tid);
+            }
+            __syncthreads();
+            ++steps;
+            const int p = s_first[fb];
+            if (p >= nb)
+                break;
+            const double dBeta = ring_rec[(start + p) & Rm].beta_old - s_beta[p];
+            if (tid > p && tid < nb)
+                s_corr[tid] += dBeta * gcur[tid * (tid - 1) / 2 + p];
+            if (tid == 0) {
+                s_upd[s_nupd++] = p;
+                s_first[fb ^ 1] = kMaxSpec;
+            }
+            fb ^= 1;
+            next = p + 1;
+            __syncthreads();
+        }
+        if (tid == 0)
+            s_first[fb] = kMaxSpec;
+        mark(3);
+
+        if (blockIdx.x == 0) {
+            if (tid < nb) {
+                const SweepRec &rc = ring_rec[(start + tid) & Rm];
+                const int c = s_comp[tid];
+                a.beta[rc.j] = s_beta[tid];
+                a.acum[rc.j] = s_acum[tid];
+                a.chosen[rc.j] = c >= 0 ? 1 : 0;
+                if (c >= 0)
+                    a.comp[rc.j] = c;
+            }
+            if (tid < 4 * kMaxSpec)
+                a.acc[((rb + 2) % 3) * kMaxSpec * 4 + tid] = 0ull;
+        }
+
+        // ---- rank-U residual update of the block
+        const int U = s_nupd;
+        if (U > 0) {
+            if (tid < 4 * U) {
+                const int u = tid >> 2, code = tid & 3;
+                const SweepRec &rc = ring_rec[(start + s_upd[u]) & Rm];
+                const double dB = rc.beta_old - s_beta[s_upd[u]];
+                const double sigma = rc.t[0], cm = rc.t[1], xm = rc.t[2];
+                const double gv = code == 0 ? 2.0 : (code == 2 ? 1.0 : 0.0);
+                const double d = code == 1 ? dB * xm : dB * ((gv - cm) * sigma);
+                float h, l;
+                df_from_double(d, h, l);
+                s_dfl[u][2 * code] = h;
+                s_dfl[u][2 * code + 1] = l;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                // the residual total moves by dBeta times the column sum of each update
+                double st = s_scal[0];
+                for (int u = 0; u < U; ++u) {
+                    const SweepRec &rc = ring_rec[(start + s_upd[u]) & Rm];
+                    st += (rc.beta_old - s_beta[s_upd[u]]) * rc.t[3];
+                }
+                s_scal[0] = st;
+            }
+            for (int i = tid; i < ns; i += kThreads) {
+                float h = eh[i], l = el[i];
+                for (int u = 0; u < U; ++u) {
+                    const unsigned slot = (start + s_upd[u]) & Rm;
+                    const unsigned c = (ring_codes[slot * a.slot_bytes + (i >> 2)] >> (2 * (i & 3))) & 3u;
+                    df_add(h, l, s_dfl[u][2 * c], s_dfl[u][2 * c + 1]);
+                }
+                eh[i] = h;
+                el[i] = l;
+            }
+        }
+        __syncthreads();
+        mark(4);
+        start += (unsigned)nb;
+        ++r;
+        rb = rb == 2 ? 0 : rb + 1;
+    }
+    if (prof) {
+        for (int k = 0; k < 5; ++k)
+            a.prof[k] = ph[k];
+        a.prof[5] = r;
+        a.prof[6] = steps;
+        a.prof[7] = ph[5];
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    // ---- epilogue
+    double s1 = 0.0, s2 = 0.0;
+    for (int i = tid; i < ns; i += kThreads) {
+        a.eps_hi[lo + i] = eh[i];
+        a.eps_lo[lo + i] = el[i];
+        const double e = (double)eh[i] + (double)el[i];
+        s1 += e;
+        s2 = fma(e, e, s2);
+    }
+    __shared__ double s_red[kThreads / 32][2];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if ((tid & 31) == 0) {
+        s_red[tid >> 5][0] = s1;
+        s_red[tid >> 5][1] = s2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double t1 = 0.0, t2 = 0.0;
+        for (int q = 0; q < kThreads / 32; ++q) {
+            t1 += s_red[q][0];
+            t2 += s_red[q][1];
+        }
+        a.part[2 * sidx] = t1;
+        a.part[2 * sidx + 1] = t2;
+        if (blockIdx.x == 0) {
+            a.stats_out[0] = 0.0;
+            *a.rounds_out = r;
+        }
+    }
+}
+
 // Sweep statistics from the resolved markers (src/BayesRBase.cpp:353-355):
 // v[g][k] counts the markers that chose component k, betasqnG[g] sums the
 // squares of the non-zero betas.  Counts and the fixed-point square sums are
@@ -976,6 +1551,38 @@ static cudaError_t launch_km(int form, int kind, const SweepArgs &a, size_t smem
 cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st)
 {
     return a.kmax <= 4 ? launch_km<4>(form, kind, a, smem, st) : launch_km<kMaxK>(form, kind, a, smem, st);
+}
+
+size_t sweep_block_smem_bytes(const SweepArgs &a)
+{
+    return make_block_plan(a.slice_max, a.slot_bytes, a.B, a.n_groups).total;
+}
+
+template <int KM>
+static cudaError_t launch_block_km(const SweepArgs &a, size_t smem, cudaStream_t st)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_sweep_block<KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    SweepArgs args = a;
+    void *params[] = {&args};
+    return cudaLaunchCooperativeKernel((const void *)k_sweep_block<KM>, dim3(a.G), dim3(kThreads), params, smem, st);
+}
+
+cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st)
+{
+    return a.kmax <= 4 ? launch_block_km<4>(a, smem, st) : launch_block_km<kMaxK>(a, smem, st);
+}
+
+int sweep_block_max_ctas_per_sm(size_t smem)
+{
+    int n = 0, m = 0;
+    cudaFuncSetAttribute(k_sweep_block<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_sweep_block<kMaxK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_block<4>, kThreads, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_block<kMaxK>, kThreads, smem) != cudaSuccess)
+        return 0;
+    return n < m ? n : m;
 }
 
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem)

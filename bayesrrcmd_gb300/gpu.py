@@ -35,6 +35,7 @@ class BrrConfig(C.Structure):
         ("seed", C.c_uint32), ("chain", C.c_uint32),
         ("v0E", C.c_double), ("s02E", C.c_double), ("v0G", C.c_double), ("s02G", C.c_double),
         ("refresh_every", C.c_int32), ("spec_width", C.c_int32), ("grid", C.c_int32), ("device", C.c_int32),
+        ("gram", C.c_int32),
     ]
 
 
@@ -61,6 +62,7 @@ EXPORTS = [
     "brr_get_marker_table", "brr_get_ragged_lists", "brr_set_groups", "brr_set_phenotype", "brr_init_chain",
     "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing", "brr_get_phase_cycles",
     "brr_set_wait_limit", "brr_xbeta", "brr_synth_bed_device", "brr_xbeta_noalloc",
+    "brr_get_gram_info",
 ]
 
 
@@ -94,6 +96,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_get_phase_cycles.argtypes = [P, C.POINTER(C.c_int64)]
     lib.brr_set_wait_limit.argtypes = [P, C.c_uint64, C.c_int32]
+    lib.brr_get_gram_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
     lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
@@ -142,6 +145,7 @@ class ChainConfig:
     spec_width: int = 0
     grid: int = 0
     device: int = 0
+    gram: int = 0
 
     def to_c(self) -> BrrConfig:
         c = BrrConfig()
@@ -154,6 +158,7 @@ class ChainConfig:
         c.seed, c.chain = self.seed & 0xFFFFFFFF, self.chain & 0xFFFFFFFF
         c.v0E, c.s02E, c.v0G, c.s02G = self.v0E, self.s02E, self.v0G, self.s02G
         c.refresh_every, c.spec_width, c.grid, c.device = self.refresh_every, self.spec_width, self.grid, self.device
+        c.gram = self.gram
         return c
 
 
@@ -285,8 +290,13 @@ class Chain:
     def set_wait_limit(self, timeout_ns: int, phantom_arrivals: int = 0):
         self._check(self.lib.brr_set_wait_limit(self.h, int(timeout_ns), int(phantom_arrivals)))
 
+    def gram_info(self):
+        b, ms, n = C.c_int32(), C.c_double(), C.c_int64()
+        self._check(self.lib.brr_get_gram_info(self.h, C.byref(b), C.byref(ms), C.byref(n)))
+        return dict(blocked=bool(b.value), build_ms=ms.value, bytes=n.value)
+
     def phase_cycles(self) -> np.ndarray:
-        out = np.zeros(6, np.int64)
+        out = np.zeros(8, np.int64)
         self._check(self.lib.brr_get_phase_cycles(self.h, _ptr(out, C.c_int64)))
         return out
 

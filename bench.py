@@ -144,6 +144,7 @@ def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chai
     ch.set_groups(group)
     ch.set_phenotype(y)
     ch.init()
+    gram = ch.gram_info()
     ch.iterate(warmup)
     torch.cuda.synchronize(device)
     t0 = time.perf_counter()
@@ -155,7 +156,7 @@ def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chai
     st = ch.state()
     ch.close()
     return dict(total_ms=total_ms, sweep_ms=sweep_ms, rounds=rounds, wall_s=wall, phases=phases.tolist(),
-                beta=st["beta"], sigmaE=st["sigmaE"], sigmaG=st["sigmaG"].tolist())
+                beta=st["beta"], sigmaE=st["sigmaE"], sigmaG=st["sigmaG"].tolist(), gram=gram)
 
 
 def run_e2e(lib, gpu, torch, device, host_bed, y, group, steps, chain_id):
@@ -319,7 +320,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": fp32c["total_ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 compensated (FP64 refresh, FP64 log-likelihoods)",
         "data": "synthetic (seeded, generated on the device)",
-        "config": {"workload": WORKLOAD, "form": "fp32c", "refresh_every": REFRESH,
+        "config": {"workload": WORKLOAD, "form": "fp32c" + (" gram-blocked" if fp32c["gram"]["blocked"] else ""),
+                   "refresh_every": REFRESH,
                    "l2": "inputs larger than L2 (2.5 GB of codes per sweep)", "parallelism": "replicas" if world > 1 else "1 chain"},
         "plain_fp64": {"value": plain_rate, "unit": "marker-updates/s", "ms_per_step": fp64["total_ms"] / args.steps,
                        "speedup_chosen_vs_plain": value / world / plain_rate,
@@ -332,7 +334,10 @@ def main():
                      "kernel": "k_sweep (FP32C, dense)", "algorithmic_bytes_per_launch": bytes_per_sweep},
         "phases_clk_per_round": {k: v / max(fp32c["phases"][5], 1) for k, v in
                                  zip(["prefetch", "dot", "barrier", "sample", "update"], fp32c["phases"][:5])},
+        "sampling_steps_per_round": fp32c["phases"][6] / max(fp32c["phases"][5], 1),
         "rounds_per_step": fp32c["rounds"] / args.steps,
+        "gram": {"blocked_sweep": fp32c["gram"]["blocked"], "build_ms": fp32c["gram"]["build_ms"],
+                 "bytes": fp32c["gram"]["bytes"]},
         "gpu_launches": 5 * args.steps + (args.steps + args.warmup) // REFRESH,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,

@@ -79,6 +79,8 @@ typedef struct brr_config {
     int32_t spec_width;        /* markers resolved per grid round (0: form default) */
     int32_t grid;              /* CTAs of the persistent sweep (0: one per SM) */
     int32_t device;            /* CUDA device ordinal */
+    int32_t gram;              /* FP32C dense: 0 blocked sweep with a precomputed marker Gram when it fits
+                                  in device memory, -1 never, 1 required */
 } brr_config;
 
 /* Chain state; arrays are caller-owned, sized M (beta, comp, acum) and N (eps).
@@ -186,11 +188,17 @@ int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_
  * than exist, so that tests can exercise the timeout path without a fault. */
 int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arrivals);
 
+/* Whether the chain runs the Gram-blocked FP32C sweep, the device time of
+ * building the packed marker Gram (ms) and its size in bytes. */
+int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes);
+
 /* Per-phase SM cycles of the sweeps of the last brr_iterate / brr_sweep call,
  * measured on the first CTA (the counterpart of the reference's per-column
- * timing log, src/BayesRBase.cpp:381-389): [0] ring prefetch and wait,
- * [1] partial dot products, [2] grid barrier, [3] component sampling,
- * [4] outputs and residual update, [5] grid rounds. */
+ * timing log, src/BayesRBase.cpp:381-389), 8 values: [0] ring prefetch and
+ * wait, [1] partial dot products, [2] grid barrier, [3] component sampling,
+ * [4] outputs and residual update, [5] grid rounds, [6] sampling steps
+ * (blocked sweep), [7] cycles of [3] spent assembling the block's dot products
+ * (blocked sweep). */
 int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles);
 
 #ifdef __cplusplus

@@ -228,3 +228,46 @@ def test_call_order_errors(gpu_lib):
         ch.set_groups(np.array([0, 1, 0], np.int32))
     with pytest.raises(gpu.BrrError):
         ch.set_phenotype(np.full(100, np.nan, np.float32))
+
+
+@pytest.mark.parametrize("miss", [0.0, 0.02])
+def test_gram_blocked_fp32c_matches_restart_fp32c_and_oracle(gpu_lib, miss):
+    """The blocked FP32C sweep (exact Gram corrections, fixed rounds of B
+    markers) follows the same chain as the restart sweep and the FP64 oracle:
+    identical components, beta within 1e-9 relative."""
+    N, M = 3000, 700
+    bed, y = problem(N, M, seed=51, miss=miss)
+    group = (np.arange(M) % 2).astype(np.int32)
+    blocked = make_gpu(bed, N, y, S2, 0, form=gpu.FORM_FP32C, group=group, seed=8, refresh_every=3, gram=1)
+    assert blocked.gram_info()["blocked"]
+    restart = make_gpu(bed, N, y, S2, 0, form=gpu.FORM_FP32C, group=group, seed=8, refresh_every=3, gram=-1)
+    assert not restart.gram_info()["blocked"]
+    oc = O.OracleChain(bed, N, y, S2, kind=0, group=group, seed=8)
+    for it in range(4):
+        blocked.iterate(1)
+        restart.iterate(1)
+        oc.iterate(it)
+        b, r, o = blocked.state(), restart.state(), oc.state()
+        for s in (b, r):
+            np.testing.assert_array_equal(s["comp"], o["comp"])
+            nz = o["beta"] != 0
+            np.testing.assert_allclose(s["beta"][nz], o["beta"][nz], rtol=1e-9, atol=1e-13)
+            np.testing.assert_allclose(s["eps"], o["eps"], rtol=0, atol=1e-10)
+            np.testing.assert_allclose(s["sigmaG"], o["sigmaG"], rtol=1e-9)
+    sw, tot, rounds = blocked.timing()
+    assert rounds == -(-M // 64)
+
+
+@pytest.mark.parametrize("width", [16, 32])
+def test_gram_blocked_other_widths(gpu_lib, width):
+    N, M = 1500, 333
+    bed, y = problem(N, M, seed=61)
+    ch = make_gpu(bed, N, y, S1, 0, form=gpu.FORM_FP32C, seed=4, gram=1, spec_width=width)
+    oc = O.OracleChain(bed, N, y, S1, kind=0, seed=4)
+    for it in range(3):
+        ch.iterate(1)
+        oc.iterate(it)
+        s, o = ch.state(), oc.state()
+        np.testing.assert_array_equal(s["comp"], o["comp"])
+        nz = o["beta"] != 0
+        np.testing.assert_allclose(s["beta"][nz], o["beta"][nz], rtol=1e-9, atol=1e-13)
