@@ -114,6 +114,8 @@ struct brr_ctx {
     double *d_nzb = nullptr;
     double *d_gram = nullptr;           // blocked FP32C: packed marker Gram
     double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries of two blocks
+    BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
+    float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)
     bool blocked = false;
     bool has_missing = false;
     double gram_ms = 0.0;
@@ -136,7 +138,7 @@ struct brr_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
     int64_t last_rounds = 0;
-    long long phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // summed over the sweeps of the last call
+    long long phase[12] = {};   // summed over the sweeps of the last call
     uint64_t wait_limit_ns = 2000000000ull;
     int phantom = 0;
 
@@ -189,6 +191,8 @@ void free_all(brr_ctx *c)
     cudaFree(c->d_nzb);
     cudaFree(c->d_gram);
     cudaFree(c->d_gstage);
+    cudaFree(c->d_brec);
+    cudaFree(c->d_bdf);
     cudaFreeHost(c->h_order);
     cudaFreeHost(c->h_stats);
     cudaFreeHost(c->h_part);
@@ -285,8 +289,12 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     group_constants(c, gc, gK);
     BRR_CUDA(cudaMemcpyAsync(c->d_gconst, gc.data(), sizeof(double) * gc.size(), cudaMemcpyHostToDevice, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->d_gK, gK.data(), sizeof(int32_t) * gK.size(), cudaMemcpyHostToDevice, c->st));
-    BRR_CUDA(launch_gather(cf.form, cf.kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u, c->d_z,
-                           c->d_group, c->d_colsum, c->d_rec, c->st));
+    if (c->blocked)
+        BRR_CUDA(launch_gather_block(c->d_order, cf.M, cf.N, c->d_table, c->d_scale, c->d_beta, c->d_u, c->d_z,
+                                     c->d_group, eps_total, c->d_brec, c->st));
+    else
+        BRR_CUDA(launch_gather(cf.form, cf.kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u,
+                               c->d_z, c->d_group, c->d_colsum, c->d_rec, c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + 1), c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
 
@@ -333,7 +341,11 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     a.phantom = c->phantom;
     a.gram = c->d_gram;
     a.gstage = c->d_gstage;
-    BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 8, c->st));
+    a.has_missing = c->has_missing ? 1 : 0;
+    a.brec = c->d_brec;
+    a.beta_df = c->d_bdf;
+    a.acum_df = c->d_bdf ? c->d_bdf + cf.M : nullptr;
+    BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 12, c->st));
     const size_t smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, cf.kind, a);
 
     BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
@@ -342,6 +354,8 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     else
         BRR_CUDA(launch_sweep(cf.form, cf.kind, a, smem, c->st));
     BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
+    if (c->blocked)
+        BRR_CUDA(launch_block_finish(cf.M, c->d_chosen, a.beta_df, a.acum_df, c->d_beta, c->d_acum, c->st));
 
     const int ng = cf.n_groups;
     BRR_CUDA(launch_sweep_stats(cf.M, c->d_group, c->d_comp, c->d_chosen, c->d_beta, ng, c->d_vstat, c->st));
@@ -350,14 +364,14 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     BRR_CUDA(cudaMemcpyAsync(vstat.data(), c->d_vstat, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->h_part, c->d_part, sizeof(double) * 2 * c->G, cudaMemcpyDeviceToHost, c->st));
-    long long rounds = 0, prof[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long rounds = 0, prof[12] = {};
     BRR_CUDA(cudaMemcpyAsync(&rounds, c->d_rounds, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(prof, c->d_prof, sizeof(prof), cudaMemcpyDeviceToHost, c->st));
     const int rc = check_device_status(c);
     if (rc)
         return rc;
     BRR_CUDA(cudaEventElapsedTime(sweep_ms, c->ev[0], c->ev[1]));
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < 12; ++k)
         c->phase[k] += prof[k];
 
     for (int g = 0; g < ng; ++g)
@@ -463,8 +477,11 @@ int prepare_blocked(brr_ctx *c)
         c->blocked = false;
         return BRR_OK;
     }
-    if (cudaMalloc((void **)&c->d_gram, gram_bytes) != cudaSuccess) {
+    if (cudaMalloc((void **)&c->d_gram, gram_bytes) != cudaSuccess ||
+        (!c->d_brec && cudaMalloc((void **)&c->d_brec, sizeof(BlockRec) * (size_t)cf.M) != cudaSuccess) ||
+        (!c->d_bdf && cudaMalloc((void **)&c->d_bdf, sizeof(float2) * 2 * (size_t)cf.M) != cudaSuccess)) {
         cudaGetLastError();
+        cudaFree(c->d_gram);
         c->d_gram = nullptr;
         if (cf.gram > 0)
             return fail(BRR_ERR_OOM, "allocation of the marker Gram failed");
@@ -476,7 +493,6 @@ int prepare_blocked(brr_ctx *c)
     if (build_gram(c->d_codes, c->col_stride, cf.N, cf.M, c->d_scale, c->d_counts, c->has_missing, c->d_gram, c->st,
                    why) != 0) {
         cudaFree(c->d_gram);
-    cudaFree(c->d_gstage);
         c->d_gram = nullptr;
         return fail(BRR_ERR_CUDA, "building the marker Gram failed: " + why);
     }
@@ -640,7 +656,7 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
             dalloc(&c.d_gconst, (size_t)cf.n_groups * kMaxK * 4) || dalloc(&c.d_gK, (size_t)cf.n_groups) ||
             dalloc(&c.d_stats, (size_t)cf.n_groups * kMaxK + cf.n_groups + 1) ||
             dalloc(&c.d_part, (size_t)std::max(2 * c.G, kPartBlocks)) || dalloc(&c.d_err, 1) ||
-            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 8) || dalloc(&c.d_gstage, (size_t)kMaxSpec * (kMaxSpec - 1)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
+            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 12) || dalloc(&c.d_gstage, (size_t)kMaxSpec * (kMaxSpec - 1)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
             dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M))
             return fail(BRR_ERR_OOM, "device allocation failed");
         if (cf.form == BRR_FORM_FP64) {
@@ -1147,7 +1163,7 @@ int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles)
 {
     if (!ctx || !cycles)
         return fail(BRR_ERR_ARG, "null argument");
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < 12; ++k)
         cycles[k] = ctx->phase[k];
     return BRR_OK;
 }

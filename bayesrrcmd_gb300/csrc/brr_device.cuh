@@ -170,4 +170,56 @@ __device__ __forceinline__ void df_from_double(double v, float &hi, float &lo)
     lo = __double2float_rn(v - (double)hi);
 }
 
+// Double-float product (ah, al) * (bh, bl): exact product of the high words by
+// FMA, cross terms added once, renormalised (relative error below 2^-44).
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float &h, float &l)
+{
+    const float p = __fmul_rn(ah, bh);
+    const float e = __fmaf_rn(ah, bh, -p);
+    const float t = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+    h = __fadd_rn(p, t);
+    l = __fsub_rn(t, __fsub_rn(h, p));
+}
+
+// Fixed-point sum (hi, lo) (value hi * 2^-4 + lo * 2^-60; lo is an unsigned
+// 64-bit sum of 56-bit parts) to a double-float pair with integer operations
+// only: the 128-bit value is assembled with its carry, the magnitude is
+// normalised by a leading-zero count and its top 48 bits become two exact
+// floats (truncation, relative error below 2^-47).
+__device__ __forceinline__ void fx_to_df(long long hi, unsigned long long lo, float &h, float &l)
+{
+    // X = hi * 2^56 + lo as (xh, xl) = (X >> 64, X mod 2^64)
+    unsigned long long xl = ((unsigned long long)hi << 56) + lo;
+    unsigned long long xh = (unsigned long long)(hi >> 8) + (xl < lo ? 1ull : 0ull);
+    const bool neg = (long long)xh < 0;
+    if (neg) {
+        xl = ~xl + 1ull;
+        xh = ~xh + (xl == 0ull ? 1ull : 0ull);
+    }
+    if ((xh | xl) == 0ull) {
+        h = l = 0.f;
+        return;
+    }
+    const int lz = xh ? __clzll((long long)xh) : 64 + __clzll((long long)xl);
+    unsigned long long th;
+    if (lz >= 64)
+        th = xl << (lz - 64);
+    else if (lz == 0)
+        th = xh;
+    else
+        th = (xh << lz) | (xl >> (64 - lz));
+    const unsigned m1 = (unsigned)(th >> 40);              // top 24 bits (bit 23 set)
+    const unsigned m2 = (unsigned)(th >> 16) & 0xFFFFFFu;  // next 24 bits
+    // bit 127 of the normalised magnitude weighs 2^(67 - lz); m1's lowest bit 2^(44 - lz)
+    const int e1 = 44 - lz;
+    const float s1 = __int_as_float((e1 + 127) << 23);
+    const float s2 = __int_as_float((e1 - 24 + 127) << 23);
+    h = __fmul_rn(__uint2float_rn(m1), s1);
+    l = __fmul_rn(__uint2float_rn(m2), s2);
+    if (neg) {
+        h = -h;
+        l = -l;
+    }
+}
+
 }  // namespace brr

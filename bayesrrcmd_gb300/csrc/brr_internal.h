@@ -25,6 +25,31 @@ struct alignas(16) SweepRec {
 };
 static_assert(sizeof(SweepRec) == 64, "SweepRec must be 64 bytes");
 
+// Record of the Gram-blocked FP32C dense sweep.  FP64 arithmetic issues at a
+// small fraction of the FP32 rate on this GPU, so every per-marker quantity the
+// resolve and the residual update need is prepared here once per sweep, by a
+// kernel over all markers, as a double-float pair (hi, lo):
+//   num = sigma * sum(g*eps) + cst + dm * sum_missing(eps)
+// with cst = beta_old*(N-1) - sigma*colmean*S and dm = sigma*colmean + xm
+// (S: sum of the residual at the sweep start, xm: value of a missing genotype).
+struct alignas(16) BlockRec {
+    float x[8];          // standardised value per 2-bit code c at x[2c], x[2c+1]
+    float sig[2];        // sigma
+    float cst[2];        // constant part of num
+    float dm[2];         // coefficient of the missing-genotype sum
+    float bo[2];         // beta_old
+    float zf[2];         // z
+    float uf;            // u rounded to FP32 (certified sampler)
+    uint32_t bnz;        // beta_old != 0
+    double beta_old;     // FP64 draws for the sampler's FP64 fallback
+    double u;
+    double z;
+    uint32_t j;
+    int32_t group;
+    uint32_t pad[4];
+};
+static_assert(sizeof(BlockRec) == 128, "BlockRec must be 128 bytes");
+
 struct SweepArgs {
     int64_t N, M;
     int G;                       // CTAs (slices of individuals)
@@ -61,6 +86,10 @@ struct SweepArgs {
     int phantom;                 // extra arrivals the barrier waits for (tests of the timeout path)
     const double *gram;          // blocked FP32C sweep: packed lower-triangle marker Gram (FP64)
     double *gstage;              // blocked FP32C sweep: 2 x B(B-1)/2 staged Gram entries
+    int has_missing;             // any missing genotype in the packed markers
+    const BlockRec *brec;        // blocked FP32C sweep: M records in sweep order
+    float2 *beta_df;             // blocked FP32C sweep: new beta per marker (hi, lo)
+    float2 *acum_df;             // blocked FP32C sweep: acum per marker (hi, lo)
 };
 
 // Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).
@@ -99,6 +128,11 @@ cudaError_t noalloc_xbeta(int dev, cudaStream_t st, int kind, int64_t N, const u
                           std::string &why);
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem);
 size_t sweep_block_smem_bytes(const SweepArgs &a);
+cudaError_t launch_gather_block(const uint32_t *order, int64_t M, int64_t N, const double *table,
+                                const double *scale, const double *beta, const double *u, const double *z,
+                                const int32_t *group, double eps_total, BlockRec *rec, cudaStream_t st);
+cudaError_t launch_block_finish(int64_t M, const uint8_t *chosen, const float2 *beta_df, const float2 *acum_df,
+                                double *beta, double *acum, cudaStream_t st);
 cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st);
 int sweep_block_max_ctas_per_sm(size_t smem);
 cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work);
