@@ -113,7 +113,7 @@ struct brr_ctx {
     uint32_t *d_nzj = nullptr;
     double *d_nzb = nullptr;
     double *d_gram = nullptr;           // blocked FP32C: packed marker Gram
-    double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries of two blocks
+    double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries (8 blocks)
     BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
     float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)
     bool blocked = false;
@@ -204,7 +204,9 @@ void free_all(brr_ctx *c)
 }
 
 constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
-constexpr size_t kAccWords = 3 * kMaxSpec * 4;
+// fixed-point accumulators: 3 rotating buffers of the restart sweep, 8 of the
+// blocked sweep; followed by two barrier counters
+constexpr size_t kAccWords = 8 * kMaxSpec * 4;
 
 // Per-group sampler constants for the current sigmaE, sigmaG, pi
 // (src/BayesRBase.cpp:309-333): c_k = log(pi_k) - log(sigmaG/sigmaE*(N-1)*cVa_k + 1)/2,
@@ -295,7 +297,7 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     else
         BRR_CUDA(launch_gather(cf.form, cf.kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u,
                                c->d_z, c->d_group, c->d_colsum, c->d_rec, c->st));
-    BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + 1), c->st));
+    BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + 2), c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
 
     SweepArgs a{};
@@ -652,11 +654,11 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
             dalloc(&c.d_vstat, (size_t)cf.n_groups * kMaxK + 2 * cf.n_groups) ||
             dalloc(&c.d_slice_lo, (size_t)c.G + 1) || dalloc(&c.d_beta, (size_t)M) || dalloc(&c.d_comp, (size_t)M) ||
             dalloc(&c.d_acum, (size_t)M) || dalloc(&c.d_order, (size_t)M) || dalloc(&c.d_u, (size_t)M) ||
-            dalloc(&c.d_z, (size_t)M) || dalloc(&c.d_rec, (size_t)M) || dalloc(&c.d_acc, kAccWords + 1) ||
+            dalloc(&c.d_z, (size_t)M) || dalloc(&c.d_rec, (size_t)M) || dalloc(&c.d_acc, kAccWords + 2) ||
             dalloc(&c.d_gconst, (size_t)cf.n_groups * kMaxK * 4) || dalloc(&c.d_gK, (size_t)cf.n_groups) ||
             dalloc(&c.d_stats, (size_t)cf.n_groups * kMaxK + cf.n_groups + 1) ||
             dalloc(&c.d_part, (size_t)std::max(2 * c.G, kPartBlocks)) || dalloc(&c.d_err, 1) ||
-            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 12) || dalloc(&c.d_gstage, (size_t)kMaxSpec * (kMaxSpec - 1)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
+            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 12) || dalloc(&c.d_gstage, sweep_block_stage_bytes(kMaxSpec) / sizeof(double)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
             dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M))
             return fail(BRR_ERR_OOM, "device allocation failed");
         if (cf.form == BRR_FORM_FP64) {

@@ -74,8 +74,8 @@ struct SweepArgs {
     double mu_new;               // subtracted from eps while it is loaded (updateMu, second half)
     double epsSum;               // ragged running sum at sweep start (after updateMu)
     double eps_total;            // dense FP32C: sum of the residual at sweep start (after updateMu)
-    unsigned long long *acc;     // [3][kMaxSpec][4] fixed-point accumulators (sum, missing sum)
-    unsigned long long *counter; // grid round counter, zero at launch
+    unsigned long long *acc;     // [kAccBuffers][kMaxSpec][4] fixed-point accumulators (sum, missing sum)
+    unsigned long long *counter; // grid round counter(s), zero at launch (blocked sweep: two)
     double *stats_out;           // [0]: ragged running sum at sweep end
     uint8_t *chosen;             // M flags: marker chose a component in this sweep
     double *part;                // [G][2] per-slice sum(eps), sum(eps^2) after the sweep
@@ -85,7 +85,7 @@ struct SweepArgs {
     uint64_t timeout_ns;         // limit of any single wait
     int phantom;                 // extra arrivals the barrier waits for (tests of the timeout path)
     const double *gram;          // blocked FP32C sweep: packed lower-triangle marker Gram (FP64)
-    double *gstage;              // blocked FP32C sweep: 2 x B(B-1)/2 staged Gram entries
+    double *gstage;              // blocked FP32C sweep: staged Gram entries (sweep_block_stage_bytes)
     int has_missing;             // any missing genotype in the packed markers
     const BlockRec *brec;        // blocked FP32C sweep: M records in sweep order
     float2 *beta_df;             // blocked FP32C sweep: new beta per marker (hi, lo)
@@ -134,6 +134,8 @@ cudaError_t launch_gather_block(const uint32_t *order, int64_t M, int64_t N, con
 cudaError_t launch_block_finish(int64_t M, const uint8_t *chosen, const float2 *beta_df, const float2 *acum_df,
                                 double *beta, double *acum, cudaStream_t st);
 cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st);
+size_t sweep_block_stage_bytes(int B);   // global Gram staging of the blocked sweep
+int sweep_block_threads();
 int sweep_block_max_ctas_per_sm(size_t smem);
 cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work);
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,

@@ -1,0 +1,121 @@
+// Reference component sampler (FP64 with an optional certified FP32 path),
+// shared by the restart sweep and the blocked sweep.
+#pragma once
+#include <math.h>
+
+#include "brr_device.cuh"
+
+namespace brr {
+
+// Component selection for one marker by one thread (src/BayesRBase.cpp:309-366).
+// logL_k = c_k + h_k*num^2 with c_k = log(pi_k) - log(sigmaG/sigmaE*(N-1)*cVa_k + 1)/2
+// and h_k = 1/(2*denom_k*sigmaE).  P(k) = exp(logL_k - max)/sum, zeroed where the
+// reference's 700 guards fire (any |logL_q - logL_k| > 700 over q >= 1); the
+// walk picks the first k whose cumulative probability reaches u.
+// FP32 = true evaluates the exponentials in single precision from the FP64
+// log-likelihood differences and keeps the decision only when u is further
+// than 2e-5 from every cumulative bound it was compared with (the FP32 error
+// is below 5e-6); otherwise the FP64 evaluation decides.
+struct Pick {
+    int comp;       // chosen component, -1 if none
+    double beta;    // new beta (beta_old when none)
+    double acum0;   // P(component 0) as stored in acum
+};
+
+template <bool FP32, int KM>
+__device__ __forceinline__ Pick pick_marker(double num, double u, double z, double beta_old,
+                                            const double *__restrict__ gc, int K)
+{
+    double L[KM];
+    const double n2 = num * num;
+#pragma unroll
+    for (int k = 0; k < KM; ++k)
+        L[k] = k < K ? (k == 0 ? gc[0] : fma(gc[4 * k + 2], n2, gc[4 * k])) : -INFINITY;
+    double lmax = L[0], lmax1 = L[1], lmin1 = L[1];
+#pragma unroll
+    for (int k = 1; k < KM; ++k) {
+        if (k < K) {
+            lmax = fmax(lmax, L[k]);
+            lmax1 = fmax(lmax1, L[k]);
+            lmin1 = fmin(lmin1, L[k]);
+        }
+    }
+    // the guards of components q >= 1 can only fire when the log-likelihoods of
+    // components 1..K-1 span more than 700
+    const bool wide = lmax1 - lmin1 > 700.0;
+    const bool guard0 = (lmax1 - L[0] > 700.0) || (L[0] - lmin1 > 700.0);
+    auto guarded = [&](int k) -> bool {
+        return k == 0 ? guard0 : (wide && ((lmax1 - L[k] > 700.0) || (L[k] - lmin1 > 700.0)));
+    };
+    Pick res;
+    res.comp = -1;
+    res.beta = beta_old;
+    res.acum0 = 0.0;
+    bool decided = false;
+    if (FP32) {
+        float e[KM];
+        float es = 0.f;
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+            e[k] = k < K ? __expf((float)(L[k] - lmax)) : 0.f;
+            es += e[k];
+        }
+        const float ies = __frcp_rn(es);
+        int chosen = -1;
+        float acum = 0.f, prev = 0.f, a0 = 0.f;
+        const float uf = (float)u;
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+            if (k < K && chosen < 0) {
+                const float pk = guarded(k) ? 0.f : e[k] * ies;
+                if (k == 0)
+                    a0 = pk;
+                prev = acum;
+                acum += pk;
+                if (uf <= acum)
+                    chosen = k;
+            }
+        }
+        const float tol = 2e-5f;
+        const bool close = chosen >= 0 ? ((uf > acum - tol) || (chosen > 0 && uf < prev + tol)) : (uf < acum + tol);
+        if (!close) {
+            res.comp = chosen;
+            res.acum0 = (double)a0;
+            decided = true;
+        }
+    }
+    if (!decided) {
+        double e[KM];
+        double es = 0.0;
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+            e[k] = k < K ? exp(L[k] - lmax) : 0.0;
+            es += e[k];
+        }
+        const double ies = 1.0 / es;
+        int chosen = -1;
+        double acum = 0.0, a0 = 0.0;
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+            if (k < K && chosen < 0) {
+                const double pk = guarded(k) ? 0.0 : e[k] * ies;
+                if (k == 0)
+                    a0 = pk;
+                acum += pk;
+                if (u <= acum)
+                    chosen = k;
+            }
+        }
+        res.comp = chosen;
+        res.acum0 = a0;
+    }
+    if (res.comp == 0) {
+        res.beta = 0.0;
+    } else if (res.comp > 0) {
+        const double sdk = gc[4 * res.comp + 3], invden = gc[4 * res.comp + 1];
+        res.beta = __dadd_rn(__dmul_rn(z, sdk), __dmul_rn(num, invden));
+    }
+    return res;
+}
+
+}  // namespace brr

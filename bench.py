@@ -333,8 +333,8 @@ def main():
                      "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
                      "kernel": "k_sweep (FP32C, dense)", "algorithmic_bytes_per_launch": bytes_per_sweep},
         "phases_clk_per_round": {k: v / max(fp32c["phases"][5], 1) for k, v in
-                                 zip(["prefetch", "dot", "barrier", "sample", "update", "block_inputs", "of_sample_picks",
-                                      "of_sample_steps", "of_dot_reduce"],
+                                 zip(["ring_wait", "dot_side", "barrier_wait", "sample", "update", "block_inputs",
+                                      "of_sample_picks", "of_sample_steps", "dot_side_idle"],
                                      [*fp32c["phases"][:5], fp32c["phases"][7], *fp32c["phases"][9:12]])},
         "sampling_steps_per_round": fp32c["phases"][6] / max(fp32c["phases"][5], 1),
         "fp64_fallbacks_per_step": fp32c["phases"][8] / args.steps,
