@@ -138,7 +138,7 @@ struct brr_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
     int64_t last_rounds = 0;
-    long long phase[12] = {};   // summed over the sweeps of the last call
+    long long phase[16] = {};   // summed over the sweeps of the last call
     uint64_t wait_limit_ns = 2000000000ull;
     int phantom = 0;
 
@@ -204,9 +204,11 @@ void free_all(brr_ctx *c)
 }
 
 constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
-// fixed-point accumulators: 3 rotating buffers of the restart sweep, 8 of the
-// blocked sweep; followed by two barrier counters
-constexpr size_t kAccWords = 8 * kMaxSpec * 4;
+// fixed-point accumulators: 3 rotating buffers of the restart sweep, 8 buffers
+// of 8 copies for the blocked sweep; followed by the barrier counters (restart
+// sweep: the first word; blocked sweep: 2 x 8 counters 16 words apart)
+constexpr size_t kAccWords = 8 * 8 * kMaxSpec * 4;
+constexpr size_t kCounterWords = 2 * 8 * 16;
 
 // Per-group sampler constants for the current sigmaE, sigmaG, pi
 // (src/BayesRBase.cpp:309-333): c_k = log(pi_k) - log(sigmaG/sigmaE*(N-1)*cVa_k + 1)/2,
@@ -297,7 +299,7 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     else
         BRR_CUDA(launch_gather(cf.form, cf.kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u,
                                c->d_z, c->d_group, c->d_colsum, c->d_rec, c->st));
-    BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + 2), c->st));
+    BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + kCounterWords), c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
 
     SweepArgs a{};
@@ -347,7 +349,7 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     a.brec = c->d_brec;
     a.beta_df = c->d_bdf;
     a.acum_df = c->d_bdf ? c->d_bdf + cf.M : nullptr;
-    BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 12, c->st));
+    BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 16, c->st));
     const size_t smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, cf.kind, a);
 
     BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
@@ -366,14 +368,14 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     BRR_CUDA(cudaMemcpyAsync(vstat.data(), c->d_vstat, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(c->h_part, c->d_part, sizeof(double) * 2 * c->G, cudaMemcpyDeviceToHost, c->st));
-    long long rounds = 0, prof[12] = {};
+    long long rounds = 0, prof[16] = {};
     BRR_CUDA(cudaMemcpyAsync(&rounds, c->d_rounds, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
     BRR_CUDA(cudaMemcpyAsync(prof, c->d_prof, sizeof(prof), cudaMemcpyDeviceToHost, c->st));
     const int rc = check_device_status(c);
     if (rc)
         return rc;
     BRR_CUDA(cudaEventElapsedTime(sweep_ms, c->ev[0], c->ev[1]));
-    for (int k = 0; k < 12; ++k)
+    for (int k = 0; k < 16; ++k)
         c->phase[k] += prof[k];
 
     for (int g = 0; g < ng; ++g)
@@ -472,10 +474,12 @@ int prepare_blocked(brr_ctx *c)
     a.slice_max = c->slice_max;
     a.slot_bytes = c->slot_bytes;
     const size_t smem = sweep_block_smem_bytes(a);
-    const int per_sm = sweep_block_max_ctas_per_sm(smem);
+    std::string occ_why;
+    const int per_sm = sweep_block_max_ctas_per_sm(smem, &occ_why);
     if (per_sm < 1 || (int64_t)per_sm * c->sms < c->G) {
         if (cf.gram > 0)
-            return fail(BRR_ERR_ARG, "the blocked sweep does not fit its CTAs");
+            return fail(BRR_ERR_ARG, "the blocked sweep does not fit its CTAs: " +
+                                         (occ_why.empty() ? std::to_string(per_sm) + " per SM" : occ_why));
         c->blocked = false;
         return BRR_OK;
     }
@@ -654,11 +658,11 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
             dalloc(&c.d_vstat, (size_t)cf.n_groups * kMaxK + 2 * cf.n_groups) ||
             dalloc(&c.d_slice_lo, (size_t)c.G + 1) || dalloc(&c.d_beta, (size_t)M) || dalloc(&c.d_comp, (size_t)M) ||
             dalloc(&c.d_acum, (size_t)M) || dalloc(&c.d_order, (size_t)M) || dalloc(&c.d_u, (size_t)M) ||
-            dalloc(&c.d_z, (size_t)M) || dalloc(&c.d_rec, (size_t)M) || dalloc(&c.d_acc, kAccWords + 2) ||
+            dalloc(&c.d_z, (size_t)M) || dalloc(&c.d_rec, (size_t)M) || dalloc(&c.d_acc, kAccWords + kCounterWords) ||
             dalloc(&c.d_gconst, (size_t)cf.n_groups * kMaxK * 4) || dalloc(&c.d_gK, (size_t)cf.n_groups) ||
             dalloc(&c.d_stats, (size_t)cf.n_groups * kMaxK + cf.n_groups + 1) ||
             dalloc(&c.d_part, (size_t)std::max(2 * c.G, kPartBlocks)) || dalloc(&c.d_err, 1) ||
-            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 12) || dalloc(&c.d_gstage, sweep_block_stage_bytes(kMaxSpec) / sizeof(double)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
+            dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 16) || dalloc(&c.d_gstage, sweep_block_stage_bytes(kMaxSpec) / sizeof(double)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
             dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M))
             return fail(BRR_ERR_OOM, "device allocation failed");
         if (cf.form == BRR_FORM_FP64) {
@@ -1165,7 +1169,7 @@ int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles)
 {
     if (!ctx || !cycles)
         return fail(BRR_ERR_ARG, "null argument");
-    for (int k = 0; k < 12; ++k)
+    for (int k = 0; k < 16; ++k)
         cycles[k] = ctx->phase[k];
     return BRR_OK;
 }

@@ -7,10 +7,14 @@
 // (packed lower triangle, FP64, brr_gram.cu).
 //
 // The sweep order is cut into blocks of B consecutive markers.  One CTA per SM
-// owns a slice of individuals and keeps its residual slice in shared memory as
-// double-float.  Block q's dot products x_t . eps are computed by every CTA
-// over its slice and summed across CTAs by exact 128-bit fixed-point integer
-// atomics; a grid-wide counter barrier publishes the sums.  Every CTA then
+// owns a slice of individuals and keeps its residual slice in shared memory in
+// fixed point, E = eps * 2^50 as a signed 64-bit integer stored as four
+// balanced 16-bit limbs.  Block q's dot products sum_i g_i E_i (g in {0,1,2}
+// the genotype) are exact integer sums: dp2a (two int16 x int8 products per
+// instruction) over the limbs, one warp per 8 markers; they are summed across
+// CTAs by exact 128-bit fixed-point integer atomics, and a grid-wide counter
+// barrier publishes the sums.  The residual update adds dBeta * x rounded to
+// the 2^-50 grid.  Every CTA then
 // resolves block q identically: the markers are sampled in order of the
 // block, and after every marker p that changes the residual the later markers'
 // dot products move by dBeta_p * G[p, t] (exact sequential chain up to
@@ -34,10 +38,12 @@
 // Buffers and why their counts suffice (iteration r: dot side publishes block
 // r+1, stages block r+2, arrives at barrier r+1; resolve side waits for barrier
 // r, reads block r's sums, copies block r+1's Gram entries):
-//  * two barrier counters, barrier q on counter q % 2 with target
-//    (G + phantom) * (q / 2 + 1): a CTA arrives at barrier q+2 only after its
-//    resolve warp passed barrier q, so two barriers at most are open;
-//  * 8 fixed-point accumulator buffers (block q in buffer q % 8): the first
+//  * two sets of barrier counters, barrier q on set q % 2, each set 8 counters
+//    (CTA s on counter s % 8, target its CTA count * (q / 2 + 1)): a CTA
+//    arrives at barrier q+2 only after it passed barrier q, so two barriers at
+//    most are open;
+//  * 8 fixed-point accumulator buffers (block q in buffer q % 8), each with 8
+//    copies (CTA s adds into copy s % 8, the reader sums them): the first
 //    CTA zeroes block q+3's buffer in iteration q before arriving at barrier
 //    q+1, after it passed barrier q-1, which every CTA arrived at after it had
 //    read the sums of block q-3 and earlier (the buffer last held block q-5);
@@ -48,6 +54,8 @@
 //  * ring of 4B records and 4B code slots: iteration r holds blocks r..r+2
 //    (codes) and r..r+3 (records).
 #include <cuda_runtime.h>
+
+#include <string>
 
 #include "brr_device.cuh"
 #include "brr_internal.h"
@@ -60,6 +68,12 @@ namespace {
 constexpr int kDotWarps = 8;
 constexpr int kBlockThreads = (kDotWarps + 1) * 32;
 constexpr int kAccBufs = 8;
+constexpr int kAccCopies = 8;   // CTA s adds into copy s % 8: 19 atomics per address and block, not 152
+constexpr int kAccBufWords = kAccCopies * kMaxSpec * 4;
+// Barrier counters: per barrier parity 8 counters 128 bytes apart; CTA s arrives
+// on counter s % 8, so 19 arrivals (not 152) serialise on one address.
+constexpr int kCounters = 8;
+constexpr int kCounterStride = 16;
 constexpr int kStageSlots = 8;
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -69,7 +83,8 @@ __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15
 __host__ __device__ inline size_t block_gram_entries(int B) { return (size_t)B * (B - 1) / 2 + (size_t)B * B; }
 
 struct PipePlan {
-    size_t eps_hi, eps_lo;  // double-float residual slice
+    size_t planes;          // residual limb planes: 8 words per 4 individuals
+    size_t fix;             // residual in fixed point: one int64 per individual
     size_t codes;           // R x slot_bytes genotype codes
     size_t recs;            // R x BlockRec
     size_t gram;            // 2 x block_gram_entries double-float Gram entries
@@ -85,10 +100,10 @@ __host__ __device__ inline PipePlan make_pipe_plan(int slice_max, int slot_bytes
     PipePlan p;
     const size_t R = 4 * (size_t)B;
     size_t o = 0;
-    p.eps_hi = o;
-    o += al16((size_t)slice_max * 4);
-    p.eps_lo = o;
-    o += al16((size_t)slice_max * 4);
+    p.planes = o;
+    o += al16((size_t)slice_max / 4 * 32);
+    p.fix = o;
+    o += al16((size_t)slice_max * 8);
     p.codes = o;
     o += al16(R * slot_bytes);
     p.recs = o;
@@ -141,6 +156,9 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
                  : "memory");
 }
 
+// Orders this thread's generic-proxy view of memory (global writes of other
+// CTAs it has acquired, shared-memory reads of the slot being refilled) before
+// its later async-proxy (bulk copy) accesses.
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async;" ::: "memory"); }
 
 // SM clock read ordered with the surrounding memory operations and barriers.
@@ -152,6 +170,62 @@ __device__ __forceinline__ long long clk()
 }
 
 __device__ __forceinline__ void dot_warps_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// ---- fixed-point residual: E = eps * 2^kFrac, |E| < 2^62, as four balanced
+// 16-bit limbs E = l0 + l1 2^16 + l2 2^32 + l3 2^48 (l_k in [-2^15, 2^15)).
+// The limb planes of 4 individuals i0..i3 (byte position b of the codes) are 8
+// words: limb k's pair (i0, i1) at word 2(k ^ (b & 3)) and (i2, i3) at the next
+// word, each pair as two int16 (low half first).  The XOR with b & 3 makes the
+// lane that reads position b see the limbs in the order its reduction wants.
+constexpr int kFrac = 50;
+constexpr long long kFixMax = 1ll << 62;
+
+__device__ __forceinline__ int sext16(unsigned w) { return (int)(w << 16) >> 16; }
+
+__device__ __forceinline__ void split_limbs(long long E, int (&l)[4])
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        l[k] = (int)((E << 48) >> 48);
+        E = (E - l[k]) >> 16;
+    }
+    l[3] = (int)E;
+}
+
+__device__ __forceinline__ void store_fix4(uint32_t *planes, int b, const long long (&E)[4])
+{
+    uint2 *w = reinterpret_cast<uint2 *>(planes + 8 * b);
+    const int p = b & 3;
+    int l0[4], l1[4], l2[4], l3[4];
+    split_limbs(E[0], l0);
+    split_limbs(E[1], l1);
+    split_limbs(E[2], l2);
+    split_limbs(E[3], l3);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        w[k ^ p] = make_uint2(__byte_perm((unsigned)l0[k], (unsigned)l1[k], 0x5410),
+                              __byte_perm((unsigned)l2[k], (unsigned)l3[k], 0x5410));
+}
+
+// Double-float value to the fixed-point grid (truncation below 2^-60, then
+// rounding to the nearest multiple of 2^-kFrac); false when out of range.
+__device__ __forceinline__ bool df_to_fix(float h, float l, long long &E)
+{
+    __int128 x1, x2;
+    if (!fx_from_float(h, x1) || !fx_from_float(l, x2))
+        return false;
+    const __int128 x = (x1 + x2 + ((__int128)1 << (59 - kFrac))) >> (60 - kFrac);   // nearest
+    if (x >= (__int128)kFixMax || x <= -(__int128)kFixMax)
+        return false;
+    E = (long long)x;
+    return true;
+}
+
+__device__ __forceinline__ void fix_to_df(long long E, float &h, float &l)
+{
+    const Fx f = fx_split((__int128)E << (60 - kFrac));
+    fx_to_df(f.hi, f.lo, h, l);
+}
 
 // Waits for phase `parity` of m, at most timeout_ns; false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t *m, unsigned parity, uint64_t timeout_ns)
@@ -447,17 +521,30 @@ __device__ __forceinline__ void write_block_outputs(const SweepArgs &a, const Bl
     }
 }
 
+// One CTA of 9 warps per SM.  The register file is split between the SM's four
+// sub-partitions (16K registers each) and warps are placed round-robin, so the
+// sub-partition holding warps 0, 4 and 8 bounds every thread to 168 registers.
 template <int KM, bool MISS>
 __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_upd[kMaxSpec];
-    __shared__ float2 s_dB[kMaxSpec];
-    __shared__ float s_dfl[kMaxSpec][8];
+    // per block parity: residual-changing markers of the block (positions,
+    // dBeta, standardised code values), and the block's prepared inputs
+    __shared__ int s_upd[2][kMaxSpec];
+    __shared__ float2 s_dB[2][kMaxSpec];
+    __shared__ float4 s_x[2][kMaxSpec][2];
+    __shared__ int s_nupd[2];
+    __shared__ float2 s_inum[2][kMaxSpec];   // num from the block's dot products (double-float)
+    __shared__ float s_iuf[2][kMaxSpec];
+    __shared__ unsigned s_imeta[2][kMaxSpec]; // group | K << 8 | (beta_old != 0) << 16
     __shared__ float s_H[kMaxGroups];
     __shared__ int32_t s_gk[kMaxGroups];
     __shared__ BlockOut s_out[2];
-    __shared__ int s_abort, s_nupd;
+    __shared__ uint32_t s_glut[256];         // code byte -> 4 genotype bytes (code 0: 2, 2: 1, 1 and 3: 0)
+    __shared__ uint32_t s_mlut[256];         // code byte -> 4 missing-indicator bytes (code 1)
+    __shared__ long long s_D[kMaxSpec][4];   // residual change per update and code, fixed point
+    __shared__ int s_abort;
+    __shared__ int s_cp_issued;
 
     const int B = a.B;
     const unsigned Bu = (unsigned)B;
@@ -477,8 +564,8 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
     const int nblk = (int)((M32 + Bu - 1) / Bu);
     auto nb_of = [&](int q) { return (int)min(Bu, M32 - (unsigned)q * Bu); };
 
-    float *eh = reinterpret_cast<float *>(smem + plan.eps_hi);
-    float *el = reinterpret_cast<float *>(smem + plan.eps_lo);
+    uint32_t *planes = reinterpret_cast<uint32_t *>(smem + plan.planes);
+    long long *fix = reinterpret_cast<long long *>(smem + plan.fix);
     uint8_t *ring_codes = smem + plan.codes;
     BlockRec *ring_rec = reinterpret_cast<BlockRec *>(smem + plan.recs);
     float2 *gbuf = reinterpret_cast<float2 *>(smem + plan.gram);
@@ -488,20 +575,40 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
     uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + plan.mbar);
     float2 *gstage = reinterpret_cast<float2 *>(a.gstage);
 
-    // ---- prologue: residual slice (with eps -= mu_new), group constants
+    // ---- prologue: residual slice (with eps -= mu_new) to fixed point, tables
     {
         float muh, mul;
         df_from_double(-a.mu_new, muh, mul);
-        for (int i = tid; i < a.slice_max; i += kBlockThreads) {
-            float h = 0.f, l = 0.f;
-            if (i < ns) {
-                h = a.eps_hi[lo + i];
-                l = a.eps_lo[lo + i];
-                df_add(h, l, muh, mul);
+        for (int b = tid; b < a.slice_max / 4; b += kBlockThreads) {
+            long long E[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                E[i] = 0;
+                const int ii = 4 * b + i;
+                if (ii < ns) {
+                    float h = a.eps_hi[lo + ii], l = a.eps_lo[lo + ii];
+                    df_add(h, l, muh, mul);
+                    if (!df_to_fix(h, l, E[i])) {
+                        atomicCAS(a.err, kDevOk, kDevRange);
+                        E[i] = 0;
+                    }
+                }
             }
-            eh[i] = h;
-            el[i] = l;
+            store_fix4(planes, b, E);
+            reinterpret_cast<longlong2 *>(fix)[2 * b] = make_longlong2(E[0], E[1]);
+            reinterpret_cast<longlong2 *>(fix)[2 * b + 1] = make_longlong2(E[2], E[3]);
         }
+    }
+    for (int v = tid; v < 256; v += kBlockThreads) {
+        uint32_t g = 0, m = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned c = (v >> (2 * k)) & 3u;
+            g |= (c == 0u ? 2u : (c == 2u ? 1u : 0u)) << (8 * k);
+            m |= (c == 1u ? 1u : 0u) << (8 * k);
+        }
+        s_glut[v] = g;
+        s_mlut[v] = m;
     }
     for (int i = tid; i < a.n_groups; i += kBlockThreads) {
         s_gk[i] = a.gK[i];
@@ -529,7 +636,8 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         }
     if (tid == 0) {
         s_abort = 0;
-        s_nupd = 0;
+        s_nupd[0] = 0;
+        s_nupd[1] = 0;
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -572,7 +680,9 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
     };
 
     // ---- Gram entries of block q (dot warps): CTA s gathers entries
-    // e = s + G*(t + 256*i) from the packed Gram into staging slot q % 8.
+    // e = s + G*(t + 256*i) from the packed Gram into staging slot q % 8.  The
+    // first entry of each thread is loaded one iteration before it is stored,
+    // so that the random reads of the Gram never delay the barrier arrival.
     double gval = 0.0;
     int gent_mine = -1;
     auto gram_entry = [&](int q, unsigned e, double *out) -> bool {
@@ -595,7 +705,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
                 return false;
             qa = q0 - Bu + pa;
         }
-        const int64_t ja = ring_rec[qa & Rm].j, jb = ring_rec[(q0 + pb) & Rm].j;
+        const int64_t ja = __ldg(&a.brec[qa].j), jb = __ldg(&a.brec[q0 + pb].j);
         const int64_t hi = ja > jb ? ja : jb, lw = ja > jb ? jb : ja;
         *out = __ldg(&a.gram[hi * (hi - 1) / 2 + lw]);
         return true;
@@ -630,88 +740,96 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
     };
 
     // ---- partial dot products of block q against the current residual (dot
-    // warps).  Warp w owns markers w, w+8, ... of the block; its lanes stride
-    // over the slice's code bytes.  Per byte the four products g*hi (exact)
-    // are combined by error-free TwoSums; rounding errors and g*lo go to the
-    // low word.  Missing genotypes are summed apart.  The warp's 8 sums are
-    // reduce-scattered so that 8 lanes convert and publish in parallel.
+    // warps), exact in integers.  Warp w owns markers w, w+8, ..., w+56 of the
+    // block; its lanes stride over the slice's code bytes (lane l reads byte
+    // positions b = l mod 32).  Accumulator slot s = 4 m' + k' of lane l holds
+    // marker w + 8 (m' ^ (l >> 2)) and limb k' ^ (l & 3) (the plane order of its
+    // byte positions), so value s of lane l is value s ^ l of the warp and the
+    // reduction is a butterfly without selects: after it lane l holds limb
+    // l & 3 of marker w + 8 (l >> 2), and four lanes combine a marker's limbs.
     auto dot_block = [&](int q) {
         const unsigned q0 = (unsigned)q * Bu;
         const int nbq = nb_of(q);
         constexpr int MPW = kMaxSpec / 8;
-        float Ah[MPW], Al[MPW], Mh[MPW], Ml[MPW];
+        int A[MPW * 4], Mx[MPW * 4];
         unsigned cofs[MPW];
 #pragma unroll
         for (int k = 0; k < MPW; ++k) {
-            Ah[k] = Al[k] = Mh[k] = Ml[k] = 0.f;
             // markers past the end of a short block read a stale slot; their
             // sums are never published
-            cofs[k] = ((q0 + (unsigned)(warp + 8 * k)) & Rm) * (unsigned)a.slot_bytes;
+            const unsigned m = (unsigned)warp + 8u * ((unsigned)k ^ (unsigned)(lane >> 2));
+            cofs[k] = ((q0 + m) & Rm) * (unsigned)a.slot_bytes;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                A[4 * k + t] = 0;
+                Mx[4 * k + t] = 0;
+            }
         }
-        const int mpw = (B + 7) / 8;
+        // all 8 slots are summed; with B < 64 the slots past the block read ring
+        // slots of other blocks and are never published
         for (int b = lane; b < nbytes; b += 32) {
-            const float4 h = reinterpret_cast<const float4 *>(eh)[b];
-            const float4 l = reinterpret_cast<const float4 *>(el)[b];
+            const uint4 w0 = reinterpret_cast<const uint4 *>(planes)[2 * b];
+            const uint4 w1 = reinterpret_cast<const uint4 *>(planes)[2 * b + 1];
+            const int wv[8] = {(int)w0.x, (int)w0.y, (int)w0.z, (int)w0.w,
+                               (int)w1.x, (int)w1.y, (int)w1.z, (int)w1.w};
 #pragma unroll
             for (int k = 0; k < MPW; ++k) {
-                if (k < mpw) {
-                    const unsigned v = ring_codes[cofs[k] + b];
-                    const unsigned x = ~v, lo1 = x & 0x55u, hi1 = (x >> 1) & 0x55u;
-                    const unsigned two = lo1 & hi1, one = lo1 & ~hi1;
-                    const float g0 = (two & 1u) ? 2.f : ((one & 1u) ? 1.f : 0.f);
-                    const float g1 = (two & 4u) ? 2.f : ((one & 4u) ? 1.f : 0.f);
-                    const float g2 = (two & 16u) ? 2.f : ((one & 16u) ? 1.f : 0.f);
-                    const float g3 = (two & 64u) ? 2.f : ((one & 64u) ? 1.f : 0.f);
-                    float s01, e01, s23, e23, s4, e4, sa, ea;
-                    two_sum(__fmul_rn(g0, h.x), __fmul_rn(g1, h.y), s01, e01);
-                    two_sum(__fmul_rn(g2, h.z), __fmul_rn(g3, h.w), s23, e23);
-                    two_sum(s01, s23, s4, e4);
-                    two_sum(Ah[k], s4, sa, ea);
-                    Ah[k] = sa;
-                    const float lo4 =
-                        __fmaf_rn(g0, l.x, __fmaf_rn(g1, l.y, __fmaf_rn(g2, l.z, __fmul_rn(g3, l.w))));
-                    Al[k] = __fadd_rn(Al[k], __fadd_rn(__fadd_rn(__fadd_rn(e01, e23), e4), __fadd_rn(ea, lo4)));
-                    if (MISS) {
-                        const unsigned mm = v & ~(v >> 1) & 0x55u;   // code 01: missing
-                        if (mm) {
-                            if (mm & 1u) df_add(Mh[k], Ml[k], h.x, l.x);
-                            if (mm & 4u) df_add(Mh[k], Ml[k], h.y, l.y);
-                            if (mm & 16u) df_add(Mh[k], Ml[k], h.z, l.z);
-                            if (mm & 64u) df_add(Mh[k], Ml[k], h.w, l.w);
-                        }
+                const unsigned v = ring_codes[cofs[k] + b];
+                const int g = (int)s_glut[v];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    A[4 * k + t] = __dp2a_lo(wv[2 * t], g, A[4 * k + t]);
+                    A[4 * k + t] = __dp2a_hi(wv[2 * t + 1], g, A[4 * k + t]);
+                }
+                if (MISS) {
+                    const int mm = (int)s_mlut[v];
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        Mx[4 * k + t] = __dp2a_lo(wv[2 * t], mm, Mx[4 * k + t]);
+                        Mx[4 * k + t] = __dp2a_hi(wv[2 * t + 1], mm, Mx[4 * k + t]);
                     }
                 }
             }
         }
-        df_rs_step<4>(Ah, Al, lane & 16, 16);
-        df_rs_step<2>(Ah, Al, lane & 8, 8);
-        df_rs_step<1>(Ah, Al, lane & 4, 4);
-        df_xor_add(Ah[0], Al[0], 2);
-        df_xor_add(Ah[0], Al[0], 1);
-        if (MISS) {
-            df_rs_step<4>(Mh, Ml, lane & 16, 16);
-            df_rs_step<2>(Mh, Ml, lane & 8, 8);
-            df_rs_step<1>(Mh, Ml, lane & 4, 4);
-            df_xor_add(Mh[0], Ml[0], 2);
-            df_xor_add(Mh[0], Ml[0], 1);
-        }
-        const int kk = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
-        const int m = warp + 8 * kk;
-        if ((lane & 3) == 0 && m < nbq) {
-            unsigned long long *acc = a.acc + ((size_t)(q % kAccBufs) * kMaxSpec + m) * 4;
-            __int128 x1, x2, m1 = 0, m2 = 0;
-            const bool ok = fx_from_float(Ah[0], x1) && fx_from_float(Al[0], x2) &&
-                            (!MISS || (fx_from_float(Mh[0], m1) && fx_from_float(Ml[0], m2)));
-            if (ok) {
-                publish(acc, x1 + x2);
-                if (MISS && (Mh[0] != 0.f || Ml[0] != 0.f))
-                    publish(acc + 2, m1 + m2);
-            } else {
-                atomicCAS(a.err, kDevOk, kDevRange);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int i = 0; i < o; ++i) {
+                A[i] += __shfl_xor_sync(0xffffffffu, A[i + o], o);
+                if (MISS)
+                    Mx[i] += __shfl_xor_sync(0xffffffffu, Mx[i + o], o);
             }
         }
+        // limb l & 3 of marker w + 8 (l >> 2): combine the four limbs (int128)
+        const int limb = lane & 3;
+        auto combine = [&](int v) {
+            __int128 x = (__int128)(long long)v << (16 * limb);
+            unsigned long long xl = (unsigned long long)x, xh = (unsigned long long)(x >> 64);
+#pragma unroll
+            for (int o = 1; o <= 2; o <<= 1) {
+                const unsigned long long yl = __shfl_xor_sync(0xffffffffu, xl, o);
+                const unsigned long long yh = __shfl_xor_sync(0xffffffffu, xh, o);
+                const unsigned long long sl = xl + yl;
+                xh = xh + yh + (sl < xl ? 1ull : 0ull);
+                xl = sl;
+            }
+            return (__int128)(((unsigned __int128)xh << 64) | xl);
+        };
+        const __int128 T = combine(A[0]);
+        const __int128 Tm = MISS ? combine(Mx[0]) : (__int128)0;
+        const int m = warp + 8 * (lane >> 2);
+        if (limb == 0 && m < nbq) {
+            unsigned long long *acc =
+                a.acc + (size_t)(q % kAccBufs) * kAccBufWords + ((size_t)(sidx % kAccCopies) * kMaxSpec + m) * 4;
+            publish(acc, T << (60 - kFrac));
+            if (MISS && Tm != 0)
+                publish(acc + 2, Tm << (60 - kFrac));
+        }
     };
-    auto arrive = [&](int q) { red_release_add_u64(a.counter + (q & 1), 1ull); };
+    auto arrive = [&](int q) {
+        red_release_add_u64(a.counter + ((size_t)(q & 1) * kCounters + (size_t)(sidx % kCounters)) * kCounterStride,
+                            1ull);
+    };
 
     // profiling (first CTA): dot side on thread 0, resolve side on warp 8 lane 0
     const bool prof_d = a.prof != nullptr && sidx == 0 && tid == 0;
@@ -727,7 +845,148 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
     };
     unsigned long long *fb_counter = a.prof ? reinterpret_cast<unsigned long long *>(a.prof + 8) : nullptr;
     long long steps = 0;
+    long long tdl = 0;   // profiling: dot products of the second warp
+    const bool prof_w1 = a.prof != nullptr && sidx == 0 && tid == 32;
+    const bool prof_h = a.prof != nullptr && sidx == 0 && tid == (kDotWarps - 1) * 32;
     int cp_issued = -1, cp_waited = -1;   // resolve warp: Gram copies issued / waited for
+
+    // ---- rank-U residual update of block q (dot warps, run at the start of the
+    // next iteration while the resolve warp works on block q+1):
+    // E += round(dBeta_u * x_u(code) * 2^kFrac)
+    auto apply_update = [&](int q) {
+        const int par = q & 1;
+        const int U = s_nupd[par];
+        if (U == 0)
+            return;
+        const unsigned qb = (unsigned)q * Bu;
+        if (tid < 4 * U) {
+            const int u = tid >> 2, code = tid & 3;
+            const float2 dB = s_dB[par][u];
+            const float4 xv = s_x[par][u][code >> 1];
+            const float xh = (code & 1) ? xv.z : xv.x, xl = (code & 1) ? xv.w : xv.y;
+            float dh, dl;
+            df_mul(dB.x, dB.y, xh, xl, dh, dl);
+            long long D = 0;
+            if (!df_to_fix(dh, dl, D))
+                atomicCAS(a.err, kDevOk, kDevRange);
+            s_D[u][code] = D;
+        }
+        dot_warps_sync();
+        // The sum of the residual is left as it was at the sweep start: the
+        // standardised columns sum to zero, so a dense update moves it only
+        // by rounding (dBeta times a column sum of order 1e-11).
+        for (int b = tid; b < nbytes; b += kDotWarps * 32) {
+            const longlong2 e01 = reinterpret_cast<const longlong2 *>(fix)[2 * b];
+            const longlong2 e23 = reinterpret_cast<const longlong2 *>(fix)[2 * b + 1];
+            long long E[4] = {e01.x, e01.y, e23.x, e23.y};
+            for (int u = 0; u < U; ++u) {
+                const unsigned v = ring_codes[((qb + s_upd[par][u]) & Rm) * a.slot_bytes + b];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    E[i] += s_D[u][(v >> (2 * i)) & 3u];
+            }
+            // padding individuals past the slice end keep a zero residual
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (4 * b + i >= ns)
+                    E[i] = 0;
+                if (E[i] >= kFixMax || E[i] <= -kFixMax) {
+                    atomicCAS(a.err, kDevOk, kDevRange);
+                    E[i] = 0;
+                }
+            }
+            reinterpret_cast<longlong2 *>(fix)[2 * b] = make_longlong2(E[0], E[1]);
+            reinterpret_cast<longlong2 *>(fix)[2 * b + 1] = make_longlong2(E[2], E[3]);
+            store_fix4(planes, b, E);
+        }
+        dot_warps_sync();
+    };
+
+    constexpr int kHelperWarp = kDotWarps - 1;   // polls the grid barrier
+    constexpr int kCopyThread = 5 * 32;   // issues the Gram bulk copies (a dot warp off the resolve warp's sub-partition)
+    constexpr int kWriterWarp = 6;        // writes a resolved block's outputs
+
+    // ---- inputs of block q (the helper warp, after its dot products): wait
+    // for barrier q (lane c < 8 polls counter c), then per marker
+    // num = sigma * sum(g*eps) + cst + dm * sum_missing(eps) as double-float,
+    // with the FP32 sampler's per-marker values.
+    long long th_poll = 0, th_in = 0;
+    auto prepare_inputs = [&](int q, bool prof) {
+        const long long t0 = prof ? clk() : 0;
+        bool ok = true;
+        if (lane < kCounters) {
+            // lane c waits for the CTAs s = c (mod 8), and the phantom arrivals on counter 0
+            const unsigned long long per = (unsigned long long)((q >> 1) + 1);
+            const int nc = lane < a.G ? (a.G - lane + kCounters - 1) / kCounters : 0;
+            const unsigned long long target = (unsigned long long)(nc + (lane == 0 ? a.phantom : 0)) * per;
+            const unsigned long long *ctr =
+                a.counter + ((size_t)(q & 1) * kCounters + (size_t)lane) * kCounterStride;
+            if (ld_acquire_u64(ctr) < target) {
+                const uint64_t tw = global_timer_ns();
+                unsigned spins = 0;
+                while (ld_acquire_u64(ctr) < target) {
+                    if ((++spins & 255u) == 0 &&
+                        (*(volatile int *)a.err != kDevOk || global_timer_ns() - tw > a.timeout_ns)) {
+                        atomicCAS(a.err, kDevOk, kDevTimeout);
+                        ok = false;
+                        break;
+                    }
+                }
+            }
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok && lane == 0)
+            s_abort = 1;
+        __syncwarp();
+        const long long t1 = prof ? clk() : 0;
+        if (!ok)
+            return;
+        const int par = q & 1, nbq = nb_of(q);
+        const unsigned qb = (unsigned)q * Bu;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int m = lane + 32 * h;
+            float nh = 0.f, nl = 0.f, uf = 2.f;
+            unsigned meta = 2u << 8;
+            if (m < nbq) {
+                const BlockRec &rc = ring_rec[(qb + m) & Rm];
+                const unsigned long long *acc = a.acc + (size_t)(q % kAccBufs) * kAccBufWords + (size_t)m * 4;
+                // the copies' 56-bit low words sum to less than 2^64 (152 parts at most)
+                long long th64 = 0, sh64 = 0;
+                unsigned long long tl64 = 0, sl64 = 0;
+#pragma unroll
+                for (int c = 0; c < kAccCopies; ++c) {
+                    const unsigned long long *ac = acc + (size_t)c * kMaxSpec * 4;
+                    th64 += (long long)ld_relaxed_u64(ac);
+                    tl64 += ld_relaxed_u64(ac + 1);
+                    if (MISS) {
+                        sh64 += (long long)ld_relaxed_u64(ac + 2);
+                        sl64 += ld_relaxed_u64(ac + 3);
+                    }
+                }
+                float th, tl;
+                fx_to_df(th64, tl64, th, tl);
+                df_mul(rc.sig[0], rc.sig[1], th, tl, nh, nl);
+                df_add(nh, nl, rc.cst[0], rc.cst[1]);
+                if (MISS) {
+                    float sh, sl, qh, ql;
+                    fx_to_df(sh64, sl64, sh, sl);
+                    df_mul(rc.dm[0], rc.dm[1], sh, sl, qh, ql);
+                    df_add(nh, nl, qh, ql);
+                }
+                uf = rc.uf;
+                meta = (unsigned)rc.group | ((unsigned)s_gk[rc.group] << 8) | (rc.bnz ? 1u << 16 : 0u);
+            }
+            s_inum[par][m] = make_float2(nh, nl);
+            s_iuf[par][m] = uf;
+            s_imeta[par][m] = meta;
+        }
+        if (prof) {
+            const long long t2 = clk();
+            th_poll += t1 - t0;
+            th_in += t2 - t1;
+        }
+    };
 
     // ---- first blocks: records 0..2 and codes 0..1 resident, block 0's dot
     // products and the Gram entries of blocks 0 and 1 staged, barrier 0
@@ -747,12 +1006,18 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
             gather_load(1);
             gather_store(1);
         }
+        if (nblk > 2)
+            gather_load(2);
         dot_warps_sync();
         if (tid == 0)
             arrive(0);
+        if (warp == kHelperWarp)
+            prepare_inputs(0, false);
     }
 
     int r = 0;
+    if (prof_d || prof_r)
+        tp = clk();
     for (; r < nblk; ++r) {
         cp_async_wait_all();
         __syncthreads();
@@ -766,65 +1031,60 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         const int nb = nb_of(r);
 
         if (warp < kDotWarps) {
-            // ---- dot side
-            if (r >= 1 && sidx == (r - 1) % a.G && warp == kDotWarps - 1)
-                write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
-            if (r + 2 < nblk)
-                gather_load(r + 2);
-            if (r + 1 < nblk)
-                dot_block(r + 1);
+            // ---- dot side: update of block r-1, dots of block r+1 and their
+            // publication, then (after the arrival) the Gram copy of block r+1, the
+            // outputs of block r-1 and the inputs of block r+1
+            if (tid == kCopyThread && r == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
+                bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
+                cp_issued = 0;
+            }
+            // staged Gram entries of block r+2 (loaded in the previous iteration) and
+            // the zeroed accumulators of block r+3 are written first, so that the
+            // release at the arrival does not wait for them
             if (r + 2 < nblk)
                 gather_store(r + 2);
-            if (sidx == 0 && r + 3 < nblk && tid < 4 * kMaxSpec)
-                a.acc[(size_t)((r + 3) % kAccBufs) * kMaxSpec * 4 + tid] = 0ull;
+            if (sidx == 0 && r + 3 < nblk)
+                for (int i = tid; i < kAccBufWords; i += kDotWarps * 32)
+                    a.acc[(size_t)((r + 3) % kAccBufs) * kAccBufWords + i] = 0ull;
+            if (r >= 1) {
+                apply_update(r - 1);
+                mark(prof_d, 4);
+            }
+            const long long td0 = prof_w1 ? clk() : 0;
+            if (r + 1 < nblk)
+                dot_block(r + 1);
+            const long long td1 = prof_w1 ? clk() : 0;
             dot_warps_sync();
+            if (prof_w1)
+                tdl += td1 - td0;
             if (tid == 0 && r + 1 < nblk)
                 arrive(r + 1);
             mark(prof_d, 1);
-        } else {
-            // ---- resolve side: barrier r
-            mark(prof_r, 8);
-            bool ok = true;
-            if (lane == 0) {
-                const unsigned long long target =
-                    (unsigned long long)(a.G + a.phantom) * (unsigned long long)((r >> 1) + 1);
-                const unsigned long long *ctr = a.counter + (r & 1);
-                if (ld_acquire_u64(ctr) < target) {
-                    const uint64_t t0 = global_timer_ns();
-                    unsigned spins = 0;
-                    while (ld_acquire_u64(ctr) < target) {
-                        if ((++spins & 255u) == 0 &&
-                            (*(volatile int *)a.err != kDevOk || global_timer_ns() - t0 > a.timeout_ns)) {
-                            atomicCAS(a.err, kDevOk, kDevTimeout);
-                            ok = false;
-                            break;
-                        }
-                    }
-                }
-                if (ok) {
-                    // the staged entries were written by generic stores of other
-                    // CTAs; the bulk copies read them through the async proxy
-                    fence_proxy_async();
-                    if (r == 0) {
-                        mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
-                        bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
-                        cp_issued = 0;
-                    }
-                    if (r + 1 < nblk) {
-                        const int q = r + 1;
-                        mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
-                        bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gent,
-                                      (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
-                        cp_issued = q;
-                    }
-                } else {
-                    s_abort = 1;
-                }
+            // inputs of block r+1, once barrier r+1 has passed
+            if (warp == kHelperWarp && r + 1 < nblk)
+                prepare_inputs(r + 1, prof_h);
+            // then, off the critical path: Gram loads of block r+3 (stored in the
+            // next iteration), the Gram copy of block r+1 (its staging was
+            // published by barrier r), the outputs of block r-1
+            if (r + 3 < nblk)
+                gather_load(r + 3);
+            if (tid == kCopyThread && r + 1 < nblk) {
+                const int q = r + 1;
+                fence_proxy_async();
+                mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
+                bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gent,
+                              (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
+                cp_issued = q;
             }
-            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-            mark(prof_r, 2);
-            if (ok) {
-                // ---- block inputs: num = sigma * sum(g*eps) + cst + dm * sum_missing(eps)
+            if (r >= 1 && sidx == (r - 1) % a.G && warp == kWriterWarp)
+                write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
+        } else {
+            // ---- resolve side
+            mark(prof_r, 8);
+            {
+                const int par = r & 1;
                 float nh[2], nl[2], ufr[2];
                 int grp[2], kk[2];
                 bool own[2], bnz[2];
@@ -832,29 +1092,14 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
                 for (int h = 0; h < 2; ++h) {
                     const int m = lane + 32 * h;
                     own[h] = m < nb;
-                    nh[h] = nl[h] = 0.f;
-                    ufr[h] = 2.f;
-                    grp[h] = 0;
-                    kk[h] = 2;
-                    bnz[h] = false;
-                    if (own[h]) {
-                        const BlockRec &rc = ring_rec[(q0 + m) & Rm];
-                        const unsigned long long *acc = a.acc + ((size_t)(r % kAccBufs) * kMaxSpec + m) * 4;
-                        float th, tl;
-                        fx_to_df((long long)ld_relaxed_u64(acc), ld_relaxed_u64(acc + 1), th, tl);
-                        df_mul(rc.sig[0], rc.sig[1], th, tl, nh[h], nl[h]);
-                        df_add(nh[h], nl[h], rc.cst[0], rc.cst[1]);
-                        if (MISS) {
-                            float sh, sl, qh, ql;
-                            fx_to_df((long long)ld_relaxed_u64(acc + 2), ld_relaxed_u64(acc + 3), sh, sl);
-                            df_mul(rc.dm[0], rc.dm[1], sh, sl, qh, ql);
-                            df_add(nh[h], nl[h], qh, ql);
-                        }
-                        ufr[h] = rc.uf;
-                        grp[h] = rc.group;
-                        kk[h] = s_gk[rc.group];
-                        bnz[h] = rc.bnz != 0u;
-                    }
+                    const float2 n = s_inum[par][m];
+                    nh[h] = n.x;
+                    nl[h] = n.y;
+                    ufr[h] = s_iuf[par][m];
+                    const unsigned meta = s_imeta[par][m];
+                    grp[h] = (int)(meta & 0xFFu);
+                    kk[h] = (int)((meta >> 8) & 0xFFu);
+                    bnz[h] = (meta >> 16) != 0u;
                 }
                 // Gram entries of block r (copied one iteration ahead)
                 bool gok = mbar_wait(&mbar[r & 1], (unsigned)((r >> 1) & 1), a.timeout_ns);
@@ -870,10 +1115,11 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
                     const float2 *gtri = gbuf + (size_t)(r & 1) * gent;
                     const float2 *gcross = gtri + npairs;
                     // updates of block r-1, not yet in the residual the dot products saw
-                    const int Up = s_nupd;
+                    const int pp = (r - 1) & 1;
+                    const int Up = r > 0 ? s_nupd[pp] : 0;
                     for (int u = 0; u < Up; ++u) {
-                        const int p = s_upd[u];
-                        const float2 dB = s_dB[u];
+                        const int p = s_upd[pp][u];
+                        const float2 dB = s_dB[pp][u];
 #pragma unroll
                         for (int h = 0; h < 2; ++h) {
                             if (!own[h])
@@ -886,6 +1132,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
                     }
                     __syncwarp();
                     mark(prof_r, 7);
+
 
                     // ---- resolve block r: lane l owns markers l and l+32; a
                     // decision is kept while its certified margin covers the move of
@@ -1011,8 +1258,13 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
                             }
                         }
                         if (lane == 0) {
-                            s_upd[nupd] = p;
-                            s_dB[nupd] = make_float2(dh, dl);
+                            s_upd[par][nupd] = p;
+                            s_dB[par][nupd] = make_float2(dh, dl);
+                        }
+                        if (lane == owner) {
+                            const float4 *xs = reinterpret_cast<const float4 *>(ring_rec[(q0 + p) & Rm].x);
+                            s_x[par][nupd][0] = xs[0];
+                            s_x[par][nupd][1] = xs[1];
                         }
                         ++nupd;
                         next = p + 1;
@@ -1020,7 +1272,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
                             ph[10] += clk() - tl1;
                     }
                     if (lane == 0)
-                        s_nupd = nupd;
+                        s_nupd[par] = nupd;
                     // the block's decisions for the CTA that writes them out
                     if (sidx == r % a.G) {
                         BlockOut &o = s_out[r & 1];
@@ -1050,79 +1302,64 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         mark(prof_d, 11);
         if (s_abort)
             break;
-
-        // ---- rank-U residual update of block r: eps += dBeta_u * x_u
-        const int U = s_nupd;
-        if (U > 0) {
-            if (tid < 4 * U) {
-                const int u = tid >> 2, code = tid & 3;
-                const BlockRec &rc = ring_rec[(q0 + s_upd[u]) & Rm];
-                const float2 dB = s_dB[u];
-                df_mul(dB.x, dB.y, rc.x[2 * code], rc.x[2 * code + 1], s_dfl[u][2 * code], s_dfl[u][2 * code + 1]);
-            }
-            __syncthreads();
-            // The sum of the residual is left as it was at the sweep start: the
-            // standardised columns sum to zero, so a dense update moves it only
-            // by rounding (dBeta times a column sum of order 1e-11).
-            for (int b = tid; b < nbytes; b += kBlockThreads) {
-                float4 h = reinterpret_cast<float4 *>(eh)[b];
-                float4 l = reinterpret_cast<float4 *>(el)[b];
-                for (int u = 0; u < U; ++u) {
-                    const unsigned v = ring_codes[((q0 + s_upd[u]) & Rm) * a.slot_bytes + b];
-                    const float *d = s_dfl[u];
-                    df_add(h.x, l.x, d[2 * (v & 3u)], d[2 * (v & 3u) + 1]);
-                    df_add(h.y, l.y, d[2 * ((v >> 2) & 3u)], d[2 * ((v >> 2) & 3u) + 1]);
-                    df_add(h.z, l.z, d[2 * ((v >> 4) & 3u)], d[2 * ((v >> 4) & 3u) + 1]);
-                    df_add(h.w, l.w, d[2 * (v >> 6)], d[2 * (v >> 6) + 1]);
-                }
-                // padding individuals past the slice end keep a zero residual
-                const int i0 = 4 * b;
-                if (i0 + 3 >= ns) {
-                    if (i0 + 0 >= ns) { h.x = 0.f; l.x = 0.f; }
-                    if (i0 + 1 >= ns) { h.y = 0.f; l.y = 0.f; }
-                    if (i0 + 2 >= ns) { h.z = 0.f; l.z = 0.f; }
-                    if (i0 + 3 >= ns) { h.w = 0.f; l.w = 0.f; }
-                }
-                reinterpret_cast<float4 *>(eh)[b] = h;
-                reinterpret_cast<float4 *>(el)[b] = l;
-            }
-        }
-        mark(prof_d, 4);
     }
-    // outputs of the last block
-    if (!s_abort && r == nblk && sidx == (nblk - 1) % a.G && warp == kDotWarps - 1)
-        write_block_outputs<KM>(a, s_out[(nblk - 1) & 1], gcf, s_gk, gbf, lane);
+    // the last block: residual update and outputs
+    if (!s_abort && r == nblk && warp < kDotWarps) {
+        apply_update(nblk - 1);
+        if (sidx == (nblk - 1) % a.G && warp == kDotWarps - 1)
+            write_block_outputs<KM>(a, s_out[(nblk - 1) & 1], gcf, s_gk, gbf, lane);
+    }
     if (prof_d) {
         a.prof[0] = ph[0];
         a.prof[1] = ph[1];
         a.prof[4] = ph[4];
         a.prof[5] = r;
-        a.prof[11] = ph[11];
+
     }
+    if (prof_h) {
+        a.prof[2] = th_poll;
+        a.prof[11] = th_in;
+    }
+    if (prof_w1)
+        a.prof[15] = tdl;
     if (prof_r) {
-        a.prof[2] = ph[2];
         a.prof[3] = ph[3];
         a.prof[6] = steps;
         a.prof[7] = ph[7];
         a.prof[9] = ph[9];
         a.prof[10] = ph[10];
+
     }   // a.prof[8]: FP64 fallbacks of the certified sampler (first CTA)
     cp_async_wait_all();
+
     // bulk copies still in flight after an abort: wait for them (bounded)
+    if (tid == kCopyThread)
+        s_cp_issued = cp_issued;
+    __syncthreads();
     if (tid == kDotWarps * 32) {
-        for (int q = cp_waited + 1; q <= cp_issued; ++q)
+        for (int q = cp_waited + 1; q <= s_cp_issued; ++q)
             mbar_wait(&mbar[q & 1], (unsigned)((q >> 1) & 1), a.timeout_ns);
     }
     __syncthreads();
 
     // ---- epilogue: residual back to HBM, per-slice sums
     double s1 = 0.0, s2 = 0.0;
-    for (int i = tid; i < ns; i += kBlockThreads) {
-        a.eps_hi[lo + i] = eh[i];
-        a.eps_lo[lo + i] = el[i];
-        const double e = (double)eh[i] + (double)el[i];
-        s1 += e;
-        s2 = fma(e, e, s2);
+    for (int b = tid; b < nbytes; b += kBlockThreads) {
+        const longlong2 e01 = reinterpret_cast<const longlong2 *>(fix)[2 * b];
+        const longlong2 e23 = reinterpret_cast<const longlong2 *>(fix)[2 * b + 1];
+        const long long E[4] = {e01.x, e01.y, e23.x, e23.y};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (4 * b + i < ns) {
+                float h, l;
+                fix_to_df(E[i], h, l);
+                a.eps_hi[lo + 4 * b + i] = h;
+                a.eps_lo[lo + 4 * b + i] = l;
+                const double e = (double)h + (double)l;
+                s1 += e;
+                s2 = fma(e, e, s2);
+            }
+        }
     }
     __shared__ double s_red[kBlockThreads / 32][2];
 #pragma unroll
@@ -1198,17 +1435,34 @@ cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st)
     return a.has_missing ? launch_block_km<kMaxK, true>(a, smem, st) : launch_block_km<kMaxK, false>(a, smem, st);
 }
 
-int sweep_block_max_ctas_per_sm(size_t smem)
+int sweep_block_max_ctas_per_sm(size_t smem, std::string *why)
 {
     int n = 1 << 30;
     const void *fs[4] = {(const void *)k_sweep_block<4, false>, (const void *)k_sweep_block<4, true>,
                          (const void *)k_sweep_block<kMaxK, false>, (const void *)k_sweep_block<kMaxK, true>};
     for (const void *f : fs) {
         int m = 0;
-        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, f, kBlockThreads, smem);
+        if (e != cudaSuccess) {
+            if (why) {
+                cudaFuncAttributes fa{};
+                cudaFuncGetAttributes(&fa, f);
+                *why = std::string(cudaGetErrorString(e)) + " (dynamic shared memory " + std::to_string(smem) +
+                       " B, static " + std::to_string(fa.sharedSizeBytes) + " B, " + std::to_string(fa.numRegs) +
+                       " registers)";
+            }
+            cudaGetLastError();
             return 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, f, kBlockThreads, smem) != cudaSuccess)
-            return 0;
+        }
+        if (m < 1 && why) {
+            cudaFuncAttributes fa{};
+            cudaFuncGetAttributes(&fa, f);
+            *why = "0 per SM (dynamic shared memory " + std::to_string(smem) + " B, static " +
+                   std::to_string(fa.sharedSizeBytes) + " B, " + std::to_string(fa.numRegs) + " registers, at most " +
+                   std::to_string(fa.maxThreadsPerBlock) + " threads)";
+        }
         n = m < n ? m : n;
     }
     return n;

@@ -136,7 +136,7 @@ cudaError_t launch_block_finish(int64_t M, const uint8_t *chosen, const float2 *
 cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st);
 size_t sweep_block_stage_bytes(int B);   // global Gram staging of the blocked sweep
 int sweep_block_threads();
-int sweep_block_max_ctas_per_sm(size_t smem);
+int sweep_block_max_ctas_per_sm(size_t smem, std::string *why = nullptr);
 cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work);
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
                const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why);

@@ -296,7 +296,7 @@ class Chain:
         return dict(blocked=bool(b.value), build_ms=ms.value, bytes=n.value)
 
     def phase_cycles(self) -> np.ndarray:
-        out = np.zeros(12, np.int64)
+        out = np.zeros(16, np.int64)
         self._check(self.lib.brr_get_phase_cycles(self.h, _ptr(out, C.c_int64)))
         return out
 

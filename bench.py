@@ -334,8 +334,9 @@ def main():
                      "kernel": "k_sweep (FP32C, dense)", "algorithmic_bytes_per_launch": bytes_per_sweep},
         "phases_clk_per_round": {k: v / max(fp32c["phases"][5], 1) for k, v in
                                  zip(["ring_wait", "dot_side", "barrier_wait", "sample", "update", "block_inputs",
-                                      "of_sample_picks", "of_sample_steps", "dot_side_idle"],
+                                      "of_sample_picks", "of_sample_steps", "next_block_inputs"],
                                      [*fp32c["phases"][:5], fp32c["phases"][7], *fp32c["phases"][9:12]])},
+        "dot_loop_clk_per_round_warp1": fp32c["phases"][15] / max(fp32c["phases"][5], 1),
         "sampling_steps_per_round": fp32c["phases"][6] / max(fp32c["phases"][5], 1),
         "fp64_fallbacks_per_step": fp32c["phases"][8] / args.steps,
         "rounds_per_step": fp32c["rounds"] / args.steps,

@@ -194,16 +194,18 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
 
 /* Per-phase SM cycles of the sweeps of the last brr_iterate / brr_sweep call,
  * measured on the first CTA (the counterpart of the reference's per-column
- * timing log, src/BayesRBase.cpp:381-389), 12 values.  Restart sweep: [0] ring
+ * timing log, src/BayesRBase.cpp:381-389), 16 values.  Restart sweep: [0] ring
  * prefetch and wait, [1] partial dot products, [2] grid barrier, [3]
  * component sampling, [4] outputs and residual update, [5] grid rounds.
- * Gram-blocked sweep: [0] ring wait and prefetch issue, [1] dot side (dot
- * products of the next block, their publication, Gram staging), [2] resolve
- * side waiting for the grid barrier, [3] resolve side sampling, [4] residual
- * update, [5] blocks, [6] sampling steps, [7] block inputs (sums, Gram copy
- * wait, corrections of the previous block), [8] samples the FP32 sampler
- * handed to FP64, [9] cycles of [3] in component picks, [10] cycles of [3]
- * resolving steps, [11] dot side waiting for the resolve side. */
+ * Gram-blocked sweep: [0] ring wait and waiting for the other warps, [1] dot
+ * products of the next block and their publication, [2] waiting for the grid
+ * barrier, [3] sampling, [4] residual update, [5] blocks, [6] sampling steps,
+ * [7] block inputs on the sampling warp (corrections of the previous block,
+ * Gram copy wait), [8] samples the FP32 sampler handed to FP64, [9] cycles of
+ * [3] in component picks, [10] cycles of [3] resolving steps, [11] assembling
+ * the next block's inputs, [15] dot products alone on the second warp.  The
+ * per-thread clock is read around long code regions, so the values are
+ * indicative. */
 int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles);
 
 #ifdef __cplusplus
