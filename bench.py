@@ -35,6 +35,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 N_IND, M_SNP = 100_000, 100_000
+DRAM_BYTES_PER_MARKER_N100K = 224.709725e9 * 1.312960e-3 / 8192
 S_GROUPS = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
 P_LO, P_HI = 0.01, 0.5
 N_CAUSAL, H2 = 1000, 0.4
@@ -309,10 +310,10 @@ def main():
     sweep_s = fp32c["sweep_ms"] / 1e3 / args.steps
     bytes_per_sweep = M_SNP * (N_IND / 4.0)      # 2-bit genotype bytes per marker-update x M
     achieved = bytes_per_sweep / sweep_s / 1e9
-    traffic = None
-    tp = ROOT / "profiles" / "sweep_traffic.json"
-    if tp.exists():
-        traffic = json.loads(tp.read_text()).get("bytes_per_sweep")
+    # DRAM bytes of one blocked-sweep launch, measured by ncu on the N=100,000 x
+    # M=8,192 case (dram__bytes.sum.per_second x gpu__time_duration.sum = 295.0 MB),
+    # scaled by the markers swept (the traffic grows with M at fixed N)
+    traffic = DRAM_BYTES_PER_MARKER_N100K * M_SNP if N_IND == 100_000 else None
     plain_rate = M_SNP * args.steps / (fp64["total_ms"] / 1e3)
     nzb = fp64["beta"] != 0
     line = {
@@ -331,7 +332,8 @@ def main():
                           "nonzero_beta_plain": int(nzb.sum())},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-                     "kernel": "k_sweep (FP32C, dense)", "algorithmic_bytes_per_launch": bytes_per_sweep},
+                     "kernel": "k_sweep_block (FP32C dense, Gram-blocked)",
+                     "algorithmic_bytes_per_launch": bytes_per_sweep},
         "phases_clk_per_round": {k: v / max(fp32c["phases"][5], 1) for k, v in
                                  zip(["ring_wait", "dot_side", "barrier_wait", "sample", "update", "block_inputs",
                                       "of_sample_picks", "of_sample_steps", "next_block_inputs"],
