@@ -1,6 +1,7 @@
 #include "data.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <fstream>
 #include <iostream>
@@ -165,6 +166,178 @@ std::vector<IndexEntry> readIndex(const std::string &indexFile, int64_t M)
     if (in.gcount() != (std::streamsize)(M * sizeof(IndexEntry)))
         throw std::string("Error: preprocessed index is shorter than the number of SNPs");
     return v;
+}
+
+namespace {
+
+void setCode(std::vector<uint8_t> &bed, int64_t cb, int64_t j, int64_t i, unsigned code)
+{
+    uint8_t &b = bed[(size_t)(j * cb + (i >> 2))];
+    const unsigned sh = 2u * (unsigned)(i & 3);
+    b = (uint8_t)((b & ~(3u << sh)) | (code << sh));
+}
+
+std::vector<uint8_t> allHomozygousMajor(int64_t N, int64_t M)
+{
+    const int64_t cb = (N + 3) / 4;
+    std::vector<uint8_t> bed((size_t)(M * cb), 0);
+    for (int64_t j = 0; j < M; ++j)
+        for (int64_t i = 0; i < N; ++i)
+            setCode(bed, cb, j, i, 3u);   // code 11: genotype 0
+    return bed;
+}
+
+std::ifstream openPreprocessed(const std::string &ppFile)
+{
+    std::ifstream in(ppFile, std::ios::binary);
+    if (!in)
+        throw std::string("Error: Failed to open preprocessed bed file [" + ppFile + "]");
+    return in;
+}
+
+void checkUncompressed(const IndexEntry &e, int64_t j)
+{
+    if (e.compressedSize != e.originalSize)
+        throw std::string("Error: marker " + std::to_string(j) +
+                          " of the preprocessed file is compressed; write it without --compress");
+}
+
+// Standardised value per 2-bit code (0: genotype 2, 1: missing, 2: genotype 1,
+// 3: genotype 0) of a dense column with the given class counts: missing values
+// take the mean of the non-missing ones, the column is centred and scaled to
+// a squared norm of N-1 (src/densemarkerbuilder.cpp:44-59).
+bool standardisedValues(int64_t N, const int64_t n[4], double v[4])
+{
+    const int64_t n2 = n[0], nm = n[1], n1 = n[2], n0 = n[3];
+    if (N - nm <= 0 || N < 2)
+        return false;
+    const double S = (double)n1 + 2.0 * (double)n2;
+    const double mean = S / (double)(N - nm);
+    const double colmean = (S + (double)nm * mean) / (double)N;
+    const double d2 = 2.0 - colmean, d1 = 1.0 - colmean, d0 = -colmean, dm = mean - colmean;
+    const double sqn = (double)n2 * d2 * d2 + (double)n1 * d1 * d1 + (double)n0 * d0 * d0 + (double)nm * dm * dm;
+    if (!(sqn > 0.0))
+        return false;
+    const double sigma = 1.0 / std::sqrt(sqn / (double)(N - 1));
+    v[0] = d2 * sigma;
+    v[1] = dm * sigma;
+    v[2] = d1 * sigma;
+    v[3] = d0 * sigma;
+    return true;
+}
+
+}  // namespace
+
+std::vector<uint8_t> readRaggedPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
+                                                 int64_t M)
+{
+    const std::vector<IndexEntry> index = readIndex(indexFile, M);
+    std::ifstream in = openPreprocessed(ppFile);
+    std::vector<uint8_t> bed = allHomozygousMajor(N, M);
+    const int64_t cb = (N + 3) / 4;
+    const unsigned listCode[3] = {2u, 0u, 1u};   // Zones: genotype 1, Ztwos: genotype 2, Zmissing
+    std::vector<int32_t> ids;
+    for (int64_t j = 0; j < M; ++j) {
+        checkUncompressed(index[(size_t)j], j);
+        in.seekg((std::streamoff)index[(size_t)j].pos);
+        double stats[4];
+        in.read(reinterpret_cast<char *>(stats), sizeof stats);
+        uint64_t used = sizeof stats;
+        for (int k = 0; k < 3; ++k) {
+            uint64_t n = 0;
+            in.read(reinterpret_cast<char *>(&n), sizeof n);
+            if (!in || n > (uint64_t)N)
+                throw std::string("Error: malformed ragged record of marker " + std::to_string(j));
+            ids.resize((size_t)n);
+            if (n)
+                in.read(reinterpret_cast<char *>(ids.data()), (std::streamsize)(n * sizeof(int32_t)));
+            if (!in)
+                throw std::string("Error: malformed ragged record of marker " + std::to_string(j));
+            for (int32_t i : ids) {
+                if (i < 0 || i >= N)
+                    throw std::string("Error: individual index out of range in marker " + std::to_string(j));
+                setCode(bed, cb, j, i, listCode[k]);
+            }
+            used += sizeof n + n * sizeof(int32_t);
+        }
+        if (used != index[(size_t)j].originalSize)
+            throw std::string("Error: ragged record size of marker " + std::to_string(j) + " does not match the index");
+    }
+    return bed;
+}
+
+std::vector<uint8_t> readDensePreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
+                                                int64_t M)
+{
+    const std::vector<IndexEntry> index = readIndex(indexFile, M);
+    std::ifstream in = openPreprocessed(ppFile);
+    std::vector<uint8_t> bed((size_t)(M * ((N + 3) / 4)), 0);
+    const int64_t cb = (N + 3) / 4;
+    std::vector<double> col((size_t)N);
+    for (int64_t j = 0; j < M; ++j) {
+        checkUncompressed(index[(size_t)j], j);
+        if (index[(size_t)j].originalSize != (uint64_t)N * sizeof(double))
+            throw std::string("Error: dense record of marker " + std::to_string(j) + " is not N doubles");
+        in.seekg((std::streamoff)index[(size_t)j].pos);
+        in.read(reinterpret_cast<char *>(col.data()), (std::streamsize)(N * sizeof(double)));
+        if (!in)
+            throw std::string("Error: the preprocessed bed file ends before marker " + std::to_string(j));
+        // distinct values (one per genotype class present, identical within a class)
+        double val[4];
+        int64_t cnt[4] = {0, 0, 0, 0};
+        int nd = 0;
+        std::vector<uint8_t> cls((size_t)N);
+        for (int64_t i = 0; i < N; ++i) {
+            int k = 0;
+            while (k < nd && !(val[k] == col[(size_t)i]))
+                ++k;
+            if (k == nd) {
+                if (nd == 4 || std::isnan(col[(size_t)i]))
+                    throw std::string("Error: marker " + std::to_string(j) +
+                                      " of the preprocessed file is not a standardised genotype column");
+                val[nd++] = col[(size_t)i];
+            }
+            ++cnt[k];
+            cls[(size_t)i] = (uint8_t)k;
+        }
+        // the first assignment of distinct values to codes whose recomputed
+        // standardised values reproduce the column
+        int best[4] = {-1, -1, -1, -1};
+        int perm[4] = {0, 1, 2, 3};
+        bool found = false;
+        do {
+            int64_t n[4] = {0, 0, 0, 0};
+            for (int k = 0; k < nd; ++k)
+                n[perm[k]] = cnt[k];
+            double v[4];
+            if (!standardisedValues(N, n, v))
+                continue;
+            bool ok = true;
+            for (int k = 0; k < nd && ok; ++k)
+                ok = std::fabs(v[perm[k]] - val[k]) <= 1e-9 * std::max(1.0, std::fabs(val[k]));
+            if (ok) {
+                for (int k = 0; k < nd; ++k)
+                    best[k] = perm[k];
+                found = true;
+            }
+        } while (!found && std::next_permutation(perm, perm + 4));
+        if (!found)
+            throw std::string("Error: marker " + std::to_string(j) +
+                              " of the preprocessed file does not match a standardised genotype column");
+        for (int64_t i = 0; i < N; ++i)
+            setCode(bed, cb, j, i, (unsigned)best[cls[(size_t)i]]);
+    }
+    return bed;
+}
+
+void writeBedFile(const std::string &bedFile, const std::vector<uint8_t> &payload)
+{
+    std::ofstream out(bedFile, std::ios::binary);
+    if (!out)
+        throw std::string("Error: Unable to open [" + bedFile + "] for writing");
+    const unsigned char magic[3] = {0x6c, 0x1b, 0x01};
+    out.write(reinterpret_cast<const char *>(magic), 3);
+    out.write(reinterpret_cast<const char *>(payload.data()), (std::streamsize)payload.size());
 }
 
 }  // namespace brr

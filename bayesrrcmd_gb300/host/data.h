@@ -43,4 +43,19 @@ void writeRaggedPreprocessed(const std::string &ppFile, const std::string &index
                              const double *stats, const int64_t *off[3], const int32_t *idx[3]);
 std::vector<IndexEntry> readIndex(const std::string &indexFile, int64_t M);
 
+// Genotype codes in the BED payload layout (M x ceil(N/4) bytes, padding bits
+// zero) rebuilt from a preprocessed file, so that `brr` consumes the files of
+// the reference's --preprocess (src/analysisrunner.cpp:186-196 maps them for
+// ppbayes).  Ragged records give the codes directly (ones, twos, missing lists);
+// a dense record is the standardised column, whose at most four distinct values
+// are matched to genotype classes by recomputing the dense builder's values
+// (src/densemarkerbuilder.cpp:44-59) from the class counts each assignment
+// implies.  Throws std::string on a malformed or compressed file.
+std::vector<uint8_t> readRaggedPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
+                                                 int64_t M);
+std::vector<uint8_t> readDensePreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
+                                                int64_t M);
+// Writes a PLINK BED file (magic + SNP-major payload).
+void writeBedFile(const std::string &bedFile, const std::vector<uint8_t> &payload);
+
 }  // namespace brr

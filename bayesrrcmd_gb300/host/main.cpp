@@ -74,10 +74,29 @@ struct Ctx {
     ~Ctx() { brr_ctx_destroy(h); }
 };
 
-void packFromBed(Ctx &ctx, const Options &opt, const Data &data, const brr_config &cfg, std::vector<uint8_t> &bed)
+// Genotype codes of the analysis: the reference's ppbayes maps the file its
+// --preprocess wrote (src/analysisrunner.cpp:186-196); when that file and its
+// index exist they are read back into 2-bit codes, otherwise the BED is read.
+std::vector<uint8_t> readGenotypes(const Options &opt, int64_t N, int64_t M, bool preprocessed)
+{
+    const std::string pp = ppFileForType(opt.preprocessDataType, opt.dataFile);
+    const std::string ix = ppIndexFileForType(opt.preprocessDataType, opt.dataFile);
+    if (preprocessed && std::ifstream(pp).good() && std::ifstream(ix).good()) {
+        std::cout << "Start reading preprocessed bed file: " << pp << std::endl;
+        if (opt.preprocessDataType == PreprocessDataType::SparseRagged)
+            return readRaggedPreprocessedAsBed(pp, ix, N, M);
+        if (opt.preprocessDataType == PreprocessDataType::Dense)
+            return readDensePreprocessedAsBed(pp, ix, N, M);
+        throw std::string("Error: the GB300 path reads dense and ragged preprocessed files (--sparse-data ragged)");
+    }
+    return readBedPayload(opt.dataFile, N, M);
+}
+
+void packFromBed(Ctx &ctx, const Options &opt, const Data &data, const brr_config &cfg, std::vector<uint8_t> &bed,
+                 bool preprocessed = false)
 {
     check(brr_ctx_create(&cfg, &ctx.h), "brr_ctx_create");
-    bed = readBedPayload(opt.dataFile, cfg.N, cfg.M);
+    bed = readGenotypes(opt, cfg.N, cfg.M, preprocessed);
     check(brr_pack_bed(ctx.h, bed.data(), (int64_t)bed.size()), "brr_pack_bed");
 }
 
@@ -193,7 +212,7 @@ bool ppbayes(const Options &opt)
     const brr_config cfg = makeConfig(opt, data);
     Ctx ctx;
     std::vector<uint8_t> bed;
-    packFromBed(ctx, opt, data, cfg, bed);
+    packFromBed(ctx, opt, data, cfg, bed, true);
     check(brr_set_groups(ctx.h, data.G.data()), "brr_set_groups");
     check(brr_set_phenotype(ctx.h, data.y.data()), "brr_set_phenotype");
     check(brr_init_chain(ctx.h), "brr_init_chain");
@@ -275,6 +294,24 @@ int main(int argc, const char *argv[])
         opt.inputOptions(argc, argv);
         if (opt.printOptions) {
             printOptions(opt);
+            return 0;
+        }
+        if (!opt.exportBedFile.empty()) {
+            // preprocessed input (per --sparse-data) back to a PLINK BED: no GPU needed
+            Data data;
+            data.readFamFile(fileWithSuffix(opt.dataFile, ".fam"));
+            data.readBimFile(fileWithSuffix(opt.dataFile, ".bim"));
+            const std::string pp = ppFileForType(opt.preprocessDataType, opt.dataFile);
+            const std::string ix = ppIndexFileForType(opt.preprocessDataType, opt.dataFile);
+            std::vector<uint8_t> bed;
+            if (opt.preprocessDataType == PreprocessDataType::SparseRagged)
+                bed = readRaggedPreprocessedAsBed(pp, ix, data.numInds(), data.numSnps());
+            else if (opt.preprocessDataType == PreprocessDataType::Dense)
+                bed = readDensePreprocessedAsBed(pp, ix, data.numInds(), data.numSnps());
+            else
+                throw std::string("Error: --export-bed reads dense and ragged preprocessed files");
+            writeBedFile(opt.exportBedFile, bed);
+            std::cout << "Wrote " << opt.exportBedFile << std::endl;
             return 0;
         }
         switch (opt.analysisType) {

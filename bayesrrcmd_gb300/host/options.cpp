@@ -221,6 +221,8 @@ void Options::inputOptions(int argc, const char *argv[])
             device = std::atoi(need(i));
         } else if (!std::strcmp(a, "--print-options")) {
             printOptions = true;
+        } else if (!std::strcmp(a, "--export-bed")) {
+            exportBedFile = need(i);
         } else {
             std::stringstream e;
             e << "\nError: invalid option \"" << a << "\".\n";

@@ -51,6 +51,7 @@ struct Options {
     int specWidth = 0;
     int device = 0;
     bool printOptions = false;
+    std::string exportBedFile;             // --export-bed: preprocessed input back to PLINK BED, then exit
 
     Options();
     // Throws std::string on an invalid option, like the reference.

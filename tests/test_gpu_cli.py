@@ -121,3 +121,34 @@ def test_ppbayes_missing_phenotypes_are_an_error(brr, dataset):
                         "--chain-length", "2", "--mcmc-samples", str(d["dir"] / "x.csv")],
                        capture_output=True, text=True)
     assert r.returncode == 1 and "phenotype" in r.stderr
+
+
+@pytest.mark.parametrize("sparse", [None, "ragged"])
+def test_ppbayes_reads_reference_preprocessed_files(brr, dataset, sparse):
+    """With <prefix>.ppbed / .ragged.sparsebed and its index present, ppbayes
+    reads them as the reference does (src/analysisrunner.cpp:186-196): files
+    written in the reference's layout from the oracle's builders give the
+    oracle's chain."""
+    import test_cli_preprocessed as P
+    d = dataset
+    if sparse is None:
+        P.write_dense(d["prefix"], d["payload"], d["N"])
+        extra = []
+    else:
+        P.write_ragged(d["prefix"], d["payload"], d["N"])
+        extra = ["--sparse-data", "ragged"]
+    out = d["dir"] / "samples_pp.csv"
+    log = run(brr, "--analysis-type", "ppbayes", "--bfile", str(d["prefix"]), "--pheno", str(d["dir"] / "toy.phen"),
+              "--group", str(d["dir"] / "toy.group"), "--S", "0.01,0.001,0.0001;0.1,0.01",
+              "--chain-length", "4", "--burn-in", "0", "--thin", "1", "--seed", "11",
+              "--mcmc-samples", str(out), *extra)
+    assert "Start reading preprocessed bed file" in log
+    M, N = d["M"], d["N"]
+    oc = O.OracleChain(d["payload"], N, d["y"], S2, kind=0 if sparse is None else 1, group=d["group"], seed=11)
+    lines = out.read_text().splitlines()
+    for it, line in enumerate(lines[1:]):
+        oc.iterate(it)
+        s = oc.state()
+        v = np.array([float(t) for t in line.split(", ")])
+        np.testing.assert_allclose(v[2:2 + M], s["beta"], rtol=1e-5, atol=1e-9)
+        np.testing.assert_array_equal(v[5 + M:5 + 2 * M], s["comp"])
