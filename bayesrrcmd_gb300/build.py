@@ -81,7 +81,7 @@ def build_cli(verbose: bool = False) -> Path:
         cxx = shutil.which("g++") or shutil.which("c++")
         if not cxx:
             raise RuntimeError("no C++ compiler for the brr host")
-        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-o", str(CLI), *map(str, srcs),
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", "-o", str(CLI), *map(str, srcs),
                f"-L{LIBDIR}", "-lbrr_gpu", "-Wl,-rpath,$ORIGIN/../lib"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)

@@ -2,8 +2,13 @@
 // src/main.cpp:8-48 + AnalysisRunner::run, src/analysisrunner.cpp:278-306,
 // restricted to --preprocess and --analysis-type ppbayes over PLINK BED).
 // Compute runs in libbrr_gpu.so through the C ABI of include/brr_gpu.h.
+#include <charconv>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <fstream>
 #include <iomanip>
@@ -150,49 +155,155 @@ bool preprocess(const Options &opt)
 // Sample file of SampleWriter::openGroups / Writer::write
 // (src/samplewriter.cpp:82-118, src/writer.cpp:9-22): header with ',' and rows
 // with ", " in the stream's default precision.
-struct SampleWriter {
-    std::ofstream out;
+// Rows are formatted and written by a background thread, so that a saved
+// iteration costs the chain only the copy of its state (the reference writes
+// synchronously, which at N = M = 100k is several times a sweep's time).  Up to
+// two rows wait; a third waits for the writer.  Numbers are printed as the
+// default ostream does (6 significant digits, %g style).
+class SampleWriter {
+public:
     void open(const std::string &file, int64_t M, int64_t N, int G)
     {
         std::cout << "Opening results file " << file << std::endl;
-        out.open(file);
-        if (!out)
+        out_.open(file);
+        if (!out_)
             throw("Error: can not open the sample file [" + file + "] for writing.");
-        out << "iteration," << "mu,";
+        M_ = M;
+        N_ = N;
+        G_ = G;
+        out_ << "iteration," << "mu,";
         for (int64_t i = 0; i < M; ++i)
-            out << "beta[" << (i + 1) << "],";
-        out << "sigmaE,";
+            out_ << "beta[" << (i + 1) << "],";
+        out_ << "sigmaE,";
         for (int g = 0; g < G; ++g)
-            out << "sigmaG[" << (g + 1) << "],";
+            out_ << "sigmaG[" << (g + 1) << "],";
         for (int64_t i = 0; i < M; ++i)
-            out << "comp[" << (i + 1) << "],";
+            out_ << "comp[" << (i + 1) << "],";
         for (int64_t i = 0; i < M; ++i)
-            out << "acum[" << (i + 1) << "],";
+            out_ << "acum[" << (i + 1) << "],";
         int64_t i;
         for (i = 0; i < N - 1; ++i)
-            out << "epsilon[" << (i + 1) << "],";
-        out << "epsilon[" << (i + 1) << "]" << std::endl;
+            out_ << "epsilon[" << (i + 1) << "],";
+        out_ << "epsilon[" << (i + 1) << "]" << std::endl;
+        thread_ = std::thread([this] { run(); });
     }
-    void write(unsigned iteration, const brr_state &st, int64_t M, int64_t N, int G)
+    // Copies the state; returns as soon as a buffer is free.
+    void write(unsigned iteration, const brr_state &st)
     {
-        std::ostringstream row;
-        auto put = [&](double v) { row << v << ", "; };
-        put(iteration);
-        put(st.mu);
-        for (int64_t j = 0; j < M; ++j)
-            put(st.beta[j]);
-        put(st.sigmaE);
-        for (int g = 0; g < G; ++g)
-            put(st.sigmaG[g]);
-        for (int64_t j = 0; j < M; ++j)
-            put((double)st.comp[j]);
-        for (int64_t j = 0; j < M; ++j)
-            put(st.acum[j]);
-        for (int64_t i = 0; i < N - 1; ++i)
-            put(st.eps[i]);
-        row << st.eps[N - 1];
-        out << row.str() << std::endl;
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [this] { return queue_.size() < 2 || failed_; });
+        if (failed_)
+            throw std::string("Error: writing the sample file failed");
+        Row r;
+        if (!free_.empty()) {
+            r = std::move(free_.back());
+            free_.pop_back();
+        }
+        lk.unlock();
+        r.iteration = iteration;
+        r.mu = st.mu;
+        r.sigmaE = st.sigmaE;
+        r.sigmaG.assign(st.sigmaG, st.sigmaG + G_);
+        r.beta.assign(st.beta, st.beta + M_);
+        r.comp.assign(st.comp, st.comp + M_);
+        r.acum.assign(st.acum, st.acum + M_);
+        r.eps.assign(st.eps, st.eps + N_);
+        lk.lock();
+        queue_.push_back(std::move(r));
+        cv_.notify_all();
     }
+    // Waits for the queued rows and closes the file.
+    void close()
+    {
+        if (!thread_.joinable())
+            return;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            done_ = true;
+        }
+        cv_.notify_all();
+        thread_.join();
+        out_.close();
+        if (failed_)
+            throw std::string("Error: writing the sample file failed");
+    }
+    ~SampleWriter()
+    {
+        try {
+            close();
+        } catch (...) {
+        }
+    }
+
+private:
+    struct Row {
+        unsigned iteration = 0;
+        double mu = 0, sigmaE = 0;
+        std::vector<double> sigmaG, beta, acum, eps;
+        std::vector<int32_t> comp;
+    };
+    static void put(std::string &s, double v)
+    {
+        char buf[64];
+        const auto r = std::to_chars(buf, buf + sizeof buf, v, std::chars_format::general, 6);
+        s.append(buf, r.ptr);
+    }
+    void format(const Row &r, std::string &s) const
+    {
+        s.clear();
+        auto item = [&](double v) {
+            put(s, v);
+            s += ", ";
+        };
+        item(r.iteration);
+        item(r.mu);
+        for (double v : r.beta)
+            item(v);
+        item(r.sigmaE);
+        for (double v : r.sigmaG)
+            item(v);
+        for (int32_t c : r.comp)
+            item((double)c);
+        for (double v : r.acum)
+            item(v);
+        for (int64_t i = 0; i + 1 < N_; ++i)
+            item(r.eps[(size_t)i]);
+        put(s, r.eps[(size_t)(N_ - 1)]);
+        s += '\n';
+    }
+    void run()
+    {
+        std::string line;
+        for (;;) {
+            Row r;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [this] { return !queue_.empty() || done_; });
+                if (queue_.empty())
+                    break;
+                r = std::move(queue_.front());
+                queue_.pop_front();
+            }
+            format(r, line);
+            out_.write(line.data(), (std::streamsize)line.size());
+            std::lock_guard<std::mutex> lk(mu_);
+            if (!out_)
+                failed_ = true;
+            free_.push_back(std::move(r));
+            cv_.notify_all();
+        }
+        out_.flush();
+    }
+
+    std::ofstream out_;
+    int64_t M_ = 0, N_ = 0;
+    int G_ = 0;
+    std::thread thread_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<Row> queue_;
+    std::vector<Row> free_;
+    bool done_ = false, failed_ = false;
 };
 
 // runBayesRAnalysis + BayesRBase::runGibbs (src/analysisrunner.cpp:123-152,
@@ -243,7 +354,7 @@ bool ppbayes(const Options &opt)
         brr_get_timing(ctx.h, &sweep_ms, &total_ms, &rounds);
         if (it >= opt.burnin && it % opt.thin == 0) {
             check(brr_get_state(ctx.h, &st), "brr_get_state");
-            writer.write(it, st, M, N, G);
+            writer.write(it, st);
         }
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - s0).count();
         std::cout << secs << "s (" << sweep_ms / 1000.0 << "s)" << std::endl;
@@ -258,6 +369,7 @@ bool ppbayes(const Options &opt)
             iterLog << ", " << sweep_ms << ", " << total_ms << ", " << rounds << std::endl;
         }
     }
+    writer.close();
     const double dur = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
     std::cout << "duration: " << (long)dur << "s" << std::endl;
     const double n = opt.chainLength ? (double)opt.chainLength : 1.0;
