@@ -66,7 +66,9 @@ namespace brr {
 namespace {
 
 constexpr int kDotWarps = 8;
-constexpr int kBlockThreads = (kDotWarps + 1) * 32;
+constexpr int kResolveWarp = kDotWarps;       // samples the blocks
+constexpr int kChoreWarp = kDotWarps + 1;     // Gram copies and gathers, outputs
+constexpr int kBlockThreads = (kDotWarps + 2) * 32;
 constexpr int kAccBufs = 8;
 constexpr int kAccCopies = 8;   // CTA s adds into copy s % 8: 19 atomics per address and block, not 152
 constexpr int kAccBufWords = kAccCopies * kMaxSpec * 4;
@@ -170,6 +172,9 @@ __device__ __forceinline__ long long clk()
 }
 
 __device__ __forceinline__ void dot_warps_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// The dot warps and the chore warp before the arrival at a grid barrier.
+__device__ __forceinline__ void arrive_sync() { asm volatile("bar.sync 2, 288;" ::: "memory"); }
 
 // ---- fixed-point residual: E = eps * 2^kFrac, |E| < 2^62, as four balanced
 // 16-bit limbs E = l0 + l1 2^16 + l2 2^32 + l3 2^48 (l_k in [-2^15, 2^15)).
@@ -521,11 +526,13 @@ __device__ __forceinline__ void write_block_outputs(const SweepArgs &a, const Bl
     }
 }
 
-// One CTA of 9 warps per SM.  The register file is split between the SM's four
-// sub-partitions (16K registers each) and warps are placed round-robin, so the
-// sub-partition holding warps 0, 4 and 8 bounds every thread to 168 registers.
+// One CTA of 10 warps per SM (8 dot warps, the resolve warp, the chore warp).
+// The register file is split between the SM's four sub-partitions (16K
+// registers each) and warps are placed round-robin, so the sub-partitions
+// holding three warps bound every thread to 168 registers: the launch bound is
+// stated for 12 warps to give the compiler that limit.
 template <int KM, bool MISS>
-__global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
+__global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     // per block parity: residual-changing markers of the block (positions,
@@ -679,8 +686,8 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         code_issued = upto;
     };
 
-    // ---- Gram entries of block q (dot warps): CTA s gathers entries
-    // e = s + G*(t + 256*i) from the packed Gram into staging slot q % 8.  The
+    // ---- Gram entries of block q (chore warp): CTA s gathers entries
+    // e = s + G*(l + 32*i) from the packed Gram into staging slot q % 8.  The
     // first entry of each thread is loaded one iteration before it is stored,
     // so that the random reads of the Gram never delay the barrier arrival.
     double gval = 0.0;
@@ -712,7 +719,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
     };
     auto gather_load = [&](int q) {
         gent_mine = -1;
-        const unsigned e = (unsigned)sidx + (unsigned)tid * (unsigned)a.G;
+        const unsigned e = (unsigned)sidx + (unsigned)lane * (unsigned)a.G;
         if (e < gent && gram_entry(q, e, &gval))
             gent_mine = (int)e;
     };
@@ -725,8 +732,8 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         float2 *slot = gstage + (size_t)(q % kStageSlots) * gent;
         if (gent_mine >= 0)
             slot[gent_mine] = split2(gval);
-        for (unsigned e = (unsigned)sidx + (unsigned)(tid + kDotWarps * 32) * (unsigned)a.G; e < gent;
-             e += (unsigned)(kDotWarps * 32) * (unsigned)a.G) {
+        for (unsigned e = (unsigned)sidx + (unsigned)(lane + 32) * (unsigned)a.G; e < gent;
+             e += 32u * (unsigned)a.G) {
             double v;
             if (gram_entry(q, e, &v))
                 slot[e] = split2(v);
@@ -902,9 +909,8 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         dot_warps_sync();
     };
 
-    constexpr int kHelperWarp = kDotWarps - 1;   // polls the grid barrier
-    constexpr int kCopyThread = 5 * 32;   // issues the Gram bulk copies (a dot warp off the resolve warp's sub-partition)
-    constexpr int kWriterWarp = 6;        // writes a resolved block's outputs
+    constexpr int kHelperWarp = kDotWarps - 1;   // polls the grid barrier, assembles the next block's inputs
+    constexpr int kCopyThread = kChoreWarp * 32; // issues the Gram bulk copies
 
     // ---- inputs of block q (the helper warp, after its dot products): wait
     // for barrier q (lane c < 8 polls counter c), then per marker
@@ -999,8 +1005,14 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
     cp_async_wait_all();
     __syncthreads();
     if (warp < kDotWarps) {
-        gather_load(0);
         dot_block(0);
+        arrive_sync();
+        if (tid == 0)
+            arrive(0);
+        if (warp == kHelperWarp)
+            prepare_inputs(0, false);
+    } else if (warp == kChoreWarp) {
+        gather_load(0);
         gather_store(0);
         if (nblk > 1) {
             gather_load(1);
@@ -1008,11 +1020,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         }
         if (nblk > 2)
             gather_load(2);
-        dot_warps_sync();
-        if (tid == 0)
-            arrive(0);
-        if (warp == kHelperWarp)
-            prepare_inputs(0, false);
+        arrive_sync();
     }
 
     int r = 0;
@@ -1030,24 +1038,42 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
         const unsigned q0 = (unsigned)r * Bu;
         const int nb = nb_of(r);
 
-        if (warp < kDotWarps) {
-            // ---- dot side: update of block r-1, dots of block r+1 and their
-            // publication, then (after the arrival) the Gram copy of block r+1, the
-            // outputs of block r-1 and the inputs of block r+1
-            if (tid == kCopyThread && r == 0) {
+        if (warp == kChoreWarp) {
+            // ---- chore warp: Gram copy of block r+1 (its staging was published by
+            // barrier r, which the helper warp passed in the previous iteration),
+            // issued early so that the L2 burst of 152 CTAs copying the same slot
+            // overlaps the dot products; staged Gram entries of block r+2 (loaded
+            // in the previous iteration) and the zeroed accumulators of block r+3,
+            // written before the arrival; then the Gram loads of block r+3 and the
+            // outputs of block r-1
+            if (lane == 0) {
                 fence_proxy_async();
-                mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
-                bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
-                cp_issued = 0;
+                if (r == 0) {
+                    mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
+                    bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
+                    cp_issued = 0;
+                }
+                if (r + 1 < nblk) {
+                    const int q = r + 1;
+                    mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
+                    bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gent,
+                                  (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
+                    cp_issued = q;
+                }
             }
-            // staged Gram entries of block r+2 (loaded in the previous iteration) and
-            // the zeroed accumulators of block r+3 are written first, so that the
-            // release at the arrival does not wait for them
             if (r + 2 < nblk)
                 gather_store(r + 2);
             if (sidx == 0 && r + 3 < nblk)
-                for (int i = tid; i < kAccBufWords; i += kDotWarps * 32)
+                for (int i = lane; i < kAccBufWords; i += 32)
                     a.acc[(size_t)((r + 3) % kAccBufs) * kAccBufWords + i] = 0ull;
+            arrive_sync();
+            if (r + 3 < nblk)
+                gather_load(r + 3);
+            if (r >= 1 && sidx == (r - 1) % a.G)
+                write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
+        } else if (warp < kDotWarps) {
+            // ---- dot side: update of block r-1, dots of block r+1 and their
+            // publication, then the inputs of block r+1
             if (r >= 1) {
                 apply_update(r - 1);
                 mark(prof_d, 4);
@@ -1056,7 +1082,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
             if (r + 1 < nblk)
                 dot_block(r + 1);
             const long long td1 = prof_w1 ? clk() : 0;
-            dot_warps_sync();
+            arrive_sync();
             if (prof_w1)
                 tdl += td1 - td0;
             if (tid == 0 && r + 1 < nblk)
@@ -1065,21 +1091,6 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
             // inputs of block r+1, once barrier r+1 has passed
             if (warp == kHelperWarp && r + 1 < nblk)
                 prepare_inputs(r + 1, prof_h);
-            // then, off the critical path: Gram loads of block r+3 (stored in the
-            // next iteration), the Gram copy of block r+1 (its staging was
-            // published by barrier r), the outputs of block r-1
-            if (r + 3 < nblk)
-                gather_load(r + 3);
-            if (tid == kCopyThread && r + 1 < nblk) {
-                const int q = r + 1;
-                fence_proxy_async();
-                mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
-                bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gent,
-                              (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
-                cp_issued = q;
-            }
-            if (r >= 1 && sidx == (r - 1) % a.G && warp == kWriterWarp)
-                write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
         } else {
             // ---- resolve side
             mark(prof_r, 8);
@@ -1304,9 +1315,10 @@ __global__ void __launch_bounds__(kBlockThreads, 1) k_sweep_block(SweepArgs a)
             break;
     }
     // the last block: residual update and outputs
-    if (!s_abort && r == nblk && warp < kDotWarps) {
-        apply_update(nblk - 1);
-        if (sidx == (nblk - 1) % a.G && warp == kDotWarps - 1)
+    if (!s_abort && r == nblk) {
+        if (warp < kDotWarps)
+            apply_update(nblk - 1);
+        else if (warp == kChoreWarp && sidx == (nblk - 1) % a.G)
             write_block_outputs<KM>(a, s_out[(nblk - 1) & 1], gcf, s_gk, gbf, lane);
     }
     if (prof_d) {
