@@ -118,6 +118,8 @@ struct brr_ctx {
     float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)
     bool blocked = false;
     bool has_missing = false;
+    int kind = BRR_KIND_DENSE;          // storage: dense codes, or ragged lists (Ragged and Eigen markers)
+    bool eigen = false;                 // Eigen sparse markers (BRR_KIND_EIGEN)
     double gram_ms = 0.0;
 
     // pinned host staging
@@ -297,7 +299,7 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
         BRR_CUDA(launch_gather_block(c->d_order, cf.M, cf.N, c->d_table, c->d_scale, c->d_beta, c->d_u, c->d_z,
                                      c->d_group, eps_total, c->d_brec, c->st));
     else
-        BRR_CUDA(launch_gather(cf.form, cf.kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u,
+        BRR_CUDA(launch_gather(cf.form, c->kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u,
                                c->d_z, c->d_group, c->d_colsum, c->d_rec, c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + kCounterWords), c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
@@ -337,6 +339,7 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     a.acc = c->d_acc;
     a.counter = c->d_acc + kAccWords;
     a.stats_out = c->d_stats;
+    a.eigen = c->eigen ? 1 : 0;
     a.part = c->d_part;
     a.err = c->d_err;
     a.rounds_out = c->d_rounds;
@@ -350,13 +353,13 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     a.beta_df = c->d_bdf;
     a.acum_df = c->d_bdf ? c->d_bdf + cf.M : nullptr;
     BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 16, c->st));
-    const size_t smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, cf.kind, a);
+    const size_t smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, c->kind, a);
 
     BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
     if (c->blocked)
         BRR_CUDA(launch_sweep_block(a, smem, c->st));
     else
-        BRR_CUDA(launch_sweep(cf.form, cf.kind, a, smem, c->st));
+        BRR_CUDA(launch_sweep(cf.form, c->kind, a, smem, c->st));
     BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
     if (c->blocked)
         BRR_CUDA(launch_block_finish(cf.M, c->d_chosen, a.beta_df, a.acum_df, c->d_beta, c->d_acum, c->st));
@@ -391,7 +394,7 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     out->eps_sum = s1;
     out->eps_sqnorm = s2;
     out->rounds = rounds;
-    if (cf.kind == BRR_KIND_RAGGED)
+    if (c->kind == BRR_KIND_RAGGED)
         c->epsSum = c->h_stats[0];
     c->sweeps += 1;
     return BRR_OK;
@@ -527,7 +530,7 @@ int refresh_eps_impl(brr_ctx *c)
         BRR_CUDA(cudaMemcpy(c->d_nzj, nzj.data(), sizeof(uint32_t) * nzj.size(), cudaMemcpyHostToDevice));
         BRR_CUDA(cudaMemcpy(c->d_nzb, nzb.data(), sizeof(double) * nzb.size(), cudaMemcpyHostToDevice));
     }
-    BRR_CUDA(launch_refresh(cf.form, cf.kind, cf.N, c->d_ystd, c->mu, c->d_codes, c->col_stride, c->d_table, c->d_nzj,
+    BRR_CUDA(launch_refresh(cf.form, c->kind, cf.N, c->d_ystd, c->mu, c->d_codes, c->col_stride, c->d_table, c->d_nzj,
                             c->d_nzb, (int64_t)nzj.size(), c->d_eps, c->d_eps_hi, c->d_eps_lo, c->st));
     BRR_CUDA(cudaStreamSynchronize(c->st));
     return BRR_OK;
@@ -547,7 +550,7 @@ int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
     const brr_config &c = *cfg;
     if (c.N < 2 || c.M < 1 || c.M > (int64_t)UINT32_MAX)
         return fail(BRR_ERR_ARG, "need N >= 2 individuals and 1 <= M < 2^32 markers");
-    if (c.kind != BRR_KIND_DENSE && c.kind != BRR_KIND_RAGGED)
+    if (c.kind != BRR_KIND_DENSE && c.kind != BRR_KIND_RAGGED && c.kind != BRR_KIND_EIGEN)
         return fail(BRR_ERR_ARG, "unknown marker kind");
     if (c.form != BRR_FORM_FP64 && c.form != BRR_FORM_FP32C)
         return fail(BRR_ERR_ARG, "unknown sweep form");
@@ -576,6 +579,8 @@ int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
 
     brr_ctx *x = new brr_ctx();
     x->cfg = c;
+    x->kind = c.kind == BRR_KIND_DENSE ? BRR_KIND_DENSE : BRR_KIND_RAGGED;
+    x->eigen = c.kind == BRR_KIND_EIGEN;
     x->dev = c.device;
     x->sms = prop.multiProcessorCount;
     x->B = spec;
@@ -605,7 +610,7 @@ int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
     }
     x->slice_max = (int)(maxch * kChunk);
     x->slot_bytes = (int)(maxch * 16);
-    if (c.kind == BRR_KIND_RAGGED && x->slice_max > 65536) {
+    if (c.kind != BRR_KIND_DENSE && x->slice_max > 65536) {
         free_all(x);
         delete x;
         return fail(BRR_ERR_ARG, "ragged slices are limited to 65536 individuals; raise grid");
@@ -690,7 +695,7 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     if (cf.kind == BRR_KIND_DENSE) {
         BRR_CUDA(launch_dense_tables(c.d_counts, cf.N, M, c.d_table, c.d_scale, c.d_colsum, d_bad, c.st));
     } else {
-        BRR_CUDA(launch_ragged_stats(c.d_counts, cf.N, M, c.d_table, d_bad, c.st));
+        BRR_CUDA(launch_ragged_stats(c.d_counts, cf.N, M, c.eigen ? 1 : 0, c.d_table, d_bad, c.st));
     }
     int bad = INT_MAX;
     cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c.st);
@@ -708,7 +713,7 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
         for (int64_t j = 0; j < M && !c.has_missing; ++j)
             c.has_missing = cnt[4 * j + 3] != 0;
     }
-    if (cf.kind == BRR_KIND_RAGGED) {
+    if (c.kind == BRR_KIND_RAGGED) {
         const int64_t MG1 = M * (int64_t)c.G + 1;
         if (3 * MG1 > (int64_t)INT_MAX)
             return fail(BRR_ERR_ARG, "ragged offset table too large for int32");
@@ -757,8 +762,8 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     a.n_groups = cf.n_groups;
     a.slice_max = c.slice_max;
     a.slot_bytes = c.slot_bytes;
-    const size_t smem = sweep_smem_bytes(cf.form, cf.kind, a);
-    const int per_sm = sweep_max_ctas_per_sm(cf.form, cf.kind, smem);
+    const size_t smem = sweep_smem_bytes(cf.form, c.kind, a);
+    const int per_sm = sweep_max_ctas_per_sm(cf.form, c.kind, smem);
     if (per_sm < 1 || (int64_t)per_sm * c.sms < c.G)
         return fail(BRR_ERR_ARG, "the sweep kernel does not fit " + std::to_string(c.G) +
                                      " co-resident CTAs (shared memory " + std::to_string(smem) + " bytes)");
@@ -781,7 +786,7 @@ int brr_get_marker_table(brr_ctx *ctx, double *table, int64_t *counts)
 int brr_get_ragged_lists(brr_ctx *ctx, int64_t *off_ones, int32_t *ones, int64_t *off_twos, int32_t *twos,
                          int64_t *off_miss, int32_t *miss)
 {
-    if (!ctx || !ctx->packed || ctx->cfg.kind != BRR_KIND_RAGGED)
+    if (!ctx || !ctx->packed || ctx->kind != BRR_KIND_RAGGED)
         return fail(BRR_ERR_ARG, "no ragged markers packed");
     const int64_t M = ctx->cfg.M, G = ctx->G, MG1 = M * G + 1;
     std::vector<int32_t> off(3 * MG1);
@@ -926,7 +931,7 @@ int brr_iterate(brr_ctx *ctx, int32_t n_iter)
             mean = c.epsSum / Nd;
         }
         c.mu = mean + std::sqrt(c.sigmaE / Nd) * normal_mu(c.key(), it);
-        if (cf.kind == BRR_KIND_RAGGED)
+        if (c.kind == BRR_KIND_RAGGED)
             c.epsSum -= c.mu * Nd;
 
         // per-marker draws and the permutation (src/BayesRBase.cpp:196-198)
@@ -1106,7 +1111,7 @@ int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, dou
     if (e == cudaSuccess && n > 0)
         e = cudaMemcpyAsync(c.d_nzb, b, sizeof(double) * n, cudaMemcpyHostToDevice, c.st);
     if (e == cudaSuccess)
-        e = launch_refresh(BRR_FORM_FP64, c.cfg.kind, N, zero, 0.0, c.d_codes, c.col_stride, c.d_table, c.d_nzj,
+        e = launch_refresh(BRR_FORM_FP64, c.kind, N, zero, 0.0, c.d_codes, c.col_stride, c.d_table, c.d_nzj,
                            c.d_nzb, n, res, nullptr, nullptr, c.st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out, res, sizeof(double) * N, cudaMemcpyDeviceToHost, c.st);
@@ -1137,7 +1142,7 @@ int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_
             return fail(BRR_ERR_ARG, "marker index out of range");
     BRR_CUDA(cudaSetDevice(ctx->dev));
     std::string why;
-    if (noalloc_xbeta(ctx->dev, ctx->st, ctx->cfg.kind, ctx->cfg.N, ctx->d_codes, ctx->col_stride, ctx->d_table, idx, b,
+    if (noalloc_xbeta(ctx->dev, ctx->st, ctx->kind, ctx->cfg.N, ctx->d_codes, ctx->col_stride, ctx->d_table, idx, b,
                       n, d_out, why) != cudaSuccess)
         return fail(BRR_ERR_CUDA, why);
     return BRR_OK;

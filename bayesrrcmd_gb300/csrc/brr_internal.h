@@ -90,6 +90,8 @@ struct SweepArgs {
     const BlockRec *brec;        // blocked FP32C sweep: M records in sweep order
     float2 *beta_df;             // blocked FP32C sweep: new beta per marker (hi, lo)
     float2 *acum_df;             // blocked FP32C sweep: acum per marker (hi, lo)
+    int eigen;                   // ragged sweep: Eigen sparse markers (missing genotypes enter
+                                 // the dot product at the marker's mean)
 };
 
 // Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).
@@ -97,7 +99,7 @@ cudaError_t launch_pack_counts(const uint8_t *bed, int64_t N, int64_t M, uint8_t
                                int64_t col_stride, int64_t *counts, cudaStream_t st);
 cudaError_t launch_dense_tables(const int64_t *counts, int64_t N, int64_t M, double *lut,
                                 double *scale, double *colsum, int *bad, cudaStream_t st);
-cudaError_t launch_ragged_stats(const int64_t *counts, int64_t N, int64_t M, double *stats,
+cudaError_t launch_ragged_stats(const int64_t *counts, int64_t N, int64_t M, int eigen, double *stats,
                                 int *bad, cudaStream_t st);
 cudaError_t launch_ragged_slice_counts(const uint8_t *codes, int64_t col_stride, int64_t M, int G,
                                        const int32_t *slice_lo, int32_t *cnt3, cudaStream_t st);

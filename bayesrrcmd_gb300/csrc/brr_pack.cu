@@ -116,17 +116,24 @@ __global__ void k_dense_tables(const int64_t *__restrict__ counts, int64_t N, in
 
 // Ragged statistics (src/sparsemarker.cpp:8-19, src/raggedsparsemarkerbuilder.cpp:43-55):
 // mean over N including missing, sd from the sum and sum of squares.
-__global__ void k_ragged_stats(const int64_t *__restrict__ counts, int64_t N, int64_t M,
+__global__ void k_ragged_stats(const int64_t *__restrict__ counts, int64_t N, int64_t M, int eigen,
                                double *__restrict__ stats, int *bad)
 {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= M)
         return;
     const int64_t n1 = counts[4 * j + 1], n2 = counts[4 * j + 2];
-    const double Zsum = (double)(n1 + 2 * n2);
-    const double sqrdZ = (double)(n1 + 4 * n2);
+    double Zsum = (double)(n1 + 2 * n2);
+    double sqrdZ = (double)(n1 + 4 * n2);
     const double Nd = (double)N;
     const double mean = __ddiv_rn(Zsum, Nd);
+    if (eigen) {
+        // src/eigensparsemarkerbuilder.cpp:46-56: the missing genotypes enter
+        // sqrdZ and Zsum at the mean before the sd is formed
+        const double nm = (double)counts[4 * j + 3];
+        sqrdZ = __dadd_rn(sqrdZ, __dmul_rn(__dmul_rn(mean, mean), nm));
+        Zsum = __dadd_rn(Zsum, __dmul_rn(mean, nm));
+    }
     const double var = __ddiv_rn(__dadd_rn(__dsub_rn(sqrdZ, __dmul_rn(__dmul_rn(2.0, mean), Zsum)),
                                            __dmul_rn(__dmul_rn(Nd, mean), mean)),
                                  __dsub_rn(Nd, 1.0));
@@ -278,10 +285,10 @@ cudaError_t launch_dense_tables(const int64_t *counts, int64_t N, int64_t M, dou
     return cudaGetLastError();
 }
 
-cudaError_t launch_ragged_stats(const int64_t *counts, int64_t N, int64_t M, double *stats, int *bad,
+cudaError_t launch_ragged_stats(const int64_t *counts, int64_t N, int64_t M, int eigen, double *stats, int *bad,
                                 cudaStream_t st)
 {
-    k_ragged_stats<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(counts, N, M, stats, bad);
+    k_ragged_stats<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(counts, N, M, eigen, stats, bad);
     return cudaGetLastError();
 }
 

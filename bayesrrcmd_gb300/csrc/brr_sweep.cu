@@ -501,11 +501,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                     for (int e = ro[2] + tm.lane; e < ro[3]; e += lpm)
                         p2 += eps64[a.ridx[1][e]];
                     p = team_sum_d(p + 2.0 * p2, tm, lpm);
+                    // Eigen markers: the residual over missing genotypes, weighted
+                    // by the marker mean when the round is resolved
+                    double pm = 0.0;
+                    if (a.eigen) {
+                        for (int e = ro[4] + tm.lane; e < ro[5]; e += lpm)
+                            pm += eps64[a.ridx[2][e]];
+                        pm = team_sum_d(pm, tm, lpm);
+                    }
                     if (tm.lane == 0) {
-                        __int128 x;
-                        ok = fx_from_double(p, x);
-                        if (ok)
+                        __int128 x, xm;
+                        ok = fx_from_double(p, x) && fx_from_double(pm, xm);
+                        if (ok) {
                             publish(acc, x);
+                            if (pm != 0.0)
+                                publish(acc + 2, xm);
+                        }
                     }
                 } else {
                     float h = 0.f, l = 0.f;
@@ -518,11 +529,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                         df_add(h, l, 2.f * eh[i], 2.f * el[i]);
                     }
                     team_df_sum(h, l, tm, lpm);
+                    float mh = 0.f, ml = 0.f;
+                    if (a.eigen) {
+                        for (int e = ro[4] + tm.lane; e < ro[5]; e += lpm) {
+                            const int i = a.ridx[2][e];
+                            df_add(mh, ml, eh[i], el[i]);
+                        }
+                        team_df_sum(mh, ml, tm, lpm);
+                    }
                     if (tm.lane == 0) {
-                        __int128 x1, x2;
-                        ok = fx_from_float(h, x1) && fx_from_float(l, x2);
-                        if (ok)
+                        __int128 x1, x2, m1, m2;
+                        ok = fx_from_float(h, x1) && fx_from_float(l, x2) && fx_from_float(mh, m1) &&
+                             fx_from_float(ml, m2);
+                        if (ok) {
                             publish(acc, x1 + x2);
+                            if (mh != 0.f || ml != 0.f)
+                                publish(acc + 2, m1 + m2);
+                        }
                     }
                 }
             }
@@ -571,7 +594,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
                 }
             } else {
                 const double mean = rc.t[0], isd = rc.t[2], Zsum = rc.t[3];
-                num = (rc.beta_old * ((double)a.N - 1.0) - mean * s_scal[1] * isd) + (tot + s_scal[0] * Zsum) * isd;
+                // Eigen markers (src/eigenbayesrkernel.cpp:17-20): Zg holds the
+                // mean at missing genotypes, so their residual sum enters times
+                // the mean; Zsum includes the imputed values, which carries the
+                // pending uniform shift over the missing genotypes too
+                const double t12 =
+                    a.eigen ? tot + mean * fx_join((long long)ld_relaxed_u64(acc + 2), ld_relaxed_u64(acc + 3)) : tot;
+                num = (rc.beta_old * ((double)a.N - 1.0) - mean * s_scal[1] * isd) + (t12 + s_scal[0] * Zsum) * isd;
             }
             const int g = rc.group;
             const Pick pk = pick_marker<FORM != kFormFP64, KM>(num, rc.u, rc.z, rc.beta_old,

@@ -18,7 +18,7 @@ import numpy as np
 MAX_GROUPS = 64
 MAX_K = 16
 
-KIND_DENSE, KIND_RAGGED = 0, 1
+KIND_DENSE, KIND_RAGGED, KIND_EIGEN = 0, 1, 2
 FORM_FP64, FORM_FP32C = 0, 1
 
 ERRORS = {

@@ -156,6 +156,48 @@ void writeRaggedPreprocessed(const std::string &ppFile, const std::string &index
     }
 }
 
+void writeEigenPreprocessed(const std::string &ppFile, const std::string &indexFile, int64_t M, const double *stats,
+                            const int64_t *off[3], const int32_t *idx3[3])
+{
+    std::ofstream out(ppFile, std::ios::binary), idx(indexFile, std::ios::binary);
+    if (!out || !idx)
+        throw("Error: Unable to open the preprocessed bed file [" + ppFile + "] for writing.");
+    uint64_t pos = 0;
+    std::vector<double> values;
+    std::vector<int32_t> rows;
+    for (int64_t j = 0; j < M; ++j) {
+        // entries in ascending individual order: 1, 2, or the mean at missing genotypes
+        const double val[3] = {1.0, 2.0, stats[4 * j]};
+        int64_t q[3], e[3];
+        for (int k = 0; k < 3; ++k) {
+            q[k] = off[k][j];
+            e[k] = off[k][j + 1];
+        }
+        values.clear();
+        rows.clear();
+        for (;;) {
+            int kb = -1;
+            for (int k = 0; k < 3; ++k)
+                if (q[k] < e[k] && (kb < 0 || idx3[k][q[k]] < idx3[kb][q[kb]]))
+                    kb = k;
+            if (kb < 0)
+                break;
+            values.push_back(val[kb]);
+            rows.push_back(idx3[kb][q[kb]++]);
+        }
+        const int64_t count = (int64_t)values.size();
+        out.write(reinterpret_cast<const char *>(stats + 4 * j), 4 * sizeof(double));
+        out.write(reinterpret_cast<const char *>(&count), sizeof count);
+        if (count) {
+            out.write(reinterpret_cast<const char *>(values.data()), (std::streamsize)(count * sizeof(double)));
+            out.write(reinterpret_cast<const char *>(rows.data()), (std::streamsize)(count * sizeof(int32_t)));
+        }
+        const uint64_t size = 4 * sizeof(double) + sizeof count + (uint64_t)count * (sizeof(double) + sizeof(int32_t));
+        writeIndexEntry(idx, pos, size);
+        pos += size;
+    }
+}
+
 std::vector<IndexEntry> readIndex(const std::string &indexFile, int64_t M)
 {
     std::vector<IndexEntry> v((size_t)M);
@@ -262,6 +304,76 @@ std::vector<uint8_t> readRaggedPreprocessedAsBed(const std::string &ppFile, cons
         }
         if (used != index[(size_t)j].originalSize)
             throw std::string("Error: ragged record size of marker " + std::to_string(j) + " does not match the index");
+    }
+    return bed;
+}
+
+std::vector<uint8_t> readEigenPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
+                                                int64_t M)
+{
+    const std::vector<IndexEntry> index = readIndex(indexFile, M);
+    std::ifstream in = openPreprocessed(ppFile);
+    std::vector<uint8_t> bed = allHomozygousMajor(N, M);
+    const int64_t cb = (N + 3) / 4;
+    std::vector<double> values;
+    std::vector<int32_t> rows;
+    std::vector<int64_t> ones;
+    for (int64_t j = 0; j < M; ++j) {
+        const std::string which = " of marker " + std::to_string(j);
+        checkUncompressed(index[(size_t)j], j);
+        in.seekg((std::streamoff)index[(size_t)j].pos);
+        double stats[4];
+        int64_t count = -1;
+        in.read(reinterpret_cast<char *>(stats), sizeof stats);
+        in.read(reinterpret_cast<char *>(&count), sizeof count);
+        if (!in || count < 0 || count > N)
+            throw std::string("Error: malformed Eigen sparse record" + which);
+        values.resize((size_t)count);
+        rows.resize((size_t)count);
+        if (count) {
+            in.read(reinterpret_cast<char *>(values.data()), (std::streamsize)(count * sizeof(double)));
+            in.read(reinterpret_cast<char *>(rows.data()), (std::streamsize)(count * sizeof(int32_t)));
+        }
+        if (!in)
+            throw std::string("Error: malformed Eigen sparse record" + which);
+        const uint64_t used = 4 * sizeof(double) + sizeof count + (uint64_t)count * (sizeof(double) + sizeof(int32_t));
+        if (used != index[(size_t)j].originalSize)
+            throw std::string("Error: Eigen sparse record size" + which + " does not match the index");
+        // Zg holds 1, 2, or the mean (stats[0]) at missing genotypes
+        // (src/eigensparsemarkerbuilder.cpp:62-72)
+        const double mean = stats[0];
+        int64_t twos = 0;
+        ones.clear();
+        for (int64_t q = 0; q < count; ++q) {
+            const int32_t i = rows[(size_t)q];
+            if (i < 0 || i >= N || (q > 0 && i <= rows[(size_t)q - 1]))
+                throw std::string("Error: individual index out of range or out of order" + which);
+            const double v = values[(size_t)q];
+            if (v == 1.0) {
+                setCode(bed, cb, j, i, 2u);
+                ones.push_back(q);
+            } else if (v == 2.0) {
+                setCode(bed, cb, j, i, 0u);
+                ++twos;
+            } else if (v == mean) {
+                setCode(bed, cb, j, i, 1u);
+            } else {
+                throw std::string("Error: value other than 1, 2 or the marker mean" + which);
+            }
+        }
+        if (mean == 1.0) {
+            // a missing genotype stored as the mean 1.0 looks like a heterozygote;
+            // the genotype sum is N, so N - 2*twos of the 1.0 entries are
+            // heterozygotes and the rest are missing.  Which ones are missing
+            // does not change the chain: Zg, the statistics, the dot products
+            // and the residual updates (zero for a value equal to the mean) are
+            // the same, so the last entries are marked missing.
+            const int64_t het = N - 2 * twos;
+            if (het < 0 || het > (int64_t)ones.size())
+                throw std::string("Error: Eigen sparse record" + which + " does not match its mean");
+            for (size_t q = (size_t)het; q < ones.size(); ++q)
+                setCode(bed, cb, j, rows[(size_t)ones[q]], 1u);
+        }
     }
     return bed;
 }

@@ -41,6 +41,11 @@ void writeDensePreprocessed(const std::string &ppFile, const std::string &indexF
                             const double *lut, const uint8_t *bedPayload);
 void writeRaggedPreprocessed(const std::string &ppFile, const std::string &indexFile, int64_t M,
                              const double *stats, const int64_t *off[3], const int32_t *idx[3]);
+// Eigen sparse records (src/eigensparsemarker.cpp:39-58): the four statistics,
+// an int64 entry count, the entries' double values (1, 2, or the mean at
+// missing genotypes) and their int32 individual indices, ascending.
+void writeEigenPreprocessed(const std::string &ppFile, const std::string &indexFile, int64_t M,
+                            const double *stats, const int64_t *off[3], const int32_t *idx[3]);
 std::vector<IndexEntry> readIndex(const std::string &indexFile, int64_t M);
 
 // Genotype codes in the BED payload layout (M x ceil(N/4) bytes, padding bits
@@ -54,6 +59,11 @@ std::vector<IndexEntry> readIndex(const std::string &indexFile, int64_t M);
 std::vector<uint8_t> readRaggedPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
                                                  int64_t M);
 std::vector<uint8_t> readDensePreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
+                                                int64_t M);
+// Eigen sparse records give the codes from the entry values; when a marker's
+// mean is exactly 1 its missing entries (stored as 1.0) are told apart from
+// heterozygotes by count only, which leaves the chain unchanged.
+std::vector<uint8_t> readEigenPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
                                                 int64_t M);
 // Writes a PLINK BED file (magic + SNP-major payload).
 void writeBedFile(const std::string &bedFile, const std::vector<uint8_t> &payload);

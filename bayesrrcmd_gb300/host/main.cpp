@@ -52,7 +52,9 @@ brr_config makeConfig(const Options &opt, const Data &data)
     brr_config c{};
     c.N = data.numInds();
     c.M = data.numSnps();
-    c.kind = opt.preprocessDataType == PreprocessDataType::SparseRagged ? BRR_KIND_RAGGED : BRR_KIND_DENSE;
+    c.kind = opt.preprocessDataType == PreprocessDataType::SparseRagged  ? BRR_KIND_RAGGED
+             : opt.preprocessDataType == PreprocessDataType::SparseEigen ? BRR_KIND_EIGEN
+                                                                          : BRR_KIND_DENSE;
     c.form = opt.form == "fp32c" ? BRR_FORM_FP32C : BRR_FORM_FP64;
     c.n_groups = (int)opt.S.size();
     if (c.n_groups < 1 || c.n_groups > BRR_MAX_GROUPS)
@@ -82,17 +84,25 @@ struct Ctx {
 // Genotype codes of the analysis: the reference's ppbayes maps the file its
 // --preprocess wrote (src/analysisrunner.cpp:186-196); when that file and its
 // index exist they are read back into 2-bit codes, otherwise the BED is read.
+std::vector<uint8_t> readPreprocessedAsBed(const Options &opt, int64_t N, int64_t M)
+{
+    const std::string pp = ppFileForType(opt.preprocessDataType, opt.dataFile);
+    const std::string ix = ppIndexFileForType(opt.preprocessDataType, opt.dataFile);
+    switch (opt.preprocessDataType) {
+    case PreprocessDataType::Dense: return readDensePreprocessedAsBed(pp, ix, N, M);
+    case PreprocessDataType::SparseEigen: return readEigenPreprocessedAsBed(pp, ix, N, M);
+    case PreprocessDataType::SparseRagged: return readRaggedPreprocessedAsBed(pp, ix, N, M);
+    default: throw std::string("Error: unsupported --sparse-data type (dense, eigen or ragged)");
+    }
+}
+
 std::vector<uint8_t> readGenotypes(const Options &opt, int64_t N, int64_t M, bool preprocessed)
 {
     const std::string pp = ppFileForType(opt.preprocessDataType, opt.dataFile);
     const std::string ix = ppIndexFileForType(opt.preprocessDataType, opt.dataFile);
     if (preprocessed && std::ifstream(pp).good() && std::ifstream(ix).good()) {
         std::cout << "Start reading preprocessed bed file: " << pp << std::endl;
-        if (opt.preprocessDataType == PreprocessDataType::SparseRagged)
-            return readRaggedPreprocessedAsBed(pp, ix, N, M);
-        if (opt.preprocessDataType == PreprocessDataType::Dense)
-            return readDensePreprocessedAsBed(pp, ix, N, M);
-        throw std::string("Error: the GB300 path reads dense and ragged preprocessed files (--sparse-data ragged)");
+        return readPreprocessedAsBed(opt, N, M);
     }
     return readBedPayload(opt.dataFile, N, M);
 }
@@ -108,8 +118,8 @@ void packFromBed(Ctx &ctx, const Options &opt, const Data &data, const brr_confi
 // src/analysisrunner.cpp:47-78 + src/preprocessgraph.cpp:152-244
 bool preprocess(const Options &opt)
 {
-    if (opt.preprocessDataType != PreprocessDataType::Dense && opt.preprocessDataType != PreprocessDataType::SparseRagged)
-        throw std::string("Error: the GB300 path preprocesses dense and ragged markers (--sparse-data ragged)");
+    if (opt.preprocessDataType == PreprocessDataType::None)
+        throw std::string("Error: unsupported --sparse-data type (dense, eigen or ragged)");
     if (opt.compress)
         std::cout << "Note: --compress is not applied; preprocessed files are written uncompressed" << std::endl;
     const auto t0 = std::chrono::steady_clock::now();
@@ -145,7 +155,10 @@ bool preprocess(const Options &opt)
               "brr_get_ragged_lists");
         const int64_t *offs[3] = {off[0].data(), off[1].data(), off[2].data()};
         const int32_t *idxs[3] = {idx[0].data(), idx[1].data(), idx[2].data()};
-        writeRaggedPreprocessed(pp, ix, M, table.data(), offs, idxs);
+        if (cfg.kind == BRR_KIND_EIGEN)
+            writeEigenPreprocessed(pp, ix, M, table.data(), offs, idxs);
+        else
+            writeRaggedPreprocessed(pp, ix, M, table.data(), offs, idxs);
     }
     const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::printf("Finished preprocessing the bed file in %.3f sec.\n\n", s);
@@ -413,16 +426,7 @@ int main(int argc, const char *argv[])
             Data data;
             data.readFamFile(fileWithSuffix(opt.dataFile, ".fam"));
             data.readBimFile(fileWithSuffix(opt.dataFile, ".bim"));
-            const std::string pp = ppFileForType(opt.preprocessDataType, opt.dataFile);
-            const std::string ix = ppIndexFileForType(opt.preprocessDataType, opt.dataFile);
-            std::vector<uint8_t> bed;
-            if (opt.preprocessDataType == PreprocessDataType::SparseRagged)
-                bed = readRaggedPreprocessedAsBed(pp, ix, data.numInds(), data.numSnps());
-            else if (opt.preprocessDataType == PreprocessDataType::Dense)
-                bed = readDensePreprocessedAsBed(pp, ix, data.numInds(), data.numSnps());
-            else
-                throw std::string("Error: --export-bed reads dense and ragged preprocessed files");
-            writeBedFile(opt.exportBedFile, bed);
+            writeBedFile(opt.exportBedFile, readPreprocessedAsBed(opt, data.numInds(), data.numSnps()));
             std::cout << "Wrote " << opt.exportBedFile << std::endl;
             return 0;
         }

@@ -17,7 +17,9 @@
  *                         (DenseMarker::Cx values; SparseMarker mean/sd/sqrdZ/Zsum,
  *                         src/densemarker.h:7-20, src/sparsemarker.h:6-18)
  *   brr_get_ragged_lists  RaggedSparseMarker::Zones/Ztwos/Zmissing
- *                         (src/raggedsparsemarker.h:7-23)
+ *                         (src/raggedsparsemarker.h:7-23); for the Eigen kind the
+ *                         entries of EigenSparseMarker::Zg by value
+ *                         (src/eigensparsemarker.h:6-16)
  *   brr_set_phenotype     Data::readPhenotypeFile result + BayesRBase::init's
  *                         standardisation (src/data.cpp:334-365,
  *                         src/BayesRBase.cpp:85-90)
@@ -57,6 +59,11 @@ extern "C" {
 
 #define BRR_KIND_DENSE 0     /* 2-bit packed genotypes, standardised on the fly */
 #define BRR_KIND_RAGGED 1    /* index lists of ones / twos / missing */
+#define BRR_KIND_EIGEN 2     /* the same index lists with the Eigen sparse marker's
+                              * statistics: missing genotypes imputed at the mean in
+                              * sqrdZ, Zsum, sd and the dot product
+                              * (src/eigensparsemarkerbuilder.cpp:40-75,
+                              * src/eigenbayesrkernel.cpp:10-20) */
 
 #define BRR_FORM_FP64 0      /* plain FP64 sweep: the drop-in */
 #define BRR_FORM_FP32C 1     /* FP32 compensated dots and residual, FP64 refresh */
@@ -122,10 +129,10 @@ int brr_pack_bed(brr_ctx *ctx, const uint8_t *bed, int64_t nbytes);
 int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes);
 
 /* Per-marker table, M x 4 doubles.  Dense: the standardised value of each
- * 2-bit code {0: g=2, 1: missing, 2: g=1, 3: g=0}.  Ragged: {mean, sd, sqrdZ,
- * Zsum}.  counts (optional): M x 4 int64 {n0, n1, n2, nmissing}. */
+ * 2-bit code {0: g=2, 1: missing, 2: g=1, 3: g=0}.  Ragged and Eigen: {mean,
+ * sd, sqrdZ, Zsum} (Eigen: sqrdZ, Zsum and sd include the imputed missing values).  counts (optional): M x 4 int64 {n0, n1, n2, nmissing}. */
 int brr_get_marker_table(brr_ctx *ctx, double *table, int64_t *counts);
-/* Ragged index lists in ascending individual order.  off_*: M+1 offsets;
+/* Ragged (and Eigen) index lists in ascending individual order.  off_*: M+1 offsets;
  * ones/twos/miss sized from the counts. */
 int brr_get_ragged_lists(brr_ctx *ctx, int64_t *off_ones, int32_t *ones,
                          int64_t *off_twos, int32_t *twos,

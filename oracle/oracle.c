@@ -251,12 +251,18 @@ int or_dense_columns(const uint8_t *bed, int64_t N, int64_t M, double *x)
 /* Ragged builder statistics (src/sparsemarker.cpp:8-19 accumulates value and
  * value^2 of non-missing genotypes; src/raggedsparsemarkerbuilder.cpp:43-55
  * divides by N including missing and forms the sd). */
-static int ragged_stats_from_counts(const int64_t c[4], int64_t N, double st[4])
+static int sparse_stats_from_counts(const int64_t c[4], int64_t N, int eigen, double st[4])
 {
-    const double Zsum = (double)(c[1] + 2 * c[2]);
-    const double sqrdZ = (double)(c[1] + 4 * c[2]);
+    double Zsum = (double)(c[1] + 2 * c[2]);
+    double sqrdZ = (double)(c[1] + 4 * c[2]);
     const double Nd = (double)N;
     const double mean = Zsum / Nd;
+    if (eigen) {
+        /* src/eigensparsemarkerbuilder.cpp:46-56: missing genotypes imputed at
+         * the mean in sqrdZ and Zsum before the sd */
+        sqrdZ += (mean * mean) * (double)c[3];
+        Zsum += mean * (double)c[3];
+    }
     const double sd = sqrt(((sqrdZ - (2.0 * mean) * Zsum) + (Nd * mean) * mean) / (Nd - 1.0));
     st[0] = mean;
     st[1] = sd;
@@ -269,7 +275,7 @@ static int ragged_stats_from_counts(const int64_t c[4], int64_t N, double st[4])
     return OR_OK;
 }
 
-int or_ragged_stats(const uint8_t *bed, int64_t N, int64_t M, double *stats)
+static int sparse_stats(const uint8_t *bed, int64_t N, int64_t M, int eigen, double *stats)
 {
     if (!bed || !stats || N < 2 || M <= 0)
         return OR_ERR_ARG;
@@ -278,9 +284,19 @@ int or_ragged_stats(const uint8_t *bed, int64_t N, int64_t M, double *stats)
         return OR_ERR_ARG;
     int rc = or_marker_counts(bed, N, M, cnt);
     for (int64_t j = 0; rc == OR_OK && j < M; ++j)
-        rc = ragged_stats_from_counts(cnt + 4 * j, N, stats + 4 * j);
+        rc = sparse_stats_from_counts(cnt + 4 * j, N, eigen, stats + 4 * j);
     free(cnt);
     return rc;
+}
+
+int or_ragged_stats(const uint8_t *bed, int64_t N, int64_t M, double *stats)
+{
+    return sparse_stats(bed, N, M, 0, stats);
+}
+
+int or_eigen_stats(const uint8_t *bed, int64_t N, int64_t M, double *stats)
+{
+    return sparse_stats(bed, N, M, 1, stats);
 }
 
 /* Index lists in ascending individual order (src/raggedsparsemarkerbuilder.cpp:25-41). */
@@ -352,7 +368,7 @@ int or_markers_create(const or_problem *p, or_markers **out)
     if (p->kind == OR_KIND_DENSE) {
         m->x = (double *)malloc(sizeof(double) * (size_t)p->N * (size_t)p->M);
         rc = m->x ? or_dense_columns(p->bed, p->N, p->M, m->x) : OR_ERR_ARG;
-    } else if (p->kind == OR_KIND_RAGGED) {
+    } else if (p->kind == OR_KIND_RAGGED || p->kind == OR_KIND_EIGEN) {
         int64_t *cnt = (int64_t *)malloc(sizeof(int64_t) * 4 * (size_t)p->M);
         m->stats = (double *)malloc(sizeof(double) * 4 * (size_t)p->M);
         rc = (cnt && m->stats) ? or_marker_counts(p->bed, p->N, p->M, cnt) : OR_ERR_ARG;
@@ -361,7 +377,7 @@ int or_markers_create(const or_problem *p, or_markers **out)
             tot[0] += cnt[4 * j + 1];
             tot[1] += cnt[4 * j + 2];
             tot[2] += cnt[4 * j + 3];
-            rc = ragged_stats_from_counts(cnt + 4 * j, p->N, m->stats + 4 * j);
+            rc = sparse_stats_from_counts(cnt + 4 * j, p->N, p->kind == OR_KIND_EIGEN, m->stats + 4 * j);
         }
         for (int k = 0; rc == OR_OK && k < 3; ++k) {
             m->off[k] = (int64_t *)malloc(sizeof(int64_t) * (size_t)(p->M + 1));
@@ -475,7 +491,29 @@ static void process_column(const or_problem *p, const or_markers *mk, or_state *
             s1 += s->eps[mk->idx[0][q]];
         for (int64_t q = mk->off[1][j]; q < mk->off[1][j + 1]; ++q)
             s2 += s->eps[mk->idx[1][q]];
-        const double dot = (s1 + 2.0 * s2) / sd;
+        double zdot = s1 + 2.0 * s2;
+        if (mk->kind == OR_KIND_EIGEN) {
+            /* Zg.dot(epsilon) over the stored entries in ascending individual
+             * order, Zg = 1, 2, or the mean at missing genotypes
+             * (src/eigensparsemarkerbuilder.cpp:62-72, src/eigenbayesrkernel.cpp:17-20) */
+            int64_t q[3], e[3];
+            for (int k = 0; k < 3; ++k) {
+                q[k] = mk->off[k][j];
+                e[k] = mk->off[k][j + 1];
+            }
+            const double val[3] = {1.0, 2.0, mean};
+            zdot = 0.0;
+            for (;;) {
+                int kb = -1;
+                for (int k = 0; k < 3; ++k)
+                    if (q[k] < e[k] && (kb < 0 || mk->idx[k][q[k]] < mk->idx[kb][q[kb]]))
+                        kb = k;
+                if (kb < 0)
+                    break;
+                zdot += val[kb] * s->eps[mk->idx[kb][q[kb]++]];
+            }
+        }
+        const double dot = zdot / sd;
         num = (beta_old * ((double)N - 1.0) - (mean * s->epsSum) / sd) + dot;
     }
 

@@ -39,6 +39,7 @@ extern "C" {
 /* Marker storage kinds (reference: src/common.h:27-32 PreprocessDataType). */
 #define OR_KIND_DENSE 0
 #define OR_KIND_RAGGED 1
+#define OR_KIND_EIGEN 2   /* ragged lists with mean-imputed statistics and dot (src/common.h:30) */
 
 /* Status codes. */
 #define OR_OK 0
@@ -72,6 +73,10 @@ int or_dense_columns(const uint8_t *bed, int64_t N, int64_t M, double *x);
 /* Ragged marker statistics (reference: src/raggedsparsemarkerbuilder.cpp:25-55,
  * src/sparsemarker.cpp:8-19).  stats: M x 4 doubles {mean, sd, sqrdZ, Zsum}. */
 int or_ragged_stats(const uint8_t *bed, int64_t N, int64_t M, double *stats);
+/* Eigen sparse marker statistics (reference: src/eigensparsemarkerbuilder.cpp:40-56):
+ * as above with the missing genotypes imputed at the mean in sqrdZ and Zsum,
+ * and the sd formed from those. */
+int or_eigen_stats(const uint8_t *bed, int64_t N, int64_t M, double *stats);
 /* Ragged index lists.  off: M+1 offsets per list kind (3 x (M+1), kinds
  * ones, twos, missing); idx: concatenated int32 indices for each kind, sized by
  * the caller from or_marker_counts (3 buffers). */
@@ -83,7 +88,7 @@ int or_ragged_lists(const uint8_t *bed, int64_t N, int64_t M,
 /* ---------------- chain ---------------- */
 typedef struct {
     int64_t N, M;
-    int32_t kind;                /* OR_KIND_DENSE or OR_KIND_RAGGED */
+    int32_t kind;                /* OR_KIND_DENSE, OR_KIND_RAGGED or OR_KIND_EIGEN */
     int32_t n_groups;
     const int32_t *group;        /* M group ids in 0..n_groups-1 */
     const int32_t *K;            /* n_groups: mixture components incl. the zero one */

@@ -6,10 +6,10 @@
    uk10k fixture (test.zip:test/data/uk10k_chr1_1mb.bed, read from the
    reference checkout when it is mounted) decoded by the oracle; only column
    sums and the first 64 markers are stored.
-2. synth_dense.npz / synth_ragged.npz: a small seeded synthetic problem (BED
-   payload, phenotype, groups) with the oracle's packer outputs and the state
-   after each of five Gibbs iterations.  Both dense and ragged problems carry
-   missing genotypes, N not a multiple of 4 or 64, and two groups with
+2. synth_dense.npz / synth_ragged.npz / synth_eigen.npz: a small seeded
+   synthetic problem (BED payload, phenotype, groups) with the oracle's packer
+   outputs and the state after each of five Gibbs iterations.  All problems
+   carry missing genotypes, N not a multiple of 4 or 64, and two groups with
    different component counts.
 """
 from __future__ import annotations
@@ -46,7 +46,7 @@ def make_synth(kind: int, iters: int = 5):
     if kind == 0:
         rc, t = O.marker_table_dense(bed, N)
     else:
-        rc, t = O.ragged_stats(bed, N)
+        rc, t = O.ragged_stats(bed, N) if kind == 1 else O.eigen_stats(bed, N)
         for name, (off, idx) in zip(("ones", "twos", "miss"), O.ragged_lists(bed, N)):
             out[f"off_{name}"], out[f"idx_{name}"] = off, idx
     assert rc == 0
@@ -74,6 +74,7 @@ def main():
         np.savez_compressed(HERE / "uk10k_counts_digest.npz", col_sums=c.sum(0), head=c[:64])
     np.savez_compressed(HERE / "synth_dense.npz", **make_synth(0))
     np.savez_compressed(HERE / "synth_ragged.npz", **make_synth(1))
+    np.savez_compressed(HERE / "synth_eigen.npz", **make_synth(2))
 
 
 if __name__ == "__main__":

@@ -54,6 +54,7 @@ def lib():
         L.or_dense_lut.argtypes = [u8, C.c_int64, C.c_int64, f64]
         L.or_dense_columns.argtypes = [u8, C.c_int64, C.c_int64, f64]
         L.or_ragged_stats.argtypes = [u8, C.c_int64, C.c_int64, f64]
+        L.or_eigen_stats.argtypes = [u8, C.c_int64, C.c_int64, f64]
         L.or_ragged_lists.argtypes = [u8, C.c_int64, C.c_int64, i64, i32, i64, i32, i64, i32]
         L.or_markers_create.argtypes = [C.POINTER(OrProblem), C.POINTER(C.c_void_p)]
         L.or_markers_destroy.argtypes = [C.c_void_p]
@@ -102,6 +103,13 @@ def ragged_stats(bed, N):
     M = bed.shape[0]
     out = np.zeros((M, 4))
     rc = lib().or_ragged_stats(p(np.ascontiguousarray(bed), C.c_uint8), N, M, p(out, C.c_double))
+    return rc, out
+
+
+def eigen_stats(bed, N):
+    M = bed.shape[0]
+    out = np.zeros((M, 4))
+    rc = lib().or_eigen_stats(p(np.ascontiguousarray(bed), C.c_uint8), N, M, p(out, C.c_double))
     return rc, out
 
 

@@ -4,10 +4,11 @@ The reference's ppbayes maps the file its --preprocess wrote
 (src/analysisrunner.cpp:186-196, src/data.cpp:52-75): dense records of N
 standardised doubles (src/densemarker.cpp:34-49) or ragged records of four
 statistics and the Zones/Ztwos/Zmissing index lists
-(src/raggedsparsemarker.cpp:43-66), with a {pos, compressedSize, originalSize}
-index per marker (src/common.h:57-61).  Files are written here in that layout
+(src/raggedsparsemarker.cpp:43-66), or Eigen sparse records of the statistics
+and the Zg entries (src/eigensparsemarker.cpp:39-58), with a
+{pos, compressedSize, originalSize} index per marker (src/common.h:57-61).  Files are written here in that layout
 from the oracle's builders; `brr --export-bed` must return the original BED
-payload bit for bit from ragged files, and from dense files codes that
+payload bit for bit from ragged and Eigen files, and from dense files codes that
 standardise to the same columns (identical codes where all three genotype
 classes occur), including markers where genotype classes are absent.
 """
@@ -73,6 +74,29 @@ def write_ragged(prefix, payload, N):
                 size += 8 + 4 * part.size
             sizes.append(size)
     write_index(str(prefix) + ".ragged.sparsebedindex", sizes)
+
+
+def write_eigen(prefix, payload, N):
+    """Records of src/eigensparsemarker.cpp:39-58: stats, int64 count, double
+    values (1, 2, or the mean at missing genotypes), int32 indices."""
+    rc, stats = O.eigen_stats(payload, N)
+    assert rc == 0
+    lists = O.ragged_lists(payload, N)
+    M = payload.shape[0]
+    sizes = []
+    with open(str(prefix) + ".eigen.sparsebed", "wb") as f:
+        for j in range(M):
+            parts = [ix[off[j]:off[j + 1]] for off, ix in lists]
+            vals = [np.full(len(parts[0]), 1.0), np.full(len(parts[1]), 2.0), np.full(len(parts[2]), stats[j, 0])]
+            rows = np.concatenate(parts).astype(np.int32)
+            order = np.argsort(rows, kind="stable")
+            f.write(stats[j].astype(np.float64).tobytes())
+            f.write(np.int64(rows.size).tobytes())
+            f.write(np.concatenate(vals)[order].astype(np.float64).tobytes())
+            f.write(rows[order].tobytes())
+            sizes.append(40 + 12 * rows.size)
+    write_index(str(prefix) + ".eigen.sparsebedindex", sizes)
+    return stats
 
 
 def export(brr, prefix, out, *extra):
@@ -151,3 +175,52 @@ def test_ragged_index_out_of_range_is_an_error(brr, tmp_path):
     open(str(prefix) + ".ragged.sparsebed", "wb").write(bytes(raw))
     r = export(brr, prefix, tmp_path / "back.bed", "--sparse-data", "ragged")
     assert r.returncode == 1 and "out of range" in r.stderr
+
+
+@pytest.mark.parametrize("missing", [0.0, 0.02])
+def test_eigen_preprocessed_back_to_bed(brr, tmp_path, missing):
+    prefix, payload, N, M = dataset(tmp_path, missing=missing)
+    write_eigen(prefix, payload, N)
+    r = export(brr, prefix, tmp_path / "back.bed", "--sparse-data", "eigen")
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(read_payload(tmp_path / "back.bed", N, M), payload)
+
+
+def test_eigen_marker_with_mean_one(brr, tmp_path):
+    """Genotype sum N: missing genotypes are stored as 1.0 like heterozygotes.
+    The reader recovers the counts (hence the statistics) exactly; which
+    entries it marks missing does not change Zg."""
+    prefix, payload, N, M = dataset(tmp_path, missing=0.02)
+    g = plink.decode_bed(payload, N)
+    rng = np.random.default_rng(3)
+    row = np.zeros(N, np.int8)
+    perm = rng.permutation(N)
+    row[perm[:100]] = 2
+    row[perm[100:233]] = 1            # 2*100 + 133 = 333 = N
+    row[perm[233:253]] = -1
+    g[5] = row
+    payload = plink.encode_bed(g)
+    plink.write_plink(prefix, payload, N)
+    stats = write_eigen(prefix, payload, N)
+    assert stats[5, 0] == 1.0
+    r = export(brr, prefix, tmp_path / "back.bed", "--sparse-data", "eigen")
+    assert r.returncode == 0, r.stderr
+    back = read_payload(tmp_path / "back.bed", N, M)
+    keep = np.arange(M) != 5
+    np.testing.assert_array_equal(back[keep], payload[keep])
+    np.testing.assert_array_equal(O.counts(back, N)[5], O.counts(payload, N)[5])
+    assert np.array_equal(O.eigen_stats(back, N)[1][5], stats[5])
+    gb = plink.decode_bed(back, N)[5]
+    Zg = lambda r: np.where(r < 0, 1.0, r.astype(float))
+    np.testing.assert_array_equal(Zg(gb), Zg(row))
+
+
+def test_eigen_value_that_is_not_a_genotype_is_an_error(brr, tmp_path):
+    prefix, payload, N, M = dataset(tmp_path, missing=0.0)
+    write_eigen(prefix, payload, N)
+    raw = bytearray(open(str(prefix) + ".eigen.sparsebed", "rb").read())
+    assert int(np.frombuffer(raw, np.int64, 1, 32)[0]) > 0
+    raw[40:48] = np.float64(1.5).tobytes()   # marker 0's first value
+    open(str(prefix) + ".eigen.sparsebed", "wb").write(bytes(raw))
+    r = export(brr, prefix, tmp_path / "back.bed", "--sparse-data", "eigen")
+    assert r.returncode == 1 and "marker 0" in r.stderr

@@ -10,11 +10,14 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 S2 = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
 
 
+NAMES = {0: "synth_dense.npz", 1: "synth_ragged.npz", 2: "synth_eigen.npz"}
+
+
 def load(kind):
-    return dict(np.load(GOLDEN / ("synth_dense.npz" if kind == 0 else "synth_ragged.npz")))
+    return dict(np.load(GOLDEN / NAMES[kind]))
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_oracle_reproduces_golden(kind):
     d = load(kind)
     N, bed = int(d["N"]), d["bed"]
@@ -22,7 +25,7 @@ def test_oracle_reproduces_golden(kind):
     if kind == 0:
         rc, t = O.marker_table_dense(bed, N)
     else:
-        rc, t = O.ragged_stats(bed, N)
+        rc, t = O.ragged_stats(bed, N) if kind == 1 else O.eigen_stats(bed, N)
         for name, (off, idx) in zip(("ones", "twos", "miss"), O.ragged_lists(bed, N)):
             np.testing.assert_array_equal(off, d[f"off_{name}"])
             np.testing.assert_array_equal(idx, d[f"idx_{name}"])

@@ -48,7 +48,7 @@ def assert_close(s, o, rtol=RTOL, what=""):
     np.testing.assert_allclose(s["mu"], o["mu"], rtol=rtol, atol=1e-14, err_msg=what)
 
 
-@pytest.mark.parametrize("kind", [gpu.KIND_DENSE, gpu.KIND_RAGGED])
+@pytest.mark.parametrize("kind", [gpu.KIND_DENSE, gpu.KIND_RAGGED, gpu.KIND_EIGEN])
 @pytest.mark.parametrize("N,M,miss", [(2000, 600, 0.0), (1203, 400, 0.01), (60, 50, 0.02)])
 def test_fp64_chain_matches_oracle_each_iteration(gpu_lib, kind, N, M, miss):
     bed, y = problem(N, M, seed=N + M + kind, miss=miss)
@@ -61,10 +61,13 @@ def test_fp64_chain_matches_oracle_each_iteration(gpu_lib, kind, N, M, miss):
     np.testing.assert_allclose(ch.state()["eps"], oc.state()["eps"], rtol=0, atol=1e-11)
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+GOLDEN_NAMES = {0: "synth_dense.npz", 1: "synth_ragged.npz", 2: "synth_eigen.npz"}
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_fp64_chain_matches_committed_golden_trace(gpu_lib, kind):
     """Two groups with 4 and 3 components, missing genotypes, N = 203."""
-    d = dict(np.load(GOLDEN / ("synth_dense.npz" if kind == 0 else "synth_ragged.npz")))
+    d = dict(np.load(GOLDEN / GOLDEN_NAMES[kind]))
     N = int(d["N"])
     ch = make_gpu(d["bed"], N, d["y"], S2, kind, group=d["group"], seed=int(d["seed"]))
     for it in range(d["trace_beta"].shape[0]):
@@ -90,7 +93,7 @@ def test_fp64_two_groups_different_component_counts(gpu_lib):
         assert (s["comp"][group == 1] < 3).all()
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_sweep_boundary_resynchronised_from_oracle_state(gpu_lib, kind):
     """brr_set_state + brr_sweep with the oracle's own order and draws, for
     several iterations of a running chain: one sweep at a time, re-synchronised."""
@@ -115,11 +118,11 @@ def test_sweep_boundary_resynchronised_from_oracle_state(gpu_lib, kind):
         np.testing.assert_allclose(np.array(out.v[:4]), o["v"][0, :4])
         np.testing.assert_allclose(out.betasqnG[0], o["betasqnG"][0], rtol=RTOL)
         np.testing.assert_allclose(out.eps_sqnorm, (o["eps"] ** 2).sum(), rtol=1e-12)
-        if kind == 1:
+        if kind != 0:
             np.testing.assert_allclose(s["epsSum"], o["epsSum"], rtol=1e-9, atol=1e-9)
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_speculation_width_does_not_change_results(gpu_lib, kind):
     """Markers are accepted only while the residual is unchanged, so the width
     of the speculative round changes the chain only through the rounding of
@@ -159,7 +162,7 @@ def test_tiny_problems(gpu_lib):
         g[:, 1] = 1
         bed = plink.encode_bed(g)
         y = np.linspace(-1, 1, N).astype(np.float32)
-        for kind in (0, 1):
+        for kind in (0, 1, 2):
             ch = make_gpu(bed, N, y, S1, kind, seed=1)
             oc = O.OracleChain(bed, N, y, S1, kind=kind, seed=1)
             for it in range(3):
@@ -173,7 +176,7 @@ def test_fp32c_tracks_fp64_oracle(gpu_lib):
     chain and beta within 1e-7 relative; the residual stays within 1e-9."""
     N, M = 4000, 800
     bed, y = problem(N, M, seed=23, miss=0.01)
-    for kind in (0, 1):
+    for kind in (0, 1, 2):
         ch = make_gpu(bed, N, y, S1, kind, form=gpu.FORM_FP32C, seed=6, refresh_every=2)
         oc = O.OracleChain(bed, N, y, S1, kind=kind, seed=6)
         for it in range(4):
@@ -190,7 +193,7 @@ def test_fp32c_tracks_fp64_oracle(gpu_lib):
 def test_refresh_reproduces_residual(gpu_lib):
     N, M = 1500, 300
     bed, y = problem(N, M, seed=31, miss=0.02)
-    for kind in (0, 1):
+    for kind in (0, 1, 2):
         ch = make_gpu(bed, N, y, S1, kind, seed=7)
         ch.iterate(3)
         before = ch.state()["eps"]

@@ -44,7 +44,7 @@ def run(brr, *args):
     return r.stdout
 
 
-@pytest.mark.parametrize("sparse", [None, "ragged"])
+@pytest.mark.parametrize("sparse", [None, "ragged", "eigen"])
 def test_preprocess_writes_reference_formats(brr, dataset, sparse):
     d = dataset
     args = ["--preprocess", "--bfile", str(d["prefix"]), "--pheno", str(d["dir"] / "toy.phen")]
@@ -58,6 +58,14 @@ def test_preprocess_writes_reference_formats(brr, dataset, sparse):
         np.testing.assert_array_equal(data, O.dense_columns(d["payload"], N))
         np.testing.assert_array_equal(idx[:, 0], np.arange(M) * N * 8)
         np.testing.assert_array_equal(idx[:, 1], N * 8)
+    elif sparse == "eigen":
+        import test_cli_preprocessed as P
+        got = (d["dir"] / "toy.eigen.sparsebed").read_bytes()
+        got_idx = (d["dir"] / "toy.eigen.sparsebedindex").read_bytes()
+        ref = d["dir"] / "ref"
+        P.write_eigen(ref, d["payload"], N)
+        assert got == (d["dir"] / "ref.eigen.sparsebed").read_bytes()
+        assert got_idx == (d["dir"] / "ref.eigen.sparsebedindex").read_bytes()
     else:
         raw = (d["dir"] / "toy.ragged.sparsebed").read_bytes()
         idx = np.fromfile(d["dir"] / "toy.ragged.sparsebedindex", np.uint64).reshape(M, 3)
@@ -123,9 +131,9 @@ def test_ppbayes_missing_phenotypes_are_an_error(brr, dataset):
     assert r.returncode == 1 and "phenotype" in r.stderr
 
 
-@pytest.mark.parametrize("sparse", [None, "ragged"])
+@pytest.mark.parametrize("sparse", [None, "ragged", "eigen"])
 def test_ppbayes_reads_reference_preprocessed_files(brr, dataset, sparse):
-    """With <prefix>.ppbed / .ragged.sparsebed and its index present, ppbayes
+    """With <prefix>.ppbed / .ragged.sparsebed / .eigen.sparsebed and its index present, ppbayes
     reads them as the reference does (src/analysisrunner.cpp:186-196): files
     written in the reference's layout from the oracle's builders give the
     oracle's chain."""
@@ -134,6 +142,9 @@ def test_ppbayes_reads_reference_preprocessed_files(brr, dataset, sparse):
     if sparse is None:
         P.write_dense(d["prefix"], d["payload"], d["N"])
         extra = []
+    elif sparse == "eigen":
+        P.write_eigen(d["prefix"], d["payload"], d["N"])
+        extra = ["--sparse-data", "eigen"]
     else:
         P.write_ragged(d["prefix"], d["payload"], d["N"])
         extra = ["--sparse-data", "ragged"]
@@ -144,9 +155,42 @@ def test_ppbayes_reads_reference_preprocessed_files(brr, dataset, sparse):
               "--mcmc-samples", str(out), *extra)
     assert "Start reading preprocessed bed file" in log
     M, N = d["M"], d["N"]
-    oc = O.OracleChain(d["payload"], N, d["y"], S2, kind=0 if sparse is None else 1, group=d["group"], seed=11)
+    kind = {None: 0, "ragged": 1, "eigen": 2}[sparse]
+    oc = O.OracleChain(d["payload"], N, d["y"], S2, kind=kind, group=d["group"], seed=11)
     lines = out.read_text().splitlines()
     for it, line in enumerate(lines[1:]):
+        oc.iterate(it)
+        s = oc.state()
+        v = np.array([float(t) for t in line.split(", ")])
+        np.testing.assert_allclose(v[2:2 + M], s["beta"], rtol=1e-5, atol=1e-9)
+        np.testing.assert_array_equal(v[5 + M:5 + 2 * M], s["comp"])
+
+
+def test_ppbayes_eigen_marker_with_mean_one(brr, dataset):
+    """A marker whose genotype sum is N stores its missing genotypes as 1.0,
+    like heterozygotes; the chain read from the Eigen file is the oracle's
+    chain on the original genotypes."""
+    import test_cli_preprocessed as P
+    d = dataset
+    N, M = d["N"], d["M"]
+    g = d["g"].copy()
+    row = np.zeros(N, np.int8)
+    perm = np.random.default_rng(7).permutation(N)
+    row[perm[:200]] = 2
+    row[perm[200:309]] = 1            # 2*200 + 109 = 509 = N
+    row[perm[309:319]] = -1
+    g[7] = row
+    payload = plink.encode_bed(g)
+    plink.write_plink(d["prefix"], payload, N)
+    stats = P.write_eigen(d["prefix"], payload, N)
+    assert stats[7, 0] == 1.0
+    out = d["dir"] / "samples_mean1.csv"
+    run(brr, "--analysis-type", "ppbayes", "--bfile", str(d["prefix"]), "--pheno", str(d["dir"] / "toy.phen"),
+        "--group", str(d["dir"] / "toy.group"), "--S", "0.01,0.001,0.0001;0.1,0.01",
+        "--chain-length", "4", "--burn-in", "0", "--thin", "1", "--seed", "11",
+        "--mcmc-samples", str(out), "--sparse-data", "eigen")
+    oc = O.OracleChain(payload, N, d["y"], S2, kind=2, group=d["group"], seed=11)
+    for it, line in enumerate(out.read_text().splitlines()[1:]):
         oc.iterate(it)
         s = oc.state()
         v = np.array([float(t) for t in line.split(", ")])

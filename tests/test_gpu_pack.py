@@ -26,7 +26,7 @@ def bits(a):
 
 
 @pytest.mark.parametrize("N,M,miss", SHAPES)
-@pytest.mark.parametrize("kind", [gpu.KIND_DENSE, gpu.KIND_RAGGED])
+@pytest.mark.parametrize("kind", [gpu.KIND_DENSE, gpu.KIND_RAGGED, gpu.KIND_EIGEN])
 def test_pack_bit_exact(gpu_lib, N, M, miss, kind):
     g, _ = plink.synth_genotypes(N, M, seed=N * 7 + M, missing=miss, p_lo=0.01)
     bed = plink.encode_bed(g)
@@ -37,7 +37,7 @@ def test_pack_bit_exact(gpu_lib, N, M, miss, kind):
         if kind == gpu.KIND_DENSE:
             rc, ref = O.marker_table_dense(bed, N)
         else:
-            rc, ref = O.ragged_stats(bed, N)
+            rc, ref = O.ragged_stats(bed, N) if kind == gpu.KIND_RAGGED else O.eigen_stats(bed, N)
             for (go, gi), (oo, oi) in zip(ch.ragged_lists(n), O.ragged_lists(bed, N)):
                 np.testing.assert_array_equal(go, oo)
                 np.testing.assert_array_equal(gi, oi)
@@ -45,16 +45,19 @@ def test_pack_bit_exact(gpu_lib, N, M, miss, kind):
         assert np.array_equal(bits(t), bits(ref))
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+NAMES = {0: "synth_dense.npz", 1: "synth_ragged.npz", 2: "synth_eigen.npz"}
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_pack_matches_committed_golden(gpu_lib, kind):
-    d = dict(np.load(GOLDEN / ("synth_dense.npz" if kind == 0 else "synth_ragged.npz")))
+    d = dict(np.load(GOLDEN / NAMES[kind]))
     N, M = int(d["N"]), int(d["M"])
     with gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind)) as ch:
         ch.pack_bed(d["bed"])
         t, n = ch.marker_table()
         np.testing.assert_array_equal(n, d["counts"])
         assert np.array_equal(bits(t), bits(d["table"]))
-        if kind == 1:
+        if kind != 0:
             for name, (go, gi) in zip(("ones", "twos", "miss"), ch.ragged_lists(n)):
                 np.testing.assert_array_equal(go, d[f"off_{name}"])
                 np.testing.assert_array_equal(gi, d[f"idx_{name}"])
@@ -77,7 +80,7 @@ def test_monomorphic_marker_is_an_error(gpu_lib):
     g[0, :50] = 1
     g[2, 3] = 2
     bed = plink.encode_bed(g)
-    for kind in (0, 1):
+    for kind in (0, 1, 2):
         with gpu.Chain(gpu.ChainConfig(N=100, M=3, kind=kind)) as ch:
             with pytest.raises(gpu.BrrError) as e:
                 ch.pack_bed(bed)

@@ -24,7 +24,7 @@ def _ptr(a, ct):
     return a.ctypes.data_as(C.POINTER(ct))
 
 
-@pytest.mark.parametrize("kind", [gpu.KIND_DENSE, gpu.KIND_RAGGED])
+@pytest.mark.parametrize("kind", [gpu.KIND_DENSE, gpu.KIND_RAGGED, gpu.KIND_EIGEN])
 def test_noalloc_matches_allocating_entry_point_on_two_calls(gpu_lib, kind):
     import torch
     N, M = 3001, 257
