@@ -497,18 +497,14 @@ int prepare_blocked(brr_ctx *c)
         c->blocked = false;
         return BRR_OK;
     }
-    BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
     std::string why;
+    float ms = 0.f;
     if (build_gram(c->d_codes, c->col_stride, cf.N, cf.M, c->d_scale, c->d_counts, c->has_missing, c->d_gram, c->st,
-                   why) != 0) {
+                   why, &ms) != 0) {
         cudaFree(c->d_gram);
         c->d_gram = nullptr;
         return fail(BRR_ERR_CUDA, "building the marker Gram failed: " + why);
     }
-    BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
-    BRR_CUDA(cudaEventSynchronize(c->ev[1]));
-    float ms = 0.f;
-    BRR_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
     c->gram_ms = ms;
     c->blocked = true;
     return BRR_OK;

@@ -97,7 +97,7 @@ cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, 
 }
 
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
-               const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why)
+               const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why, float *device_ms)
 {
     const int64_t npad = ((N + 7) / 8) * 8;
     const int64_t T = std::min<int64_t>(M, 8192);
@@ -121,6 +121,13 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     }
     if (rc == 0)
         cublasSetStream(h, st);
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (rc == 0) {
+        cu(cudaEventCreate(&ev[0]), "event");
+        cu(cudaEventCreate(&ev[1]), "event");
+    }
+    if (rc == 0)
+        cu(cudaEventRecord(ev[0], st), "event");
     if (rc == 0) {
         k_decode_bf16<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, 0, M, gp, nm);
         cu(cudaGetLastError(), "decode");
@@ -158,7 +165,14 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
             }
         }
     }
+    if (rc == 0)
+        cu(cudaEventRecord(ev[1], st), "event");
     cu(cudaStreamSynchronize(st), "Gram build");
+    if (rc == 0 && device_ms)
+        cu(cudaEventElapsedTime(device_ms, ev[0], ev[1]), "event");
+    for (cudaEvent_t e : ev)
+        if (e)
+            cudaEventDestroy(e);
     if (h)
         cublasDestroy(h);
     cudaFree(gp);

@@ -141,6 +141,7 @@ int sweep_block_threads();
 int sweep_block_max_ctas_per_sm(size_t smem, std::string *why = nullptr);
 cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work);
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
-               const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why);
+               const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why,
+               float *device_ms);
 
 }  // namespace brr

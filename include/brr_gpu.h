@@ -196,7 +196,8 @@ int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_
 int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arrivals);
 
 /* Whether the chain runs the Gram-blocked FP32C sweep, the device time of
- * building the packed marker Gram (ms) and its size in bytes. */
+ * building the packed marker Gram (ms: decode, GEMMs and combine, without the
+ * allocations and the library's initialisation) and its size in bytes. */
 int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes);
 
 /* Per-phase SM cycles of the sweeps of the last brr_iterate / brr_sweep call,
