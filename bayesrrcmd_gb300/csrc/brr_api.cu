@@ -49,6 +49,12 @@ cudaError_t dalloc(T **p, size_t n)
     return cudaMalloc((void **)p, n * sizeof(T));
 }
 
+}  // namespace
+
+namespace brr {
+
+int api_fail(int code, const std::string &msg) { return fail(code, msg); }
+
 // Sweep permutation: Fisher-Yates from the counter-based stream.  The
 // reference shuffles with std::random_shuffle (src/BayesRBase.cpp:198); any
 // uniform permutation is equivalent in law, this one is replayable.
@@ -64,7 +70,7 @@ void make_permutation(StreamKey key, uint32_t it, uint32_t M, uint32_t *perm)
     }
 }
 
-}  // namespace
+}  // namespace brr
 
 struct brr_ctx {
     brr_config cfg{};

@@ -94,6 +94,70 @@ struct SweepArgs {
                                  // the dot product at the marker's mean)
 };
 
+// ---------------------------------------------------------------------------
+// Batched chains on shared genotypes (brr_batch.cu).
+//
+// C chains (distinct seeds and phenotypes) sweep the markers in one shared
+// order, 32 markers per block.  Each chain's residual is held exactly in fixed
+// point, E = eps * 2^kBatchFrac (int64), and on chip as kBatchLimbs balanced
+// 11-bit limbs stored as FP16, so that the dot products X_block^T E and the
+// rank-32 residual update are FP16 tensor-core GEMMs with FP32 accumulation
+// whose every partial sum is an integer below 2^24, i.e. exact.
+constexpr int kBatchFrac = 40;
+constexpr int kBatchLimbs = 4;
+constexpr int kBatchBlock = 32;          // markers per block
+constexpr int kBatchMaxChains = 64;
+constexpr int kBatchCopies = 8;          // copies of the exchange accumulators (CTA s adds into s % 8)
+
+struct alignas(16) BatchRec {
+    double sigma;        // 1 / sd of the marker column
+    double colmean;      // column mean
+    double S;            // sum of the genotypes over all individuals (exact integer)
+    uint32_t j;          // marker id
+    int32_t group;
+};
+static_assert(sizeof(BatchRec) == 32, "BatchRec must be 32 bytes");
+
+struct BatchArgs {
+    int64_t N, M;
+    int G;                           // CTAs: slices of individuals
+    int C;                           // chains (32 or 64)
+    int kext;                        // individuals per slice, padded to a multiple of 16
+    int n_groups;
+    const int32_t *slice_lo;         // G+1 slice boundaries
+    const uint8_t *codes;            // M x col_stride 2-bit codes
+    int64_t col_stride;
+    const BatchRec *rec;             // M records in sweep order
+    const double *gconst;            // [C][n_groups][kMaxK][4] sampler constants per chain
+    const int32_t *gK;               // [n_groups] mixture sizes
+    const double *u, *z;             // [C][M] draws
+    double *beta, *acum;             // [C][M]
+    int32_t *comp;                   // [C][M]
+    uint8_t *chosen;                 // [C][M] the sampler chose a component in this sweep
+    long long *E;                    // [C][N] fixed-point residual (in at sweep start, out at the end)
+    const long long *dmu;            // [C] fixed-point shift added to E at the start (updateMu)
+    long long *sumE;                 // [C] exact residual total, carried through the sweep
+    unsigned long long *acc;         // [kBatchCopies][C][32] dot-product accumulators (zero at launch)
+    unsigned *pacc;                  // [2][kBatchCopies][32][32] integer block Gram accumulators (zero at launch)
+    long long *wx;                   // [C][33] per block: W per marker, then the constant
+    unsigned long long *counter;     // 2 barrier counters, 32 words apart (zero at launch)
+    double *part;                    // [G][C][2] per slice: sum(E) (bits of an int64) and sum(eps^2)
+    int *err;
+    uint64_t timeout_ns;
+    long long *prof;                 // optional [8] cycle counters of CTA 0
+};
+
+// Sets the string brr_last_error() returns and passes the status code through.
+int api_fail(int code, const std::string &msg);
+
+cudaError_t launch_batch_gather(const uint32_t *order, int64_t M, const double *scale, const int64_t *counts,
+                                const int32_t *group, BatchRec *rec, cudaStream_t st);
+cudaError_t launch_batch_stats(int64_t M, int C, const int32_t *group, const int32_t *comp, const uint8_t *chosen,
+                               const double *beta, int n_groups, unsigned long long *out, cudaStream_t st);
+size_t batch_smem_bytes(int C, int kext);
+int batch_max_ctas_per_sm(int C, int kext, size_t smem);
+cudaError_t launch_sweep_batch(const BatchArgs &a, int kmax, cudaStream_t st);
+
 // Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).
 cudaError_t launch_pack_counts(const uint8_t *bed, int64_t N, int64_t M, uint8_t *codes,
                                int64_t col_stride, int64_t *counts, cudaStream_t st);

@@ -132,4 +132,7 @@ BRR_HD bool inv_scaled_chisq(StreamKey k, uint32_t it, uint32_t purpose, uint32_
     return true;
 }
 
+// Fisher-Yates permutation of 0..M-1 for iteration it (host; defined in brr_api.cu).
+void make_permutation(StreamKey key, uint32_t it, uint32_t M, uint32_t *perm);
+
 }  // namespace brr

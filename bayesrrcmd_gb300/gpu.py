@@ -63,6 +63,9 @@ EXPORTS = [
     "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing", "brr_get_phase_cycles",
     "brr_set_wait_limit", "brr_xbeta", "brr_synth_bed_device", "brr_xbeta_noalloc",
     "brr_get_gram_info",
+    "brr_batch_create", "brr_batch_destroy", "brr_batch_pack_bed", "brr_batch_pack_bed_device",
+    "brr_batch_set_groups", "brr_batch_set_phenotypes", "brr_batch_init", "brr_batch_iterate",
+    "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_get_geometry",
 ]
 
 
@@ -100,6 +103,18 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
     lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
+    lib.brr_batch_create.argtypes = [C.POINTER(BrrConfig), C.c_int32, C.POINTER(P)]
+    lib.brr_batch_destroy.argtypes = [P]
+    lib.brr_batch_pack_bed.argtypes = [P, C.POINTER(C.c_uint8), C.c_int64]
+    lib.brr_batch_pack_bed_device.argtypes = [P, P, C.c_int64]
+    lib.brr_batch_set_groups.argtypes = [P, C.POINTER(C.c_int32)]
+    lib.brr_batch_set_phenotypes.argtypes = [P, C.POINTER(C.c_float)]
+    lib.brr_batch_init.argtypes = [P]
+    lib.brr_batch_iterate.argtypes = [P, C.c_int32]
+    lib.brr_batch_get_chain_state.argtypes = [P, C.c_int32, C.POINTER(BrrState)]
+    lib.brr_batch_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.brr_batch_set_wait_limit.argtypes = [P, C.c_uint64]
+    lib.brr_batch_get_geometry.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
     for name in EXPORTS:
         if name != "brr_last_error":
             getattr(lib, name).restype = C.c_int
@@ -304,3 +319,91 @@ class Chain:
         sw, tot, r = C.c_double(), C.c_double(), C.c_int64()
         self._check(self.lib.brr_get_timing(self.h, C.byref(sw), C.byref(tot), C.byref(r)))
         return sw.value, tot.value, r.value
+
+
+class Batch:
+    """C = 32 or 64 chains (distinct seeds cfg.chain .. cfg.chain+C-1, one
+    phenotype each) on shared dense genotypes, swept together with the
+    tensor-core batched form behind the C ABI."""
+
+    def __init__(self, cfg: ChainConfig, chains: int, lib: Optional[C.CDLL] = None):
+        self.cfg = cfg
+        self.C = int(chains)
+        self.lib = lib or load_library()
+        self._c = cfg.to_c()
+        h = C.c_void_p()
+        self._check(self.lib.brr_batch_create(C.byref(self._c), self.C, C.byref(h)))
+        self.h = h
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise BrrError(rc, self.lib.brr_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.brr_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def pack_bed(self, bed_payload: np.ndarray):
+        a = np.ascontiguousarray(bed_payload, dtype=np.uint8)
+        self._check(self.lib.brr_batch_pack_bed(self.h, _ptr(a, C.c_uint8), a.size))
+
+    def pack_bed_device(self, dev_ptr: int, nbytes: int):
+        self._check(self.lib.brr_batch_pack_bed_device(self.h, C.c_void_p(dev_ptr), nbytes))
+
+    def set_groups(self, group: np.ndarray):
+        g = np.ascontiguousarray(group, dtype=np.int32)
+        self._check(self.lib.brr_batch_set_groups(self.h, _ptr(g, C.c_int32)))
+
+    def set_phenotypes(self, y: np.ndarray):
+        a = np.ascontiguousarray(y, dtype=np.float32)
+        if a.shape != (self.C, self.cfg.N):
+            raise ValueError(f"phenotypes must be {self.C} x {self.cfg.N}")
+        self._check(self.lib.brr_batch_set_phenotypes(self.h, _ptr(a, C.c_float)))
+
+    def init(self):
+        self._check(self.lib.brr_batch_init(self.h))
+
+    def iterate(self, n: int = 1):
+        self._check(self.lib.brr_batch_iterate(self.h, int(n)))
+
+    def state(self, chain: int) -> dict:
+        M, N = self.cfg.M, self.cfg.N
+        beta = np.zeros(M, np.float64)
+        comp = np.zeros(M, np.int32)
+        acum = np.zeros(M, np.float64)
+        eps = np.zeros(N, np.float64)
+        st = BrrState()
+        st.beta, st.comp, st.acum, st.eps = (_ptr(beta, C.c_double), _ptr(comp, C.c_int32),
+                                             _ptr(acum, C.c_double), _ptr(eps, C.c_double))
+        self._check(self.lib.brr_batch_get_chain_state(self.h, int(chain), C.byref(st)))
+        G = len(self.cfg.S)
+        return dict(beta=beta, comp=comp, acum=acum, eps=eps, mu=st.mu, sigmaE=st.sigmaE, epsSum=st.epsSum,
+                    sigmaG=np.array(st.sigmaG[:G]),
+                    pi=np.array(st.pi[:]).reshape(MAX_GROUPS, MAX_K)[:G].copy(), iteration=st.iteration)
+
+    def timing(self):
+        sw, tot = C.c_double(), C.c_double()
+        cyc = np.zeros(4, np.int64)
+        self._check(self.lib.brr_batch_get_timing(self.h, C.byref(sw), C.byref(tot), _ptr(cyc, C.c_int64)))
+        return sw.value, tot.value, cyc
+
+    def set_wait_limit(self, timeout_ns: int):
+        self._check(self.lib.brr_batch_set_wait_limit(self.h, int(timeout_ns)))
+
+    def geometry(self):
+        g, sl, sm = C.c_int32(), C.c_int32(), C.c_int64()
+        self._check(self.lib.brr_batch_get_geometry(self.h, C.byref(g), C.byref(sl), C.byref(sm)))
+        return dict(ctas=g.value, slice=sl.value, smem=sm.value)

@@ -200,6 +200,35 @@ int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arriva
  * allocations and the library's initialisation) and its size in bytes. */
 int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes);
 
+/* ---- Batched chains on shared genotypes (the C4 batching form) -------------
+ * C = 32 or 64 chains with distinct seeds (chain ids cfg.chain .. cfg.chain+C-1)
+ * and one phenotype each sweep the same dense markers in one shared order per
+ * iteration (the permutation of chain cfg.chain's stream); per chain the
+ * iteration is BayesRBase::runGibbs's loop body (src/BayesRBase.cpp:186-247).
+ * The dot products X_block^T E and the residual updates run on the tensor
+ * cores with each residual held exactly as fixed point eps * 2^40 (|eps| < 8);
+ * markers with missing genotypes are rejected.  Sizes: N up to about
+ * 152 x 336 individuals for 64 chains, 152 x 660 for 32. */
+typedef struct brr_batch brr_batch;
+int brr_batch_create(const brr_config *cfg, int32_t chains, brr_batch **out);
+int brr_batch_destroy(brr_batch *b);
+int brr_batch_pack_bed(brr_batch *b, const uint8_t *bed, int64_t nbytes);
+int brr_batch_pack_bed_device(brr_batch *b, const uint8_t *d_bed, int64_t nbytes);
+int brr_batch_set_groups(brr_batch *b, const int32_t *group);
+/* chains x N phenotype values, chain-major */
+int brr_batch_set_phenotypes(brr_batch *b, const float *y);
+int brr_batch_init(brr_batch *b);
+int brr_batch_iterate(brr_batch *b, int32_t n_iter);
+/* One chain's state; eps is the exact fixed-point residual as doubles. */
+int brr_batch_get_chain_state(brr_batch *b, int32_t chain, brr_state *st);
+/* Device time of the sweeps and of the whole last brr_batch_iterate call (ms);
+ * cycles (optional, 4 values): CTA 0's cycles in the dot, publish, resolve and
+ * update phases, summed over the sweeps of that call. */
+int brr_batch_get_timing(brr_batch *b, double *sweep_ms, double *total_ms, int64_t *cycles);
+int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns);
+/* CTAs of the sweep, individuals per slice and shared memory per CTA. */
+int brr_batch_get_geometry(brr_batch *b, int32_t *ctas, int32_t *slice, int64_t *smem_bytes);
+
 /* Per-phase SM cycles of the sweeps of the last brr_iterate / brr_sweep call,
  * measured on the first CTA (the counterpart of the reference's per-column
  * timing log, src/BayesRBase.cpp:381-389), 16 values.  Restart sweep: [0] ring

@@ -650,7 +650,7 @@ int or_iterate(const or_problem *p, const or_markers *mk, or_state *s, uint32_t 
     }
     for (int64_t j = 0; j < M; ++j)
         or_marker_draws(p->seed, p->chain, it, (uint32_t)j, &u[j], &z[j]);
-    or_permutation(p->seed, p->chain, it, (uint32_t)M, order);
+    or_permutation(p->seed, p->shared_perm ? p->perm_chain : p->chain, it, (uint32_t)M, order);
     s->m0 = 0.0;
     memset(s->v, 0, sizeof s->v);
     memset(s->betasqnG, 0, sizeof s->betasqnG);

@@ -97,6 +97,10 @@ typedef struct {
     const uint8_t *bed;          /* M x ceil(N/4) SNP-major BED payload */
     uint32_t seed, chain;
     double v0E, s02E, v0G, s02G;
+    /* batched chains: when shared_perm != 0 the sweep order of every
+     * iteration is the permutation of chain perm_chain's stream */
+    int32_t shared_perm;
+    uint32_t perm_chain;
 } or_problem;
 
 typedef struct {

@@ -22,6 +22,7 @@ class OrProblem(C.Structure):
         ("group", C.POINTER(C.c_int32)), ("K", C.POINTER(C.c_int32)), ("S", C.POINTER(C.c_double)),
         ("y", C.POINTER(C.c_float)), ("bed", C.POINTER(C.c_uint8)), ("seed", C.c_uint32), ("chain", C.c_uint32),
         ("v0E", C.c_double), ("s02E", C.c_double), ("v0G", C.c_double), ("s02G", C.c_double),
+        ("shared_perm", C.c_int32), ("perm_chain", C.c_uint32),
     ]
 
 
@@ -157,7 +158,8 @@ def gamma(seed, chain, it, purpose, sub, shape):
 class OracleChain:
     """Oracle chain over the same inputs as the GPU Chain."""
 
-    def __init__(self, bed, N, y, S, kind=0, group=None, seed=1, chain=0, priors=(1e-4, 1e-4, 1e-4, 1e-4)):
+    def __init__(self, bed, N, y, S, kind=0, group=None, seed=1, chain=0, priors=(1e-4, 1e-4, 1e-4, 1e-4),
+                 perm_chain=None):
         self.bed = np.ascontiguousarray(bed, np.uint8)
         self.N, self.M = N, bed.shape[0]
         self.y = np.ascontiguousarray(y, np.float32)
@@ -174,6 +176,8 @@ class OracleChain:
         pr.y, pr.bed = p(self.y, C.c_float), p(self.bed, C.c_uint8)
         pr.seed, pr.chain = seed, chain
         pr.v0E, pr.s02E, pr.v0G, pr.s02G = priors
+        if perm_chain is not None:
+            pr.shared_perm, pr.perm_chain = 1, perm_chain
         self.pr = pr
         h = C.c_void_p()
         rc = lib().or_markers_create(C.byref(pr), C.byref(h))

@@ -69,3 +69,26 @@ def test_invalid_config_rejected():
     assert lib.brr_ctx_create(C.byref(bad), C.byref(h)) == -1
     bad = gpu.ChainConfig(N=10, M=5, spec_width=12).to_c()
     assert lib.brr_ctx_create(C.byref(bad), C.byref(h)) == -1
+
+
+def test_batch_config_rejected_before_the_device():
+    """The batched form checks its arguments before it looks for a GPU."""
+    lib = gpu.load_library()
+    h = C.c_void_p()
+    cfg = gpu.ChainConfig(N=100, M=5).to_c()
+    assert lib.brr_batch_create(C.byref(cfg), 48, C.byref(h)) == -1          # 32 or 64 chains
+    assert b"32 or 64" in lib.brr_last_error()
+    rag = gpu.ChainConfig(N=100, M=5, kind=gpu.KIND_RAGGED).to_c()
+    assert lib.brr_batch_create(C.byref(rag), 64, C.byref(h)) == -1          # dense markers only
+    bad = gpu.ChainConfig(N=100, M=5, S=[[0.1, 0.0]]).to_c()
+    assert lib.brr_batch_create(C.byref(bad), 64, C.byref(h)) == -1
+
+
+def test_batch_without_gpu_is_a_device_error():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = gpu.load_library()
+    h = C.c_void_p()
+    cfg = gpu.ChainConfig(N=100, M=5).to_c()
+    assert lib.brr_batch_create(C.byref(cfg), 64, C.byref(h)) == -8
