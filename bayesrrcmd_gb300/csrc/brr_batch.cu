@@ -23,7 +23,10 @@
 //      integers, into global accumulators; grid barrier 1;
 //   2. one warp per chain resolves the 32 markers in order: lane t samples
 //      marker t from num_t = sigma_t (dot_t - colmean_t * sum(E)) 2^-40 +
-//      beta_old (N-1) in FP64; when marker p changes, the later markers' dots
+//      beta_old (N-1) (FP64; the component is decided in FP32 with a
+//      rigorous error bound and in FP64 whenever the bound cannot certify it,
+//      so the decisions are the FP64 ones; acum is kept to FP32 precision);
+//      when marker p changes, the later markers' dots
 //      move by W_p P[p][t] - C_p S_t exactly (W_p = round(dBeta sigma_p 2^40),
 //      C_p = round(dBeta sigma_p colmean_p 2^40)); grid barrier 2;
 //   3. every CTA applies E_i += sum_p W_p g_p[i] - sum_p C_p through D2 and
@@ -34,6 +37,7 @@
 #include "brr_internal.h"
 #include "brr_device.cuh"
 #include "brr_pick.cuh"
+#include "brr_stream.h"
 
 namespace brr {
 namespace {
@@ -170,6 +174,17 @@ __device__ __forceinline__ long long join4(const int (&d)[kBatchLimbs])
     return x;
 }
 
+// floor(v / 2048 + 1/2) of an integer-valued float |v| < 2^21 (the carry that
+// brings a limb into [-1024, 1023]): y = v / 2048 + 1/2 has a fraction that is
+// a multiple of 2^-11, so floor(y) is the nearest integer to y - 1/2 + 2^-12 =
+// v / 2048 + 2^-12, formed exactly by one FMA and rounded by adding and
+// removing 1.5 * 2^23.
+__device__ __forceinline__ float limb_carry(float v)
+{
+    const float q = __fmaf_rn(v, 1.f / 2048.f, 1.f / 4096.f);
+    return __fsub_rn(__fadd_rn(q, 12582912.f), 12582912.f);
+}
+
 __device__ __forceinline__ unsigned short h_bits(int v) { return __half_as_ushort(__int2half_rn(v)); }
 __device__ __forceinline__ int h_int(unsigned short b) { return __half2int_rn(__ushort_as_half(b)); }
 
@@ -181,14 +196,18 @@ __device__ __forceinline__ unsigned short g_half(unsigned code)
 }
 
 struct BatchPlan {
-    unsigned off_g, off_e, off_w, off_codes, total;
+    unsigned off_g, off_e, off_w, off_codes, off_p, total;
+    int nres;            // resolver warps per CTA (chains per CTA, at most 8)
     unsigned sbo_g;      // stride between 8-marker groups of g (= kext/8 * 128)
     unsigned lbo_e;      // stride between 8-individual groups of E (= R/8 * 128)
 };
 
-__host__ __device__ inline BatchPlan batch_plan(int C, int kext)
+__host__ __device__ inline BatchPlan batch_plan(int C, int kext, int G)
 {
     BatchPlan p;
+    p.nres = (C + G - 1) / G;
+    if (p.nres > kBW)
+        p.nres = kBW;
     const unsigned R = 4u * (unsigned)C;
     p.sbo_g = (unsigned)(kext / 8) * 128u;
     p.lbo_e = (R / 8u) * 128u;
@@ -196,7 +215,8 @@ __host__ __device__ inline BatchPlan batch_plan(int C, int kext)
     p.off_e = p.off_g + 32u * (unsigned)kext * 2u;
     p.off_w = p.off_e + R * (unsigned)kext * 2u;
     p.off_codes = p.off_w + R * 32u * 2u;
-    p.total = p.off_codes + 32u * (unsigned)(kext / 4);
+    p.off_p = p.off_codes + 32u * (unsigned)(kext / 4);
+    p.total = p.off_p + (unsigned)p.nres * kBatchBlock * 33u * 4u;
     p.total = (p.total + 1023u) & ~1023u;
     // every CTA allocates all 512 TMEM columns and waits at grid barriers, so
     // no two CTAs may share an SM: at least half the SM's shared memory each
@@ -213,7 +233,7 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
     __shared__ unsigned s_tmem;
     __shared__ int s_abort;
     __shared__ uint32_t s_j[kBatchBlock];
-    __shared__ int s_cl[kBatchMaxChains][kBatchLimbs];
+    __shared__ float s_cl[kBatchMaxChains][kBatchLimbs];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int s = blockIdx.x;
@@ -221,11 +241,12 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
     const int kext = a.kext;
     const int lo = a.slice_lo[s];
     const int ns = a.slice_lo[s + 1] - lo;
-    const BatchPlan pl = batch_plan(C, kext);
+    const BatchPlan pl = batch_plan(C, kext, a.G);
     uint8_t *g_t = smem + pl.off_g;
     uint8_t *e_t = smem + pl.off_e;
     uint8_t *w_t = smem + pl.off_w;
     uint8_t *s_codes = smem + pl.off_codes;
+    int *s_pbuf = reinterpret_cast<int *>(smem + pl.off_p);
     const int nblocks = (int)((a.M + kBatchBlock - 1) / kBatchBlock);
     const int KS = kext / 16;                       // K steps of the dot GEMM
     const int NT = (kext + 127) / 128;              // individual tiles of the update GEMM
@@ -233,7 +254,7 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
     const double inv2f = 1.0 / (double)(1ll << kBatchFrac);
     unsigned long long *cnt1 = a.counter, *cnt2 = a.counter + kCounterGap;
     long long *prof = (a.prof && s == 0) ? a.prof : nullptr;
-    long long ph[6] = {0, 0, 0, 0, 0, 0};
+    long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
     if (tid == 0) {
         s_abort = 0;
@@ -367,7 +388,7 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
         if (warp == 0) {
             float f[32];
             tmem_ld32(tmem + 64u, f);
-            unsigned *pacc = a.pacc + ((size_t)(b & 1) * kBatchCopies + (s % kBatchCopies)) * (kBatchBlock * kBatchBlock) +
+            unsigned *pacc = a.pacc + ((size_t)(b & 1) * kBatchPCopies + (s % kBatchPCopies)) * (kBatchBlock * kBatchBlock) +
                              lane * kBatchBlock;
             for (int t = 0; t < lane; ++t)
                 atomicAdd(pacc + t, (unsigned)(int)f[t]);
@@ -387,18 +408,19 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
             const int64_t q = (int64_t)b * kBatchBlock + lane;
             bool done = q >= a.M;
             BatchRec rc{};
-            double bold = 0.0, u = 1.0, z = 0.0;
+            ChainRec cr{0.0, 1.0, 0.0, 0.0};
             if (!done) {
                 rc = a.rec[q];
-                const size_t cj = (size_t)c * a.M + rc.j;
-                bold = a.beta[cj];
-                u = a.u[cj];
-                z = a.z[cj];
+                cr = a.crec[(size_t)c * a.M + q];
             }
+            const double bold = cr.beta_old, u = cr.u, z = cr.z;
+            const float uf = __double2float_rn(u);
             const int grp = done ? 0 : rc.group;
             const double *gc = a.gconst + ((size_t)c * a.n_groups + grp) * kMaxK * 4;
+            const float *gcf = a.gcf + ((size_t)c * a.n_groups + grp) * kMaxK * 2;
             const int K = a.gK[grp];
             bool ok = true;
+            const long long tw = prof ? clock64() : 0;
             if (lane == 0)
                 ok = counter_wait(cnt1, (unsigned long long)a.G * (unsigned long long)(b + 1), a.err, a.timeout_ns);
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
@@ -410,6 +432,10 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                 }
                 break;
             }
+            const long long tl = prof ? clock64() : 0;
+            if (prof && k == 0)
+                ph[4] += tl - tw;
+            int steps = 0;
             long long dot = 0;
 #pragma unroll
             for (int cp = 0; cp < kBatchCopies; ++cp) {
@@ -417,47 +443,126 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                 dot += (long long)ld_relaxed_u64(p);
                 *p = 0ull;
             }
+            // the block's integer Gram (lower triangle) into this warp's rows:
+            // row t holds P[t][p] for p < t, 33 words apart
+            int *sP = s_pbuf + (warp % pl.nres) * (kBatchBlock * 33);
+            {
+                const unsigned *pk_base = a.pacc + (size_t)(b & 1) * kBatchPCopies * (kBatchBlock * kBatchBlock);
+#pragma unroll 8
+                for (int e = lane; e < kBatchBlock * kBatchBlock; e += 32) {
+                    const int t = e >> 5, pp = e & 31;
+                    if (pp < t) {
+                        unsigned v = 0;
+#pragma unroll
+                        for (int cp = 0; cp < kBatchPCopies; ++cp)
+                            v += __ldcg(pk_base + (size_t)cp * (kBatchBlock * kBatchBlock) + e);
+                        sP[t * 33 + pp] = (int)v;
+                    }
+                }
+            }
+            __syncwarp();
             long long sumE = a.sumE[c];
-            const long long Sq = (long long)rc.S;
+            // num_t from the exact integer dot and residual total, once per
+            // block in FP64; then carried as a double-float pair through the
+            // block's changes: after marker p changes, num_t moves by
+            // dBeta_p x_p.x_t = dBeta_p sigma_p sigma_t (P[p][t] - colmean_t S_p)
+            const double num0 = fma(rc.sigma * inv2f, (double)dot,
+                                    fma(-rc.sigma * rc.colmean * inv2f, (double)sumE, bold * ((double)a.N - 1.0)));
+            float nh, nl, sh, sl, mh, ml, zh, zl, boh, bol;
+            df_from_double(num0, nh, nl);
+            df_from_double(rc.sigma, sh, sl);
+            df_from_double(rc.colmean, mh, ml);
+            df_from_double(z, zh, zl);
+            df_from_double(bold, boh, bol);
+            const float Sf = (float)rc.S;
+            const float4 *gdf = a.gdf + ((size_t)c * a.n_groups + grp) * kMaxK;
+            float bnh = boh, bnl = bol, acum_f = 0.f;
+            double acum_d = 0.0;
+            bool acum_is_d = false;
+            int fcomp = -1;
             long long Wl = 0, Csum = 0;
-            const unsigned *pk_base = a.pacc + (size_t)(b & 1) * kBatchCopies * (kBatchBlock * kBatchBlock);
-            for (;;) {
-                const double num = rc.sigma * ((double)dot - rc.colmean * (double)sumE) * inv2f +
-                                   bold * ((double)a.N - 1.0);
-                const Pick pk = pick_marker<false, KM>(num, u, z, bold, gc, K);
-                const bool chg = !done && (bold != 0.0 || pk.beta != 0.0);
+            const float two40 = (float)(1ll << kBatchFrac);
+            for (;; ++steps) {
+                int comp = -1;
+                float a032 = 0.f;
+                const bool cert = pick_f32<KM>(nh, nl, uf, gcf, K, comp, a032);
+                double fb_beta = bold, fb_acum = 0.0;
+                if (!cert) {
+                    const Pick pk = pick_marker<false, KM>((double)nh + (double)nl, u, z, bold, gc, K);
+                    comp = pk.comp;
+                    fb_acum = pk.acum0;
+                    fb_beta = pk.beta;
+                }
+                const bool chg = !done && (bold != 0.0 || comp > 0);
                 const unsigned mask = __ballot_sync(0xffffffffu, chg);
                 const int p = mask ? __ffs(mask) - 1 : 32;
                 if (!done && lane <= p) {
-                    const size_t cj = (size_t)c * a.M + rc.j;
-                    a.beta[cj] = pk.beta;
-                    a.acum[cj] = pk.acum0;
-                    a.chosen[cj] = pk.comp >= 0 ? 1 : 0;
-                    if (pk.comp >= 0)
-                        a.comp[cj] = pk.comp;
+                    // the decision of marker t is final (src/BayesRBase.cpp:346-366)
+                    fcomp = comp;
+                    if (comp == 0) {
+                        bnh = bnl = 0.f;
+                    } else if (comp > 0) {
+                        if (cert) {
+                            const float4 k4 = gdf[comp];   // {sdk hi, lo, invden hi, lo}
+                            float ah, al, bh, bl;
+                            df_mul(zh, zl, k4.x, k4.y, ah, al);
+                            df_mul(nh, nl, k4.z, k4.w, bh, bl);
+                            df_add(ah, al, bh, bl);
+                            bnh = ah;
+                            bnl = al;
+                        } else {
+                            df_from_double(fb_beta, bnh, bnl);
+                        }
+                    }
+                    acum_is_d = !cert;
+                    acum_f = a032;
+                    acum_d = fb_acum;
                     done = true;
                 }
                 if (!mask)
                     break;
+                // marker p's update: dBeta sigma_p (double-float) and the exact
+                // fixed-point coefficients W_p = round(dBeta sigma_p 2^40),
+                // C_p = round(dBeta sigma_p colmean_p 2^40)
+                float uh = 0.f, ul = 0.f;
                 long long Wp = 0, Cp = 0;
                 if (lane == p) {
-                    const double db = bold - pk.beta;
-                    Wp = llrint(db * rc.sigma * (double)(1ll << kBatchFrac));
-                    Cp = llrint(db * rc.sigma * rc.colmean * (double)(1ll << kBatchFrac));
+                    float dh = boh, dl = bol;
+                    df_add(dh, dl, -bnh, -bnl);
+                    df_mul(dh, dl, sh, sl, uh, ul);
+                    float ch, cl;
+                    df_mul(uh, ul, mh, ml, ch, cl);
+                    Wp = __float2ll_rn(__fmul_rn(uh, two40)) + __float2ll_rn(__fmul_rn(ul, two40));
+                    Cp = __float2ll_rn(__fmul_rn(ch, two40)) + __float2ll_rn(__fmul_rn(cl, two40));
                     Wl = Wp;
                 }
+                uh = __shfl_sync(0xffffffffu, uh, p);
+                ul = __shfl_sync(0xffffffffu, ul, p);
+                const float Sp = __shfl_sync(0xffffffffu, Sf, p);
                 Wp = __shfl_sync(0xffffffffu, Wp, p);
                 Cp = __shfl_sync(0xffffffffu, Cp, p);
-                const long long Sp = __shfl_sync(0xffffffffu, Sq, p);
                 Csum += Cp;
                 if (lane > p) {
-                    long long P = 0;
-#pragma unroll
-                    for (int cp = 0; cp < kBatchCopies; ++cp)
-                        P += (long long)__ldcg(pk_base + (size_t)cp * (kBatchBlock * kBatchBlock) + lane * kBatchBlock + p);
-                    dot += Wp * P - Cp * Sq;
+                    const float P = (float)sP[lane * 33 + p];
+                    // r = P - colmean_t S_p, G = sigma_t r, num += (dBeta sigma_p) G
+                    const float qh = __fmul_rn(mh, Sp);
+                    const float ql = __fmaf_rn(ml, Sp, __fmaf_rn(mh, Sp, -qh));
+                    float rh = P, rl = 0.f;
+                    df_add(rh, rl, -qh, -ql);
+                    float gh, gl, xh, xl;
+                    df_mul(sh, sl, rh, rl, gh, gl);
+                    df_mul(uh, ul, gh, gl, xh, xl);
+                    df_add(nh, nl, xh, xl);
                 }
-                sumE += Wp * Sp - (long long)a.N * Cp;
+                sumE += Wp * (long long)Sp - (long long)a.N * Cp;
+            }
+            if (q < a.M) {
+                const size_t cj = (size_t)c * a.M + rc.j;
+                a.beta[cj] = fcomp == 0 ? 0.0 : (fcomp > 0 ? (double)bnh + (double)bnl : bold);
+                a.acum[cj] = acum_is_d ? acum_d : (double)acum_f;
+                a.chosen[cj] = fcomp >= 0 ? 1 : 0;
+                if (fcomp >= 0)
+                    a.comp[cj] = fcomp;
             }
             a.wx[(size_t)c * (kBatchBlock + 1) + lane] = Wl;
             if (lane == 0) {
@@ -467,15 +572,22 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
             __syncwarp();
             if (lane == 0)
                 red_release_add_u64(cnt2, 1ull);
+            if (prof && k == 0) {
+                ph[5] += clock64() - tl;
+                ph[6] += steps + 1;
+            }
         }
+        const long long t2 = prof ? clock64() : 0;
         if (tid == 0 && !s_abort &&
             !counter_wait(cnt2, (unsigned long long)C * (unsigned long long)(b + 1), a.err, a.timeout_ns)) {
             atomicCAS(a.err, kDevOk, kDevTimeout);
             s_abort = 1;
         }
         __syncthreads();
-        if (prof)
+        if (prof) {
+            ph[7] += clock64() - t2;
             ph[2] += clock64() - t0, t0 = clock64();
+        }
         if (s_abort)
             break;
 
@@ -498,12 +610,12 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                 atomicCAS(a.err, kDevOk, kDevRange);
 #pragma unroll
             for (int l = 0; l < kBatchLimbs; ++l)
-                s_cl[c][l] = d[l];
+                s_cl[c][l] = (float)d[l];
         }
         // the block Gram accumulators of this block are read by now: clear them for block b+2
         if (s == 0)
-            for (int e = tid; e < kBatchCopies * kBatchBlock * kBatchBlock; e += kBT)
-                a.pacc[(size_t)(b & 1) * kBatchCopies * (kBatchBlock * kBatchBlock) + e] = 0u;
+            for (int e = tid; e < kBatchPCopies * kBatchBlock * kBatchBlock; e += kBT)
+                a.pacc[(size_t)(b & 1) * kBatchPCopies * (kBatchBlock * kBatchBlock) + e] = 0u;
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -535,32 +647,36 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                     float f[32];
                     tmem_ld32(tmem + ((unsigned)(q4 * 32) << 16) + (unsigned)(it * R + ck * 32), f);
                     if (i < ns) {
+                        // limbs + update - constant, renormalised with carries, all in
+                        // FP32 on exact integers (|values| < 2^17)
 #pragma unroll
                         for (int cc = 0; cc < 8; cc += 2) {
                             const int c = ck * 8 + cc;     // chains c, c+1: rows 4c .. 4c+7
                             uint4 *ep = reinterpret_cast<uint4 *>(e_t + (i >> 3) * pl.lbo_e + (c >> 1) * 128 + (i & 7) * 16);
-                            const uint4 old = *ep;
-                            const uint32_t ow[4] = {old.x, old.y, old.z, old.w};
-                            uint32_t nw[4];
+                            uint4 w4 = *ep;
+                            uint32_t *w = reinterpret_cast<uint32_t *>(&w4);
 #pragma unroll
                             for (int h = 0; h < 2; ++h) {
-                                int carry = 0, v[kBatchLimbs];
-#pragma unroll
-                                for (int l = 0; l < kBatchLimbs; ++l) {
-                                    const uint32_t word = ow[2 * h + (l >> 1)];
-                                    const int e = h_int((unsigned short)((l & 1) ? (word >> 16) : (word & 0xFFFFu)));
-                                    int x = e + (int)f[(cc + h) * 4 + l] - s_cl[c + h][l] + carry;
-                                    if (l < kBatchLimbs - 1) {
-                                        carry = (x + (int)kLimbHalf) >> 11;
-                                        x -= carry * 2048;
-                                    }
-                                    v[l] = x;
-                                }
-                                ok = ok && v[kBatchLimbs - 1] >= -(int)kLimbHalf && v[kBatchLimbs - 1] < (int)kLimbHalf;
-                                nw[2 * h] = (uint32_t)h_bits(v[0]) | ((uint32_t)h_bits(v[1]) << 16);
-                                nw[2 * h + 1] = (uint32_t)h_bits(v[2]) | ((uint32_t)h_bits(v[3]) << 16);
+                                const float2 e01 = __half22float2(*reinterpret_cast<const __half2 *>(&w[2 * h]));
+                                const float2 e23 = __half22float2(*reinterpret_cast<const __half2 *>(&w[2 * h + 1]));
+                                const float *cl = s_cl[c + h];
+                                const float *d = &f[(cc + h) * 4];
+                                float v0 = __fsub_rn(__fadd_rn(e01.x, d[0]), cl[0]);
+                                const float k0 = limb_carry(v0);
+                                v0 = __fmaf_rn(-2048.f, k0, v0);
+                                float v1 = __fadd_rn(__fsub_rn(__fadd_rn(e01.y, d[1]), cl[1]), k0);
+                                const float k1 = limb_carry(v1);
+                                v1 = __fmaf_rn(-2048.f, k1, v1);
+                                float v2 = __fadd_rn(__fsub_rn(__fadd_rn(e23.x, d[2]), cl[2]), k1);
+                                const float k2 = limb_carry(v2);
+                                v2 = __fmaf_rn(-2048.f, k2, v2);
+                                const float v3 = __fadd_rn(__fsub_rn(__fadd_rn(e23.y, d[3]), cl[3]), k2);
+                                ok = ok && v3 >= -1024.f && v3 < 1024.f;
+                                const __half2 n01 = __floats2half2_rn(v0, v1), n23 = __floats2half2_rn(v2, v3);
+                                w[2 * h] = *reinterpret_cast<const uint32_t *>(&n01);
+                                w[2 * h + 1] = *reinterpret_cast<const uint32_t *>(&n23);
                             }
-                            *ep = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+                            *ep = w4;
                         }
                     }
                 }
@@ -632,13 +748,27 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
         __syncthreads();
     }
     if (prof && tid == 0)
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 8; ++k)
             prof[k] = ph[k];
 
     tc_fence_before();
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+__global__ void k_batch_draws(uint32_t seed, uint32_t chain0, uint32_t it, int64_t M,
+                              const uint32_t *__restrict__ order, const double *__restrict__ beta,
+                              ChainRec *__restrict__ crec)
+{
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (q >= M)
+        return;
+    const uint32_t j = order[q];
+    double u, z;
+    marker_draws(StreamKey{seed, chain0 + (uint32_t)c}, it, j, &u, &z);
+    crec[(size_t)c * M + q] = ChainRec{beta[(size_t)c * M + j], u, z, 0.0};
 }
 
 __global__ void k_batch_gather(const uint32_t *__restrict__ order, int64_t M, const double *__restrict__ scale,
@@ -705,7 +835,7 @@ __global__ void __launch_bounds__(256) k_batch_stats(int64_t M, const int32_t *_
 template <int KM>
 cudaError_t launch_batch_km(const BatchArgs &a, cudaStream_t st)
 {
-    const size_t smem = batch_smem_bytes(a.C, a.kext);
+    const size_t smem = batch_smem_bytes(a.C, a.kext, a.G);
     cudaError_t e = cudaFuncSetAttribute(k_sweep_batch<KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
@@ -717,7 +847,7 @@ cudaError_t launch_batch_km(const BatchArgs &a, cudaStream_t st)
 
 }  // namespace
 
-size_t batch_smem_bytes(int C, int kext) { return batch_plan(C, kext).total; }
+size_t batch_smem_bytes(int C, int kext, int G) { return batch_plan(C, kext, G).total; }
 
 int batch_max_ctas_per_sm(int C, int kext, size_t smem)
 {
@@ -736,6 +866,14 @@ cudaError_t launch_batch_gather(const uint32_t *order, int64_t M, const double *
                                 const int32_t *group, BatchRec *rec, cudaStream_t st)
 {
     k_batch_gather<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(order, M, scale, counts, group, rec);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_draws(uint32_t seed, uint32_t chain0, uint32_t it, int64_t M, int C, const uint32_t *order,
+                               const double *beta, ChainRec *crec, cudaStream_t st)
+{
+    k_batch_draws<<<dim3((unsigned)((M + 255) / 256), (unsigned)C), 256, 0, st>>>(seed, chain0, it, M, order, beta,
+                                                                                  crec);
     return cudaGetLastError();
 }
 

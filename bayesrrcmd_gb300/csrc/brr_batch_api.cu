@@ -57,7 +57,10 @@ struct brr_batch {
     int32_t *d_slice_lo = nullptr, *d_group = nullptr, *d_gK = nullptr;
     uint32_t *d_order = nullptr;
     BatchRec *d_rec = nullptr;
-    double *d_u = nullptr, *d_z = nullptr, *d_beta = nullptr, *d_acum = nullptr, *d_gconst = nullptr;
+    ChainRec *d_crec = nullptr;
+    float *d_gcf = nullptr;
+    float4 *d_gdf = nullptr;
+    double *d_beta = nullptr, *d_acum = nullptr, *d_gconst = nullptr;
     int32_t *d_comp = nullptr;
     uint8_t *d_chosen = nullptr;
     long long *d_E = nullptr, *d_dmu = nullptr, *d_sumE = nullptr, *d_wx = nullptr, *d_prof = nullptr;
@@ -78,7 +81,7 @@ struct brr_batch {
     std::future<void> perm_future;
     uint32_t perm_next_it = UINT32_MAX;
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
-    long long phase[4] = {0, 0, 0, 0};
+    long long phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
     StreamKey key(int c) const { return StreamKey{cfg.seed, cfg.chain + (uint32_t)c}; }
 };
@@ -90,7 +93,7 @@ void free_batch(brr_batch *b)
     if (b->perm_future.valid())
         b->perm_future.wait();
     void *dev[] = {b->d_codes, b->d_counts, b->d_lut,  b->d_scale, b->d_colsum, b->d_slice_lo, b->d_group,
-                   b->d_gK,    b->d_order,  b->d_rec,  b->d_u,     b->d_z,      b->d_beta,     b->d_acum,
+                   b->d_gK,    b->d_order,  b->d_rec,  b->d_crec,  b->d_gcf,    b->d_gdf,      b->d_beta,     b->d_acum,
                    b->d_gconst, b->d_comp,  b->d_chosen, b->d_E,    b->d_dmu,   b->d_sumE,   b->d_wx,       b->d_prof,
                    b->d_acc,   b->d_counter, b->d_stats, b->d_pacc, b->d_part,  b->d_err};
     for (void *p : dev)
@@ -104,11 +107,13 @@ void free_batch(brr_batch *b)
 }
 
 size_t acc_words(int C) { return (size_t)kBatchCopies * C * kBatchBlock; }
-size_t pacc_words() { return (size_t)2 * kBatchCopies * kBatchBlock * kBatchBlock; }
+size_t pacc_words() { return (size_t)2 * kBatchPCopies * kBatchBlock * kBatchBlock; }
 size_t stats_words(int C, int ng) { return (size_t)C * (ng * kMaxK + 2 * ng); }
 
-// Sampler constants of chain c (src/BayesRBase.cpp:309-333), as in the single-chain driver.
-void chain_constants(const brr_batch *b, int c, double *gc, int32_t *gK)
+// Sampler constants of chain c (src/BayesRBase.cpp:309-333), as in the
+// single-chain driver, and their FP32 form for the certified sampler:
+// {logL_k - logL_0 constant, h_k} per component.
+void chain_constants(const brr_batch *b, int c, double *gc, float *gcf, float4 *gdf, int32_t *gK)
 {
     const brr_config &cf = b->cfg;
     const double NM1 = (double)(cf.N - 1);
@@ -131,6 +136,20 @@ void chain_constants(const brr_batch *b, int c, double *gc, int32_t *gK)
             row[4 * k + 1] = 1.0 / denom;
             row[4 * k + 2] = 0.5 / denom / sE;
             row[4 * k + 3] = std::sqrt(sE / denom);
+        }
+        float *frow = gcf + (size_t)g * kMaxK * 2;
+        float4 *drow = gdf + (size_t)g * kMaxK;
+        auto split = [](double v, float &h, float &l) {
+            h = (float)v;
+            l = (float)(v - (double)h);
+        };
+        for (int k = 0; k < kMaxK; ++k) {
+            frow[2 * k] = (k == 0 || k >= K) ? 0.f : (float)(row[4 * k] - row[0]);
+            frow[2 * k + 1] = (k == 0 || k >= K) ? 0.f : (float)row[4 * k + 2];
+            float4 d4{0.f, 0.f, 0.f, 0.f};
+            split(row[4 * k + 3], d4.x, d4.y);
+            split(row[4 * k + 1], d4.z, d4.w);
+            drow[k] = d4;
         }
     }
 }
@@ -224,7 +243,7 @@ int brr_batch_create(const brr_config *cfg, int32_t chains, brr_batch **out)
     }
     b->kext = (int)(maxch * 16);
     b->col_stride = 16 * ((c.N + 63) / 64);
-    const size_t smem = batch_smem_bytes(chains, b->kext);
+    const size_t smem = batch_smem_bytes(chains, b->kext, G);
     const int per_sm = smem <= (size_t)prop.sharedMemPerBlockOptin ? batch_max_ctas_per_sm(chains, b->kext, smem) : 0;
     if (per_sm < 1 || (int64_t)per_sm * b->sms < G) {
         // shared memory per individual of a slice: genotypes 64 B, residual limbs 8 B per chain, codes 8 B
@@ -266,7 +285,9 @@ int brr_batch_pack_bed_device(brr_batch *b, const uint8_t *d_bed, int64_t nbytes
             balloc(&b->d_lut, (size_t)M * 4) || balloc(&b->d_scale, (size_t)M * 2) || balloc(&b->d_colsum, (size_t)M) ||
             balloc(&b->d_slice_lo, (size_t)b->G + 1) || balloc(&b->d_group, (size_t)M) ||
             balloc(&b->d_gK, (size_t)kMaxGroups) || balloc(&b->d_order, (size_t)M) || balloc(&b->d_rec, (size_t)M) ||
-            balloc(&b->d_u, (size_t)(C * M)) || balloc(&b->d_z, (size_t)(C * M)) || balloc(&b->d_beta, (size_t)(C * M)) ||
+            balloc(&b->d_crec, (size_t)(C * M)) || balloc(&b->d_gcf, (size_t)C * cf.n_groups * kMaxK * 2) ||
+            balloc(&b->d_gdf, (size_t)C * cf.n_groups * kMaxK) ||
+            balloc(&b->d_beta, (size_t)(C * M)) ||
             balloc(&b->d_acum, (size_t)(C * M)) || balloc(&b->d_comp, (size_t)(C * M)) ||
             balloc(&b->d_chosen, (size_t)(C * M)) ||
             balloc(&b->d_gconst, (size_t)C * cf.n_groups * kMaxK * 4) || balloc(&b->d_E, (size_t)(C * cf.N)) ||
@@ -429,6 +450,8 @@ int brr_batch_iterate(brr_batch *b, int32_t n_iter)
     for (int g = 0; g < ng; ++g)
         kmax = std::max(kmax, cf.K[g]);
     std::vector<double> gc((size_t)C * ng * kMaxK * 4);
+    std::vector<float> gcf((size_t)C * ng * kMaxK * 2);
+    std::vector<float4> gdf((size_t)C * ng * kMaxK);
     std::vector<int32_t> gK(ng);
     std::vector<long long> dmu(C);
     std::vector<double> part((size_t)b->G * C * 2);
@@ -449,16 +472,18 @@ int brr_batch_iterate(brr_batch *b, int32_t n_iter)
             b->sumE[c] += (long long)N * dmu[c];
             b->mu[c] = mu_new;
         }
-        // per-marker draws of every chain and the shared permutation (src/BayesRBase.cpp:196-198)
-        for (int c = 0; c < C; ++c)
-            BATCH_CUDA(launch_draws(cf.seed, cf.chain + (uint32_t)c, it, M, b->d_u + (size_t)c * M, b->d_z + (size_t)c * M,
-                                    b->st));
+        // the shared permutation and every chain's per-marker draws, laid out
+        // in sweep order with beta_old (src/BayesRBase.cpp:196-198)
         b->perm_future.wait();
         std::memcpy(b->h_order, b->perm_next.data(), sizeof(uint32_t) * M);
         BATCH_CUDA(cudaMemcpyAsync(b->d_order, b->h_order, sizeof(uint32_t) * M, cudaMemcpyHostToDevice, b->st));
+        BATCH_CUDA(launch_batch_draws(cf.seed, cf.chain, it, M, C, b->d_order, b->d_beta, b->d_crec, b->st));
         for (int c = 0; c < C; ++c)
-            chain_constants(b, c, gc.data() + (size_t)c * ng * kMaxK * 4, gK.data());
+            chain_constants(b, c, gc.data() + (size_t)c * ng * kMaxK * 4, gcf.data() + (size_t)c * ng * kMaxK * 2,
+                            gdf.data() + (size_t)c * ng * kMaxK, gK.data());
         BATCH_CUDA(cudaMemcpyAsync(b->d_gconst, gc.data(), sizeof(double) * gc.size(), cudaMemcpyHostToDevice, b->st));
+        BATCH_CUDA(cudaMemcpyAsync(b->d_gcf, gcf.data(), sizeof(float) * gcf.size(), cudaMemcpyHostToDevice, b->st));
+        BATCH_CUDA(cudaMemcpyAsync(b->d_gdf, gdf.data(), sizeof(float4) * gdf.size(), cudaMemcpyHostToDevice, b->st));
         BATCH_CUDA(cudaMemcpyAsync(b->d_gK, gK.data(), sizeof(int32_t) * ng, cudaMemcpyHostToDevice, b->st));
         BATCH_CUDA(cudaMemcpyAsync(b->d_dmu, dmu.data(), sizeof(long long) * C, cudaMemcpyHostToDevice, b->st));
         BATCH_CUDA(cudaMemcpyAsync(b->d_sumE, b->sumE.data(), sizeof(long long) * C, cudaMemcpyHostToDevice, b->st));
@@ -482,9 +507,10 @@ int brr_batch_iterate(brr_batch *b, int32_t n_iter)
         a.col_stride = b->col_stride;
         a.rec = b->d_rec;
         a.gconst = b->d_gconst;
+        a.gcf = b->d_gcf;
+        a.gdf = b->d_gdf;
         a.gK = b->d_gK;
-        a.u = b->d_u;
-        a.z = b->d_z;
+        a.crec = b->d_crec;
         a.beta = b->d_beta;
         a.acum = b->d_acum;
         a.comp = b->d_comp;
@@ -517,7 +543,7 @@ int brr_batch_iterate(brr_batch *b, int32_t n_iter)
         float ms = 0.f;
         BATCH_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
         sweep_total += ms;
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 8; ++k)
             b->phase[k] += prof[k];
 
         // per chain: the residual total from the slices must equal the one the
@@ -616,7 +642,7 @@ int brr_batch_get_timing(brr_batch *b, double *sweep_ms, double *total_ms, int64
     if (total_ms)
         *total_ms = b->last_total_ms;
     if (cycles)
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 8; ++k)
             cycles[k] = b->phase[k];
     return BRR_OK;
 }
@@ -638,7 +664,7 @@ int brr_batch_get_geometry(brr_batch *b, int32_t *ctas, int32_t *slice, int64_t 
     if (slice)
         *slice = b->kext;
     if (smem_bytes)
-        *smem_bytes = (int64_t)batch_smem_bytes(b->C, b->kext);
+        *smem_bytes = (int64_t)batch_smem_bytes(b->C, b->kext, b->G);
     return BRR_OK;
 }
 

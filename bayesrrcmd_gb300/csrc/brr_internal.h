@@ -107,7 +107,8 @@ constexpr int kBatchFrac = 40;
 constexpr int kBatchLimbs = 4;
 constexpr int kBatchBlock = 32;          // markers per block
 constexpr int kBatchMaxChains = 64;
-constexpr int kBatchCopies = 8;          // copies of the exchange accumulators (CTA s adds into s % 8)
+constexpr int kBatchCopies = 8;          // copies of the dot accumulators (CTA s adds into s % 8)
+constexpr int kBatchPCopies = 4;         // copies of the block Gram accumulators (CTA s adds into s % 4)
 
 struct alignas(16) BatchRec {
     double sigma;        // 1 / sd of the marker column
@@ -117,6 +118,15 @@ struct alignas(16) BatchRec {
     int32_t group;
 };
 static_assert(sizeof(BatchRec) == 32, "BatchRec must be 32 bytes");
+
+// Per chain and sweep position: beta_old of the marker and its draws.
+struct alignas(32) ChainRec {
+    double beta_old;
+    double u;
+    double z;
+    double pad;
+};
+static_assert(sizeof(ChainRec) == 32, "ChainRec must be 32 bytes");
 
 struct BatchArgs {
     int64_t N, M;
@@ -129,16 +139,18 @@ struct BatchArgs {
     int64_t col_stride;
     const BatchRec *rec;             // M records in sweep order
     const double *gconst;            // [C][n_groups][kMaxK][4] sampler constants per chain
+    const float *gcf;                // [C][n_groups][kMaxK][2] FP32 {logL_k - logL_0 constant, h_k}
+    const float4 *gdf;               // [C][n_groups][kMaxK] double-float {sdk hi, lo, invden hi, lo}
     const int32_t *gK;               // [n_groups] mixture sizes
-    const double *u, *z;             // [C][M] draws
-    double *beta, *acum;             // [C][M]
+    const ChainRec *crec;            // [C][M] in sweep order
+    double *beta, *acum;             // [C][M] by marker id
     int32_t *comp;                   // [C][M]
     uint8_t *chosen;                 // [C][M] the sampler chose a component in this sweep
     long long *E;                    // [C][N] fixed-point residual (in at sweep start, out at the end)
     const long long *dmu;            // [C] fixed-point shift added to E at the start (updateMu)
     long long *sumE;                 // [C] exact residual total, carried through the sweep
     unsigned long long *acc;         // [kBatchCopies][C][32] dot-product accumulators (zero at launch)
-    unsigned *pacc;                  // [2][kBatchCopies][32][32] integer block Gram accumulators (zero at launch)
+    unsigned *pacc;                  // [2][kBatchPCopies][32][32] integer block Gram accumulators (zero at launch)
     long long *wx;                   // [C][33] per block: W per marker, then the constant
     unsigned long long *counter;     // 2 barrier counters, 32 words apart (zero at launch)
     double *part;                    // [G][C][2] per slice: sum(E) (bits of an int64) and sum(eps^2)
@@ -152,9 +164,13 @@ int api_fail(int code, const std::string &msg);
 
 cudaError_t launch_batch_gather(const uint32_t *order, int64_t M, const double *scale, const int64_t *counts,
                                 const int32_t *group, BatchRec *rec, cudaStream_t st);
+// Per chain c and sweep position q: beta_old of marker order[q] and its draws
+// (u, z) from chain (chain0 + c)'s stream for iteration it.
+cudaError_t launch_batch_draws(uint32_t seed, uint32_t chain0, uint32_t it, int64_t M, int C, const uint32_t *order,
+                               const double *beta, ChainRec *crec, cudaStream_t st);
 cudaError_t launch_batch_stats(int64_t M, int C, const int32_t *group, const int32_t *comp, const uint8_t *chosen,
                                const double *beta, int n_groups, unsigned long long *out, cudaStream_t st);
-size_t batch_smem_bytes(int C, int kext);
+size_t batch_smem_bytes(int C, int kext, int G);
 int batch_max_ctas_per_sm(int C, int kext, size_t smem);
 cudaError_t launch_sweep_batch(const BatchArgs &a, int kmax, cudaStream_t st);
 

@@ -118,4 +118,82 @@ __device__ __forceinline__ Pick pick_marker(double num, double u, double z, doub
     return res;
 }
 
+// FP32 component selection with a rigorous error bound, falling back to the
+// FP64 evaluation of pick_marker when the bound cannot certify the decision.
+// With D_k = logL_k - logL_0 = dc_k + h_k*num^2 (dc_0 = h_0 = 0) evaluated by one
+// FMA from rounded inputs, |error(D_k)| <= 3u(|dc_k| + |h_k num^2|) with
+// u = 2^-24.  The 700 guards compare differences of D (the logL_0 offset
+// cancels); a guard whose difference lies within the error band of 700
+// falls back.  Probabilities then carry at most 2*max_err + 2^-21 relative
+// error, so a u within tol = 4e-5 + 4*max_err of a cumulative bound falls back.
+template <int KM>
+__device__ __forceinline__ bool pick_f32(float xh, float xl, float uf, const float *__restrict__ gcf, int K,
+                                         int &comp, float &a0out)
+{
+    // num = xh + xl (double-float); num^2 to FP32 within 3u
+    const float n2 = __fmaf_rn(xh, xh, 2.f * xh * xl);
+    float D[KM];
+    float maxerr = 0.f;
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+        if (k == 0 || k >= K) {
+            D[k] = k == 0 ? 0.f : -INFINITY;
+        } else {
+            const float dc = gcf[2 * k], h = gcf[2 * k + 1];
+            D[k] = __fmaf_rn(h, n2, dc);
+            maxerr = fmaxf(maxerr, 3.0e-7f * (fabsf(dc) + fabsf(h * n2)));
+        }
+    }
+    float dmax = 0.f, dmax1 = D[1], dmin1 = D[1];
+#pragma unroll
+    for (int k = 1; k < KM; ++k) {
+        if (k < K) {
+            dmax = fmaxf(dmax, D[k]);
+            dmax1 = fmaxf(dmax1, D[k]);
+            dmin1 = fminf(dmin1, D[k]);
+        }
+    }
+    const float band = 2.f * maxerr + 1e-3f;
+    const float spread = dmax1 - dmin1;
+    bool unsure = fabsf(spread - 700.f) < band || fabsf(dmax1 - 700.f) < band || fabsf(-dmin1 - 700.f) < band;
+    const bool wide = spread > 700.f;
+    const bool guard0 = (dmax1 > 700.f) || (-dmin1 > 700.f);
+    float e[KM];
+    float es = 0.f;
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+        e[k] = k < K ? __expf(D[k] - dmax) : 0.f;
+        es += e[k];
+    }
+    const float ies = __frcp_rn(es);
+    int chosen = -1;
+    float acum = 0.f, prev = 0.f, a0 = 0.f;
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+        if (k < K && chosen < 0) {
+            bool guard;
+            if (k == 0) {
+                guard = guard0;
+            } else {
+                const float d1 = dmax1 - D[k], d2 = D[k] - dmin1;
+                if (wide && (fabsf(d1 - 700.f) < band || fabsf(d2 - 700.f) < band))
+                    unsure = true;
+                guard = wide && (d1 > 700.f || d2 > 700.f);
+            }
+            const float pk = guard ? 0.f : e[k] * ies;
+            if (k == 0)
+                a0 = pk;
+            prev = acum;
+            acum += pk;
+            if (uf <= acum)
+                chosen = k;
+        }
+    }
+    const float tol = 4e-5f + 4.f * maxerr;
+    const bool close = chosen >= 0 ? ((uf > acum - tol) || (chosen > 0 && uf < prev + tol)) : (uf < acum + tol);
+    comp = chosen;
+    a0out = a0;
+    return !(unsure || close);
+}
+
 }  // namespace brr

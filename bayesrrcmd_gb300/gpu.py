@@ -396,7 +396,7 @@ class Batch:
 
     def timing(self):
         sw, tot = C.c_double(), C.c_double()
-        cyc = np.zeros(4, np.int64)
+        cyc = np.zeros(8, np.int64)
         self._check(self.lib.brr_batch_get_timing(self.h, C.byref(sw), C.byref(tot), _ptr(cyc, C.c_int64)))
         return sw.value, tot.value, cyc
 

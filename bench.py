@@ -11,6 +11,11 @@ the plain FP64 kernel is timed beside it on the same steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+Beside the headline, the batching form is measured on its own workload
+(64 chains with their own phenotypes on N = 50,000 x M = 200,000 shared
+genotypes; the "batched" object): aggregate marker-updates/s of all chains
+against the plain FP64 single-chain kernel on the same genotypes.
+
 `--impl reference` times the reference algorithm's CPU implementation on the
 host cores (the repository's FP64 restatement, since the reference itself
 cannot be built: Eigen, Boost.Random and TBB are absent) on a bounded sample
@@ -52,6 +57,16 @@ def peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def peaks_bf16():
+    """Dense bf16 tensor peak (TFLOP/s) for a kernel timed inside a long step:
+    the sustained figure of MEASURED_PEAKS.json, else the fallback."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("bf16_tflops_sustained", d["bf16_tflops"]))
+    return 1700.0
 
 
 class ClockSampler:
@@ -186,6 +201,69 @@ def run_e2e(lib, gpu, torch, device, host_bed, y, group, steps, chain_id):
     return dict(wall=wall, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps)
 
 
+# Batching form: 64 chains (distinct seeds, one phenotype each) on shared
+# genotypes, N = 50,000 x M = 200,000, p ~ U(0.01, 0.5), 1,000 causal markers per
+# phenotype with h2 ~ U(0.1, 0.7); marker blocks of 32 on the tensor cores.
+B_N, B_M, B_C = 50_000, 200_000, 64
+B_WORKLOAD = ("batched BayesR, 64 chains (distinct seeds, 64 phenotypes h2~U(0.1,0.7), 1,000 causal each) on shared "
+              "dense genotypes N=50,000 x M=200,000, p~U(0.01,0.5), blocks of 32, S=0.01,0.001,0.0001")
+
+
+def run_batched(lib, gpu, torch, device, steps, warmup):
+    """Aggregate marker-updates/s of the 64-chain tensor-core form and of the
+    plain FP64 single-chain kernel on the same genotypes."""
+    S = [[0.01, 0.001, 0.0001]]
+    seed = SEED + 7
+    cb = (B_N + 3) // 4
+    d_bed = torch.empty(B_M * cb, dtype=torch.uint8, device=device)
+    gpu.synth_bed_device(d_bed.data_ptr(), B_N, B_M, seed, P_LO, P_HI, 0.0, lib=lib)
+    probe = gpu.Chain(gpu.ChainConfig(N=B_N, M=B_M, S=S, device=device), lib=lib)
+    probe.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+    rng = np.random.default_rng(seed)
+    ys = np.zeros((B_C, B_N), np.float32)
+    for c in range(B_C):
+        h2 = rng.uniform(0.1, 0.7)
+        causal = np.sort(rng.choice(B_M, N_CAUSAL, replace=False)).astype(np.uint32)
+        b = rng.normal(0.0, np.sqrt(h2 / N_CAUSAL), N_CAUSAL)
+        ys[c] = probe.xbeta(causal, b) + rng.normal(0.0, np.sqrt(1.0 - h2), B_N)
+    probe.close()
+    bt = gpu.Batch(gpu.ChainConfig(N=B_N, M=B_M, S=S, seed=seed, device=device), B_C, lib=lib)
+    bt.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+    bt.set_phenotypes(ys)
+    bt.init()
+    geo = bt.geometry()
+    bt.iterate(warmup)
+    torch.cuda.synchronize(device)
+    bt.iterate(steps)
+    torch.cuda.synchronize(device)
+    b_sweep, b_total, cyc = bt.timing()
+    bt.close()
+    ch = gpu.Chain(gpu.ChainConfig(N=B_N, M=B_M, S=S, seed=seed, form=gpu.FORM_FP64, device=device), lib=lib)
+    ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+    ch.set_phenotype(ys[0])
+    ch.init()
+    p_steps = 2
+    ch.iterate(1)
+    ch.iterate(p_steps)
+    p_sweep, p_total, _ = ch.timing()
+    ch.close()
+    del d_bed
+    torch.cuda.empty_cache()
+    nblocks = (B_M + 31) // 32
+    # algorithmic tensor work per block: X_block^T E and X_block dB (2 * 32 * C * N
+    # each) plus the block Gram (32 * 32 * N); the kernel computes the residual
+    # as four 11-bit limbs, i.e. four times the dot and update products
+    alg_flop = nblocks * (2 * 2 * 32 * B_C * B_N + 2 * 32 * 32 * B_N)
+    issued_flop = nblocks * (2 * 2 * 32 * 4 * B_C * B_N + 2 * 128 * 32 * B_N)
+    sweep_s = b_sweep / 1e3 / steps
+    rate = B_C * B_M * steps / (b_total / 1e3)
+    plain = B_M * p_steps / (p_total / 1e3)
+    return dict(rate=rate, ms_per_step=b_total / steps, sweep_ms=b_sweep / steps, plain=plain,
+                plain_ms=p_total / p_steps, alg_tflops=alg_flop / sweep_s / 1e12,
+                issued_tflops=issued_flop / sweep_s / 1e12,
+                cycles=(cyc / steps / nblocks).tolist(), geometry=geo)
+
+
 def numpy_sample(m_sample, seed):
     """A CPU-generated sample of the workload: N individuals, m_sample markers."""
     from bayesrrcmd_gb300 import plink
@@ -235,6 +313,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-chain batching-form measurement")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: N=100,000 x M=8,192 (200 MB of codes, above L2), same settings")
     args = ap.parse_args()
@@ -304,6 +383,26 @@ def main():
                "h2d_bytes_per_step": int(e["h2d_per_step"]), "d2h_bytes_per_step": int(e["d2h_per_step"]),
                "includes": f"chain of {e2e_steps} iterations: pinned-host BED upload + device packing + "
                            f"marker Gram + init, then per iteration the sample read-back"}
+    batched = None
+    if not args.no_batch and not args.small:
+        bsteps = int(os.environ.get("BRR_BATCH_STEPS", "3"))
+        bb = run_batched(lib, gpu, torch, device, bsteps, max(args.warmup, 2))
+        bf16_peak = peaks_bf16()
+        batched = {
+            "workload": B_WORKLOAD, "value": bb["rate"] * world, "unit": "marker-updates/s (all chains)",
+            "chains": B_C, "steps": bsteps, "ms_per_step": bb["ms_per_step"], "sweep_ms": bb["sweep_ms"],
+            "plain_fp64_same_genotypes": {"value": bb["plain"], "unit": "marker-updates/s (one chain)",
+                                          "ms_per_step": bb["plain_ms"]},
+            "aggregate_vs_plain": bb["rate"] / bb["plain"],
+            "roofline": {"bound": "tensor", "achieved": bb["alg_tflops"], "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": bb["alg_tflops"] / bf16_peak, "traffic": None,
+                         "issued_tflops": bb["issued_tflops"], "kernel": "k_sweep_batch (tcgen05 kind::f16)",
+                         "note": "algorithmic FLOPs: X_block^T E, X_block dB and the block Gram"},
+            "phase_clk_per_block_cta0": dict(zip(["dots", "publish", "resolve", "update", "resolve_wait_dots",
+                                                  "resolve_chain0", "steps_chain0", "resolve_wait_slowest"],
+                                                 bb["cycles"])),
+            "geometry": bb["geometry"],
+        }
     if rank != 0:
         return
     cpu = None
@@ -357,6 +456,7 @@ def main():
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "batched": batched,
     }
     print(json.dumps(line))
 

@@ -222,8 +222,10 @@ int brr_batch_iterate(brr_batch *b, int32_t n_iter);
 /* One chain's state; eps is the exact fixed-point residual as doubles. */
 int brr_batch_get_chain_state(brr_batch *b, int32_t chain, brr_state *st);
 /* Device time of the sweeps and of the whole last brr_batch_iterate call (ms);
- * cycles (optional, 4 values): CTA 0's cycles in the dot, publish, resolve and
- * update phases, summed over the sweeps of that call. */
+ * cycles (optional, 8 values), summed over the sweeps of that call, measured on
+ * CTA 0 (indicative): the dot, publish, resolve and update phases; then, of
+ * the resolve phase, the wait for all CTAs' dot products, chain 0's own
+ * resolve, chain 0's sampling steps, and the wait for the slowest chain. */
 int brr_batch_get_timing(brr_batch *b, double *sweep_ms, double *total_ms, int64_t *cycles);
 int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns);
 /* CTAs of the sweep, individuals per slice and shared memory per CTA. */

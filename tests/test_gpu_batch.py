@@ -6,7 +6,8 @@ stream (the batch shares one order per iteration).  The batched residual is
 exact fixed point (eps * 2^40): the chains differ from the FP64 oracle by the
 rounding of the fixed-point update coefficients, so beta (with an absolute
 floor of 1e-13 for betas near zero), sigmaE and sigmaG are compared at 1e-9
-relative, components exactly, the residual at 1e-10 absolute.  The constant
+relative, components exactly, the residual at 1e-10 absolute, acum
+(P(component 0), evaluated with FP32 exponentials) at 2e-6 relative.  The constant
 part of each update is rounded once and applied to every individual, which
 moves the residual mean coherently by up to 2^-41 per update: mu, a mean
 plus a draw, gets an absolute bar of 1e-10.
@@ -46,7 +47,7 @@ def compare(s, o, what):
     nz = o["beta"] != 0
     np.testing.assert_array_equal(s["beta"] != 0, nz, err_msg=what)
     np.testing.assert_allclose(s["beta"][nz], o["beta"][nz], rtol=RTOL, atol=1e-13, err_msg=what)
-    np.testing.assert_allclose(s["acum"], o["acum"], rtol=1e-8, atol=1e-14, err_msg=what)
+    np.testing.assert_allclose(s["acum"], o["acum"], rtol=2e-6, atol=1e-12, err_msg=what)
     np.testing.assert_allclose(s["sigmaE"], o["sigmaE"], rtol=RTOL, err_msg=what)
     np.testing.assert_allclose(s["sigmaG"], o["sigmaG"], rtol=RTOL, err_msg=what)
     np.testing.assert_allclose(s["mu"], o["mu"], rtol=RTOL, atol=1e-10, err_msg=what)
