@@ -314,6 +314,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-chain batching-form measurement")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the batching-form leg (profiling); --batch-markers sets its M")
+    ap.add_argument("--batch-markers", type=int, default=None)
     ap.add_argument("--small", action="store_true",
                     help="profiling case: N=100,000 x M=8,192 (200 MB of codes, above L2), same settings")
     args = ap.parse_args()
@@ -351,6 +354,16 @@ def main():
     lib = gpu.load_library()
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
+    if args.batch_only:
+        global B_M
+        if args.batch_markers:
+            B_M = args.batch_markers
+        bb = run_batched(lib, gpu, torch, device, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps({"batched_only": True, "markers": B_M, "value": bb["rate"], "unit": "marker-updates/s",
+                              "aggregate_vs_plain": bb["rate"] / bb["plain"], "ms_per_step": bb["ms_per_step"],
+                              "alg_tflops": bb["alg_tflops"], "cycles_per_block": bb["cycles"]}))
+        return
     d_bed, y, group = make_problem(lib, gpu, torch, device, rank)
 
     def barrier():
