@@ -20,7 +20,7 @@ LIBDIR = PKG / "lib"
 BUILD = PKG / "_build"
 LIB = LIBDIR / "libbrr_gpu.so"
 SOURCES = ["brr_pack.cu", "brr_sweep.cu", "brr_block.cu", "brr_batch.cu", "brr_api.cu", "brr_batch_api.cu",
-           "brr_noalloc.cu", "brr_gram.cu"]
+           "brr_multi_api.cu", "brr_noalloc.cu", "brr_gram.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
 

@@ -72,91 +72,8 @@ void make_permutation(StreamKey key, uint32_t it, uint32_t M, uint32_t *perm)
 
 }  // namespace brr
 
-struct brr_ctx {
-    brr_config cfg{};
-    int dev = 0;
-    int sms = 0;
-    cudaStream_t st = nullptr;
-    int G = 0;
-    int B = 16;
-    int64_t chunks = 0;
-    int64_t col_stride = 0;
-    int slice_max = 0;
-    int slot_bytes = 0;
-    std::vector<int32_t> slice_lo;
-    bool packed = false, pheno = false, inited = false;
+#include "brr_ctx.h"
 
-    // device buffers
-    int32_t *d_slice_lo = nullptr;
-    uint8_t *d_codes = nullptr;
-    int64_t *d_counts = nullptr;
-    double *d_table = nullptr;
-    double *d_scale = nullptr;
-    double *d_colsum = nullptr;
-    uint8_t *d_chosen = nullptr;
-    unsigned long long *d_vstat = nullptr;   // sweep statistics: counts, fixed-point square sums
-    int32_t *d_roff = nullptr;          // 3 x (M*G+1)
-    uint16_t *d_ridx[3] = {nullptr, nullptr, nullptr};
-    int64_t rtot[3] = {0, 0, 0};
-    int32_t *d_group = nullptr;
-    double *d_ystd = nullptr;
-    double *d_beta = nullptr;
-    int32_t *d_comp = nullptr;
-    double *d_acum = nullptr;
-    double *d_eps = nullptr;
-    float *d_eps_hi = nullptr, *d_eps_lo = nullptr;
-    uint32_t *d_order = nullptr;
-    double *d_u = nullptr, *d_z = nullptr;
-    SweepRec *d_rec = nullptr;
-    unsigned long long *d_acc = nullptr;   // accumulators followed by the counter
-    double *d_gconst = nullptr;
-    int32_t *d_gK = nullptr;
-    double *d_stats = nullptr;
-    double *d_part = nullptr;
-    int *d_err = nullptr;
-    long long *d_rounds = nullptr;
-    long long *d_prof = nullptr;        // per-phase cycles of the last sweep (CTA 0)
-    uint32_t *d_nzj = nullptr;
-    double *d_nzb = nullptr;
-    double *d_gram = nullptr;           // blocked FP32C: packed marker Gram
-    double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries (8 blocks)
-    BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
-    float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)
-    bool blocked = false;
-    bool has_missing = false;
-    int kind = BRR_KIND_DENSE;          // storage: dense codes, or ragged lists (Ragged and Eigen markers)
-    bool eigen = false;                 // Eigen sparse markers (BRR_KIND_EIGEN)
-    double gram_ms = 0.0;
-
-    // pinned host staging
-    uint32_t *h_order = nullptr;
-    double *h_stats = nullptr;
-    double *h_part = nullptr;
-
-    // host chain state
-    std::vector<int32_t> group;
-    std::vector<double> ystd;
-    double mu = 0.0, sigmaE = 0.0, epsSum = 0.0;
-    double sigmaG[BRR_MAX_GROUPS] = {};
-    double pi[BRR_MAX_GROUPS * BRR_MAX_K] = {};
-    uint32_t iteration = 0;
-    int64_t sweeps = 0;
-
-    // timing
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    double last_sweep_ms = 0.0, last_total_ms = 0.0;
-    int64_t last_rounds = 0;
-    long long phase[16] = {};   // summed over the sweeps of the last call
-    uint64_t wait_limit_ns = 2000000000ull;
-    int phantom = 0;
-
-    // permutation prepared one iteration ahead on a host thread
-    std::future<void> perm_future;
-    std::vector<uint32_t> perm_next;
-    uint32_t perm_next_it = UINT32_MAX;
-
-    StreamKey key() const { return StreamKey{cfg.seed, cfg.chain}; }
-};
 
 namespace {
 
@@ -211,12 +128,9 @@ void free_all(brr_ctx *c)
         cudaStreamDestroy(c->st);
 }
 
-constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
 // fixed-point accumulators: 3 rotating buffers of the restart sweep, 8 buffers
 // of 8 copies for the blocked sweep; followed by the barrier counters (restart
 // sweep: the first word; blocked sweep: 2 x 8 counters 16 words apart)
-constexpr size_t kAccWords = 8 * 8 * kMaxSpec * 4;
-constexpr size_t kCounterWords = 2 * 8 * 16;
 
 // Per-group sampler constants for the current sigmaE, sigmaG, pi
 // (src/BayesRBase.cpp:309-333): c_k = log(pi_k) - log(sigmaG/sigmaE*(N-1)*cVa_k + 1)/2,
@@ -292,8 +206,105 @@ int download_eps(brr_ctx *c, double *eps_host)
     return BRR_OK;
 }
 
-// One sweep over the order already in d_order with draws in d_u/d_z.
-int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, float *sweep_ms)
+// Slices of individuals for G CTAs in whole 64-individual chunks.
+void compute_slices(brr_ctx *x, int G)
+{
+    G = (int)std::min<int64_t>(std::max(G, 1), x->chunks);
+    x->G = G;
+    x->slice_lo.assign(G + 1, 0);
+    int64_t maxch = 0;
+    for (int s = 0; s <= G; ++s) {
+        const int64_t ch = (int64_t)s * x->chunks / G;
+        x->slice_lo[s] = (int32_t)std::min<int64_t>(ch * kChunk, x->cfg.N);
+        if (s > 0)
+            maxch = std::max<int64_t>(maxch, ch - (int64_t)(s - 1) * x->chunks / G);
+    }
+    x->slice_max = (int)(maxch * kChunk);
+    x->slot_bytes = (int)(maxch * 16);
+}
+
+// Per (marker, slice) ragged index lists from the packed codes for the current slices.
+int build_ragged_lists(brr_ctx &c)
+{
+    const int64_t M = c.cfg.M;
+    const int64_t MG1 = M * (int64_t)c.G + 1;
+    if (3 * MG1 > (int64_t)INT_MAX)
+        return fail(BRR_ERR_ARG, "ragged offset table too large for int32");
+    cudaFree(c.d_roff);
+    c.d_roff = nullptr;
+    if (dalloc(&c.d_roff, (size_t)(3 * MG1)))
+        return fail(BRR_ERR_OOM, "device allocation failed");
+    BRR_CUDA(cudaMemsetAsync(c.d_roff, 0, sizeof(int32_t) * 3 * MG1, c.st));
+    BRR_CUDA(launch_ragged_slice_counts(c.d_codes, c.col_stride, M, c.G, c.d_slice_lo, c.d_roff, c.st));
+    int32_t *tmp = nullptr;
+    if (dalloc(&tmp, (size_t)((MG1 + 1023) / 1024 + 1)))
+        return fail(BRR_ERR_OOM, "device allocation failed");
+    // totals must fit int32: the counts bound them by the genotype counts
+    std::vector<int64_t> cnt(M * 4);
+    BRR_CUDA(cudaMemcpyAsync(cnt.data(), c.d_counts, sizeof(int64_t) * M * 4, cudaMemcpyDeviceToHost, c.st));
+    BRR_CUDA(cudaStreamSynchronize(c.st));
+    int64_t tot[3] = {0, 0, 0};
+    for (int64_t j = 0; j < M; ++j) {
+        tot[0] += cnt[4 * j + 1];
+        tot[1] += cnt[4 * j + 2];
+        tot[2] += cnt[4 * j + 3];
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (tot[k] > (int64_t)INT_MAX) {
+            cudaFree(tmp);
+            return fail(BRR_ERR_ARG, "ragged index list longer than 2^31 entries");
+        }
+        BRR_CUDA(launch_exclusive_scan_i32(c.d_roff + k * MG1, MG1, tmp, c.st));
+        cudaFree(c.d_ridx[k]);
+        c.d_ridx[k] = nullptr;
+        if (dalloc(&c.d_ridx[k], (size_t)tot[k] + 1)) {
+            cudaFree(tmp);
+            return fail(BRR_ERR_OOM, "device allocation failed");
+        }
+        c.rtot[k] = tot[k];
+    }
+    BRR_CUDA(cudaStreamSynchronize(c.st));
+    cudaFree(tmp);
+    BRR_CUDA(launch_ragged_fill(c.d_codes, c.col_stride, M, c.G, c.d_slice_lo, c.d_roff, c.d_roff + MG1,
+                                c.d_roff + 2 * MG1, c.d_ridx[0], c.d_ridx[1], c.d_ridx[2], c.st));
+    return BRR_OK;
+}
+
+}  // namespace
+
+// New slicing (G CTAs) and round width B of a packed chain; the residual and
+// the chain state are per individual and marker, so they carry over.
+int brr::reslice(brr_ctx *c, int G, int B)
+{
+    if (!c->packed)
+        return fail(BRR_ERR_ARG, "markers are not packed");
+    BRR_CUDA(cudaSetDevice(c->dev));
+    BRR_CUDA(cudaStreamSynchronize(c->st));
+    compute_slices(c, G);
+    if (B > 0)
+        c->B = B;
+    cudaFree(c->d_slice_lo);
+    c->d_slice_lo = nullptr;
+    cudaFree(c->d_part);
+    c->d_part = nullptr;
+    cudaFreeHost(c->h_part);
+    c->h_part = nullptr;
+    if (dalloc(&c->d_slice_lo, (size_t)c->G + 1) || dalloc(&c->d_part, (size_t)std::max(2 * c->G, kPartBlocks)) ||
+        cudaMallocHost((void **)&c->h_part, sizeof(double) * std::max(2 * c->G, kPartBlocks)) != cudaSuccess)
+        return fail(BRR_ERR_OOM, "allocation for the new slices failed");
+    BRR_CUDA(cudaMemcpy(c->d_slice_lo, c->slice_lo.data(), sizeof(int32_t) * (c->G + 1), cudaMemcpyHostToDevice));
+    if (c->kind == BRR_KIND_RAGGED) {
+        const int rc = build_ragged_lists(*c);
+        if (rc)
+            return rc;
+    }
+    BRR_CUDA(cudaStreamSynchronize(c->st));
+    return BRR_OK;
+}
+
+// Sampler constants, records in sweep order and the sweep arguments for the
+// order in d_order and the draws in d_u/d_z.
+int brr::sweep_prepare(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, size_t &smem)
 {
     const brr_config &cf = c->cfg;
     std::vector<double> gc;
@@ -310,7 +321,7 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + kCounterWords), c->st));
     BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
 
-    SweepArgs a{};
+    a = SweepArgs{};
     a.N = cf.N;
     a.M = cf.M;
     a.G = c->G;
@@ -359,17 +370,16 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     a.beta_df = c->d_bdf;
     a.acum_df = c->d_bdf ? c->d_bdf + cf.M : nullptr;
     BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 16, c->st));
-    const size_t smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, c->kind, a);
+    smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, c->kind, a);
+    return BRR_OK;
+}
 
-    BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
-    if (c->blocked)
-        BRR_CUDA(launch_sweep_block(a, smem, c->st));
-    else
-        BRR_CUDA(launch_sweep(cf.form, c->kind, a, smem, c->st));
-    BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
-    if (c->blocked)
-        BRR_CUDA(launch_block_finish(cf.M, c->d_chosen, a.beta_df, a.acum_df, c->d_beta, c->d_acum, c->st));
 
+// Statistics of the sweep just run: component counts, squared betas, residual
+// sums, rounds, device status.
+int brr::sweep_finish(brr_ctx *c, brr_sweep_out *out)
+{
+    const brr_config &cf = c->cfg;
     const int ng = cf.n_groups;
     BRR_CUDA(launch_sweep_stats(cf.M, c->d_group, c->d_comp, c->d_chosen, c->d_beta, ng, c->d_vstat, c->st));
     const size_t nv = (size_t)ng * kMaxK + 2 * ng;
@@ -383,7 +393,6 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     const int rc = check_device_status(c);
     if (rc)
         return rc;
-    BRR_CUDA(cudaEventElapsedTime(sweep_ms, c->ev[0], c->ev[1]));
     for (int k = 0; k < 16; ++k)
         c->phase[k] += prof[k];
 
@@ -403,6 +412,33 @@ int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, f
     if (c->kind == BRR_KIND_RAGGED)
         c->epsSum = c->h_stats[0];
     c->sweeps += 1;
+    return BRR_OK;
+}
+
+namespace {
+
+// One sweep over the order already in d_order with draws in d_u/d_z.
+int run_sweep(brr_ctx *c, double mu_new, double eps_total, brr_sweep_out *out, float *sweep_ms)
+{
+    const brr_config &cf = c->cfg;
+    SweepArgs a{};
+    size_t smem = 0;
+    int rc = sweep_prepare(c, mu_new, eps_total, a, smem);
+    if (rc)
+        return rc;
+    BRR_CUDA(cudaEventRecord(c->ev[0], c->st));
+    if (c->blocked)
+        BRR_CUDA(launch_sweep_block(a, smem, c->st));
+    else
+        BRR_CUDA(launch_sweep(cf.form, c->kind, a, smem, c->st));
+    BRR_CUDA(cudaEventRecord(c->ev[1], c->st));
+    if (c->blocked)
+        BRR_CUDA(launch_block_finish(cf.M, c->d_chosen, a.beta_df, a.acum_df, c->d_beta, c->d_acum, c->st));
+
+    rc = sweep_finish(c, out);
+    if (rc)
+        return rc;
+    BRR_CUDA(cudaEventElapsedTime(sweep_ms, c->ev[0], c->ev[1]));
     return BRR_OK;
 }
 
@@ -540,6 +576,57 @@ int refresh_eps_impl(brr_ctx *c)
 
 }  // namespace
 
+// FP64 refresh when due, updateMu (dense src/DenseBayesRRmz.cpp:36-42, ragged
+// src/SparseBayesRRG.cpp:106-113), the per-marker draws and the permutation
+// (src/BayesRBase.cpp:196-198) of iteration it.
+int brr::iter_pre(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total)
+{
+    const brr_config &cf = c.cfg;
+    const int64_t N = cf.N, M = cf.M;
+    const double Nd = (double)N;
+    if (c.perm_next_it != it)
+        schedule_permutation(&c, it);
+    if (cf.form == BRR_FORM_FP32C && cf.refresh_every > 0 && c.sweeps > 0 && c.sweeps % cf.refresh_every == 0) {
+        const int rc = refresh_eps_impl(&c);
+        if (rc)
+            return rc;
+    }
+    const double old_mu = c.mu;
+    BRR_CUDA(launch_mu_prep(cf.form, N, old_mu, c.d_eps, c.d_eps_hi, c.d_eps_lo, c.d_part, kPartBlocks, c.st));
+    double mean, esum = 0.0;
+    if (cf.kind == BRR_KIND_DENSE) {
+        BRR_CUDA(cudaMemcpyAsync(c.h_part, c.d_part, sizeof(double) * kPartBlocks, cudaMemcpyDeviceToHost, c.st));
+        BRR_CUDA(cudaStreamSynchronize(c.st));
+        for (int b = 0; b < kPartBlocks; ++b)
+            esum += c.h_part[b];
+        mean = esum / Nd;
+    } else {
+        c.epsSum += old_mu * Nd;
+        mean = c.epsSum / Nd;
+    }
+    c.mu = mean + std::sqrt(c.sigmaE / Nd) * normal_mu(c.key(), it);
+    if (c.kind == BRR_KIND_RAGGED)
+        c.epsSum -= c.mu * Nd;
+    BRR_CUDA(launch_draws(cf.seed, cf.chain, it, M, c.d_u, c.d_z, c.st));
+    c.perm_future.wait();
+    std::memcpy(c.h_order, c.perm_next.data(), sizeof(uint32_t) * M);
+    BRR_CUDA(cudaMemcpyAsync(c.d_order, c.h_order, sizeof(uint32_t) * M, cudaMemcpyHostToDevice, c.st));
+    schedule_permutation(&c, it + 1);
+    mu_new = c.mu;
+    eps_total = esum - c.mu * Nd;
+    return BRR_OK;
+}
+
+// sigmaE, sigmaG and pi draws after the sweep (src/BayesRBase.cpp:237-247).
+int brr::iter_post(brr_ctx &c, const brr_sweep_out &so, uint32_t it)
+{
+    const int rc = post_sweep_draws(&c, so, it);
+    if (rc)
+        return rc;
+    c.iteration = it + 1;
+    return BRR_OK;
+}
+
 extern "C" {
 
 const char *brr_last_error(void) { return g_last_error.c_str(); }
@@ -599,19 +686,7 @@ int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
     // slices of individuals in 64-individual chunks (16 bytes of codes)
     x->chunks = (c.N + kChunk - 1) / kChunk;
     x->col_stride = x->chunks * 16;
-    int G = c.grid > 0 ? c.grid : x->sms;
-    G = (int)std::min<int64_t>(G, x->chunks);
-    x->G = G;
-    x->slice_lo.resize(G + 1);
-    int64_t maxch = 0;
-    for (int s = 0; s <= G; ++s) {
-        const int64_t ch = (int64_t)s * x->chunks / G;
-        x->slice_lo[s] = (int32_t)std::min<int64_t>(ch * kChunk, c.N);
-        if (s > 0)
-            maxch = std::max<int64_t>(maxch, ch - (int64_t)(s - 1) * x->chunks / G);
-    }
-    x->slice_max = (int)(maxch * kChunk);
-    x->slot_bytes = (int)(maxch * 16);
+    compute_slices(x, c.grid > 0 ? c.grid : x->sms);
     if (c.kind != BRR_KIND_DENSE && x->slice_max > 65536) {
         free_all(x);
         delete x;
@@ -716,46 +791,9 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
             c.has_missing = cnt[4 * j + 3] != 0;
     }
     if (c.kind == BRR_KIND_RAGGED) {
-        const int64_t MG1 = M * (int64_t)c.G + 1;
-        if (3 * MG1 > (int64_t)INT_MAX)
-            return fail(BRR_ERR_ARG, "ragged offset table too large for int32");
-        cudaFree(c.d_roff);
-        c.d_roff = nullptr;
-        if (dalloc(&c.d_roff, (size_t)(3 * MG1)))
-            return fail(BRR_ERR_OOM, "device allocation failed");
-        BRR_CUDA(cudaMemsetAsync(c.d_roff, 0, sizeof(int32_t) * 3 * MG1, c.st));
-        BRR_CUDA(launch_ragged_slice_counts(c.d_codes, c.col_stride, M, c.G, c.d_slice_lo, c.d_roff, c.st));
-        int32_t *tmp = nullptr;
-        if (dalloc(&tmp, (size_t)((MG1 + 1023) / 1024 + 1)))
-            return fail(BRR_ERR_OOM, "device allocation failed");
-        // totals must fit int32: the counts bound them by the genotype counts
-        std::vector<int64_t> cnt(M * 4);
-        BRR_CUDA(cudaMemcpyAsync(cnt.data(), c.d_counts, sizeof(int64_t) * M * 4, cudaMemcpyDeviceToHost, c.st));
-        BRR_CUDA(cudaStreamSynchronize(c.st));
-        int64_t tot[3] = {0, 0, 0};
-        for (int64_t j = 0; j < M; ++j) {
-            tot[0] += cnt[4 * j + 1];
-            tot[1] += cnt[4 * j + 2];
-            tot[2] += cnt[4 * j + 3];
-        }
-        for (int k = 0; k < 3; ++k) {
-            if (tot[k] > (int64_t)INT_MAX) {
-                cudaFree(tmp);
-                return fail(BRR_ERR_ARG, "ragged index list longer than 2^31 entries");
-            }
-            BRR_CUDA(launch_exclusive_scan_i32(c.d_roff + k * MG1, MG1, tmp, c.st));
-            cudaFree(c.d_ridx[k]);
-            c.d_ridx[k] = nullptr;
-            if (dalloc(&c.d_ridx[k], (size_t)tot[k] + 1)) {
-                cudaFree(tmp);
-                return fail(BRR_ERR_OOM, "device allocation failed");
-            }
-            c.rtot[k] = tot[k];
-        }
-        BRR_CUDA(cudaStreamSynchronize(c.st));
-        cudaFree(tmp);
-        BRR_CUDA(launch_ragged_fill(c.d_codes, c.col_stride, M, c.G, c.d_slice_lo, c.d_roff, c.d_roff + MG1,
-                                    c.d_roff + 2 * MG1, c.d_ridx[0], c.d_ridx[1], c.d_ridx[2], c.st));
+        const int rc = build_ragged_lists(c);
+        if (rc)
+            return rc;
     }
     BRR_CUDA(cudaStreamSynchronize(c.st));
     // the sweep kernel must fit one CTA per slice on the GPU at once
@@ -901,59 +939,27 @@ int brr_iterate(brr_ctx *ctx, int32_t n_iter)
     if (!ctx || !ctx->inited)
         return fail(BRR_ERR_ARG, "chain not initialised");
     brr_ctx &c = *ctx;
-    const brr_config &cf = c.cfg;
     BRR_CUDA(cudaSetDevice(c.dev));
-    const int64_t N = cf.N, M = cf.M;
-    const double Nd = (double)N;
     double sweep_total = 0.0;
     int64_t rounds_total = 0;
     std::memset(c.phase, 0, sizeof(c.phase));
     BRR_CUDA(cudaEventRecord(c.ev[2], c.st));
-    if (c.perm_next_it != c.iteration)
-        schedule_permutation(&c, c.iteration);
     for (int32_t n = 0; n < n_iter; ++n) {
         const uint32_t it = c.iteration;
-        if (cf.form == BRR_FORM_FP32C && cf.refresh_every > 0 && c.sweeps > 0 && c.sweeps % cf.refresh_every == 0) {
-            const int rc = refresh_eps_impl(&c);
-            if (rc)
-                return rc;
-        }
-        // updateMu (dense src/DenseBayesRRmz.cpp:36-42, ragged src/SparseBayesRRG.cpp:106-113)
-        const double old_mu = c.mu;
-        BRR_CUDA(launch_mu_prep(cf.form, N, old_mu, c.d_eps, c.d_eps_hi, c.d_eps_lo, c.d_part, kPartBlocks, c.st));
-        double mean, esum = 0.0;
-        if (cf.kind == BRR_KIND_DENSE) {
-            BRR_CUDA(cudaMemcpyAsync(c.h_part, c.d_part, sizeof(double) * kPartBlocks, cudaMemcpyDeviceToHost, c.st));
-            BRR_CUDA(cudaStreamSynchronize(c.st));
-            for (int b = 0; b < kPartBlocks; ++b)
-                esum += c.h_part[b];
-            mean = esum / Nd;
-        } else {
-            c.epsSum += old_mu * Nd;
-            mean = c.epsSum / Nd;
-        }
-        c.mu = mean + std::sqrt(c.sigmaE / Nd) * normal_mu(c.key(), it);
-        if (c.kind == BRR_KIND_RAGGED)
-            c.epsSum -= c.mu * Nd;
-
-        // per-marker draws and the permutation (src/BayesRBase.cpp:196-198)
-        BRR_CUDA(launch_draws(cf.seed, cf.chain, it, M, c.d_u, c.d_z, c.st));
-        c.perm_future.wait();
-        std::memcpy(c.h_order, c.perm_next.data(), sizeof(uint32_t) * M);
-        BRR_CUDA(cudaMemcpyAsync(c.d_order, c.h_order, sizeof(uint32_t) * M, cudaMemcpyHostToDevice, c.st));
-        schedule_permutation(&c, it + 1);
-
+        double mu_new = 0.0, eps_total = 0.0;
+        int rc = iter_pre(c, it, mu_new, eps_total);
+        if (rc)
+            return rc;
         brr_sweep_out so{};
         float ms = 0.f;
-        int rc = run_sweep(&c, c.mu, esum - c.mu * Nd, &so, &ms);
+        rc = run_sweep(&c, mu_new, eps_total, &so, &ms);
         if (rc)
             return rc;
         sweep_total += ms;
         rounds_total += so.rounds;
-        rc = post_sweep_draws(&c, so, it);
+        rc = iter_post(c, so, it);
         if (rc)
             return rc;
-        c.iteration = it + 1;
     }
     BRR_CUDA(cudaEventRecord(c.ev[3], c.st));
     BRR_CUDA(cudaEventSynchronize(c.ev[3]));

@@ -1,0 +1,117 @@
+// The single-chain context behind brr_ctx and the phases of one iteration that
+// the multi-instance driver (brr_multi_api.cu) reuses.
+#pragma once
+#include <future>
+#include <vector>
+
+#include "brr_device.cuh"
+#include "brr_internal.h"
+#include "brr_stream.h"
+
+struct brr_ctx {
+    brr_config cfg{};
+    int dev = 0;
+    int sms = 0;
+    cudaStream_t st = nullptr;
+    int G = 0;
+    int B = 16;
+    int64_t chunks = 0;
+    int64_t col_stride = 0;
+    int slice_max = 0;
+    int slot_bytes = 0;
+    std::vector<int32_t> slice_lo;
+    bool packed = false, pheno = false, inited = false;
+
+    // device buffers
+    int32_t *d_slice_lo = nullptr;
+    uint8_t *d_codes = nullptr;
+    int64_t *d_counts = nullptr;
+    double *d_table = nullptr;
+    double *d_scale = nullptr;
+    double *d_colsum = nullptr;
+    uint8_t *d_chosen = nullptr;
+    unsigned long long *d_vstat = nullptr;   // sweep statistics: counts, fixed-point square sums
+    int32_t *d_roff = nullptr;          // 3 x (M*G+1)
+    uint16_t *d_ridx[3] = {nullptr, nullptr, nullptr};
+    int64_t rtot[3] = {0, 0, 0};
+    int32_t *d_group = nullptr;
+    double *d_ystd = nullptr;
+    double *d_beta = nullptr;
+    int32_t *d_comp = nullptr;
+    double *d_acum = nullptr;
+    double *d_eps = nullptr;
+    float *d_eps_hi = nullptr, *d_eps_lo = nullptr;
+    uint32_t *d_order = nullptr;
+    double *d_u = nullptr, *d_z = nullptr;
+    brr::SweepRec *d_rec = nullptr;
+    unsigned long long *d_acc = nullptr;   // accumulators followed by the counter
+    double *d_gconst = nullptr;
+    int32_t *d_gK = nullptr;
+    double *d_stats = nullptr;
+    double *d_part = nullptr;
+    int *d_err = nullptr;
+    long long *d_rounds = nullptr;
+    long long *d_prof = nullptr;        // per-phase cycles of the last sweep (CTA 0)
+    uint32_t *d_nzj = nullptr;
+    double *d_nzb = nullptr;
+    double *d_gram = nullptr;           // blocked FP32C: packed marker Gram
+    double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries (8 blocks)
+    brr::BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
+    float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)
+    bool blocked = false;
+    bool has_missing = false;
+    int kind = BRR_KIND_DENSE;          // storage: dense codes, or ragged lists (Ragged and Eigen markers)
+    bool eigen = false;                 // Eigen sparse markers (BRR_KIND_EIGEN)
+    double gram_ms = 0.0;
+
+    // pinned host staging
+    uint32_t *h_order = nullptr;
+    double *h_stats = nullptr;
+    double *h_part = nullptr;
+
+    // host chain state
+    std::vector<int32_t> group;
+    std::vector<double> ystd;
+    double mu = 0.0, sigmaE = 0.0, epsSum = 0.0;
+    double sigmaG[BRR_MAX_GROUPS] = {};
+    double pi[BRR_MAX_GROUPS * BRR_MAX_K] = {};
+    uint32_t iteration = 0;
+    int64_t sweeps = 0;
+
+    // timing
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double last_sweep_ms = 0.0, last_total_ms = 0.0;
+    int64_t last_rounds = 0;
+    long long phase[16] = {};   // summed over the sweeps of the last call
+    uint64_t wait_limit_ns = 2000000000ull;
+    int phantom = 0;
+
+    // permutation prepared one iteration ahead on a host thread
+    std::future<void> perm_future;
+    std::vector<uint32_t> perm_next;
+    uint32_t perm_next_it = UINT32_MAX;
+
+    brr::StreamKey key() const { return brr::StreamKey{cfg.seed, cfg.chain}; }
+};
+
+namespace brr {
+
+constexpr size_t kAccWords = 8 * 8 * kMaxSpec * 4;
+constexpr size_t kCounterWords = 2 * 8 * 16;
+constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
+
+// Phases of one iteration of a chain (BayesRBase::runGibbs loop body,
+// src/BayesRBase.cpp:186-247), as brr_iterate runs them:
+//   iter_pre      FP64 refresh when due, updateMu, per-marker draws, permutation
+//   sweep_prepare sampler constants, records in sweep order, sweep arguments
+//   (the sweep kernel launch)
+//   sweep_finish  sweep statistics, residual sums, device status
+//   iter_post     sigmaE, sigmaG and pi draws, next iteration
+int iter_pre(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total);
+int sweep_prepare(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, size_t &smem);
+int sweep_finish(brr_ctx *c, brr_sweep_out *out);
+int iter_post(brr_ctx &c, const brr_sweep_out &so, uint32_t it);
+// New slicing (G CTAs) and, if B > 0, round width of a packed chain.
+int reslice(brr_ctx *c, int G, int B);
+
+}  // namespace brr

@@ -92,6 +92,7 @@ struct SweepArgs {
     float2 *acum_df;             // blocked FP32C sweep: acum per marker (hi, lo)
     int eigen;                   // ragged sweep: Eigen sparse markers (missing genotypes enter
                                  // the dot product at the marker's mean)
+    unsigned long long *t_out;   // optional [2]: global timer (ns) at the start and end of the sweep (CTA 0)
 };
 
 // ---------------------------------------------------------------------------
@@ -173,6 +174,17 @@ cudaError_t launch_batch_stats(int64_t M, int C, const int32_t *group, const int
 size_t batch_smem_bytes(int C, int kext, int G);
 int batch_max_ctas_per_sm(int C, int kext, size_t smem);
 cudaError_t launch_sweep_batch(const BatchArgs &a, int kmax, cudaStream_t st);
+
+// Several chains of different sizes in one cooperative launch (k_sweep_multi).
+constexpr int kMaxInstances = 32;
+struct MultiSweepArgs {
+    int n;                               // instances
+    int cta_start[kMaxInstances + 1];    // CTAs [cta_start[i], cta_start[i+1]) run instance i
+    int kind[kMaxInstances];             // sweep kind of each instance (dense or ragged lists)
+    SweepArgs inst[kMaxInstances];
+};
+int sweep_multi_max_ctas_per_sm(int form, int kmax, size_t smem);
+cudaError_t launch_sweep_multi(int form, int kmax, const MultiSweepArgs &m, size_t smem, cudaStream_t st);
 
 // Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).
 cudaError_t launch_pack_counts(const uint8_t *bed, int64_t N, int64_t M, uint8_t *codes,

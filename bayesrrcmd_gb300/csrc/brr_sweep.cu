@@ -252,8 +252,11 @@ __device__ __forceinline__ double lut_select(unsigned c, double l0, double l1, d
 }
 
 // --------------------------------------------------------------------------
+// The sweep of one chain over its G CTAs; sidx is this CTA's slice.  Run by
+// k_sweep (one chain per launch) and k_sweep_multi (several chains of
+// different sizes, each on its own group of CTAs, in one launch).
 template <int FORM, int KIND, int KM>
-__global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
+__device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_beta[kMaxSpec];
@@ -269,8 +272,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
     const int B = a.B;
     const int lpm = kThreads / B;
     const int R = 4 * B;
-    const int sidx = blockIdx.x;
     const int tid = threadIdx.x;
+    if (a.t_out && sidx == 0 && tid == 0)
+        a.t_out[0] = global_timer_ns();
     const int lo = a.slice_lo[sidx];
     const int ns = a.slice_lo[sidx + 1] - lo;
     const int nbytes = ((ns + kChunk - 1) / kChunk) * 16;
@@ -394,7 +398,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
     const Team tm = make_team(lpm);
     const int team = tid >> lpm_log2;
     const double Nm1 = (double)(a.N - 1);
-    const bool prof = a.prof != nullptr && blockIdx.x == 0 && tid == 0;
+    const bool prof = a.prof != nullptr && sidx == 0 && tid == 0;
     long long ph[6] = {0, 0, 0, 0, 0, 0};
     long long tp = prof ? clock64() : 0;
     auto mark = [&](int k) {
@@ -616,7 +620,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
 
         const int first = s_first;
         const int last = first < nb ? first : nb - 1;
-        if (blockIdx.x == 0) {
+        if (sidx == 0) {
             // outputs of the resolved markers, only from CTA 0
             if (tid <= last) {
                 const SweepRec &rc = ring_rec[(start + tid) & Rm];
@@ -756,11 +760,36 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
         }
         a.part[2 * sidx] = t1;
         a.part[2 * sidx + 1] = t2;
-        if (blockIdx.x == 0) {
+        if (sidx == 0) {
             a.stats_out[0] = s_scal[1];
             *a.rounds_out = r;
+            if (a.t_out)
+                a.t_out[1] = global_timer_ns();
         }
     }
+}
+
+template <int FORM, int KIND, int KM>
+__global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
+{
+    sweep_body<FORM, KIND, KM>(a, (int)blockIdx.x);
+}
+
+// Several independent chains of different sizes in one cooperative launch:
+// CTAs [cta_start[i], cta_start[i+1]) run instance i's sweep over its slices,
+// with its own barrier counter, records and residual; the instances share no
+// data, so one chain's progress never waits on another's.
+template <int FORM, int KM>
+__global__ void __launch_bounds__(kThreads, 1) k_sweep_multi(const __grid_constant__ MultiSweepArgs m)
+{
+    int i = 0;
+    while (i + 1 < m.n && (int)blockIdx.x >= m.cta_start[i + 1])
+        ++i;
+    const int sidx = (int)blockIdx.x - m.cta_start[i];
+    if (m.kind[i] == kKindDense)
+        sweep_body<FORM, kKindDense, KM>(m.inst[i], sidx);
+    else
+        sweep_body<FORM, kKindRagged, KM>(m.inst[i], sidx);
 }
 
 // Sweep statistics from the resolved markers (src/BayesRBase.cpp:353-355):
@@ -896,6 +925,48 @@ static cudaError_t launch_km(int form, int kind, const SweepArgs &a, size_t smem
 cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st)
 {
     return a.kmax <= 4 ? launch_km<4>(form, kind, a, smem, st) : launch_km<kMaxK>(form, kind, a, smem, st);
+}
+
+static const void *multi_fn(int form, int kmax)
+{
+    if (form == kFormFP64)
+        return kmax <= 4 ? (const void *)k_sweep_multi<kFormFP64, 4> : (const void *)k_sweep_multi<kFormFP64, kMaxK>;
+    return kmax <= 4 ? (const void *)k_sweep_multi<kFormFP32C, 4> : (const void *)k_sweep_multi<kFormFP32C, kMaxK>;
+}
+
+int sweep_multi_max_ctas_per_sm(int form, int kmax, size_t smem)
+{
+    const void *fn = multi_fn(form, kmax);
+    int n = 0;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// The cooperative launch goes through cudaLaunchKernelEx with the cooperative
+// attribute, which stream capture records as a cooperative graph node.
+cudaError_t launch_sweep_multi(int form, int kmax, const MultiSweepArgs &m, size_t smem, cudaStream_t st)
+{
+    const void *fn = multi_fn(form, kmax);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)m.cta_start[m.n]);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    MultiSweepArgs args = m;
+    void *params[] = {&args};
+    return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem)

@@ -66,6 +66,9 @@ EXPORTS = [
     "brr_batch_create", "brr_batch_destroy", "brr_batch_pack_bed", "brr_batch_pack_bed_device",
     "brr_batch_set_groups", "brr_batch_set_phenotypes", "brr_batch_init", "brr_batch_iterate",
     "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_get_geometry",
+    "brr_multi_create", "brr_multi_destroy", "brr_multi_pack_bed", "brr_multi_pack_bed_device",
+    "brr_multi_set_groups", "brr_multi_set_phenotype", "brr_multi_init", "brr_multi_tune", "brr_multi_iterate",
+    "brr_multi_get_state", "brr_multi_get_timing",
 ]
 
 
@@ -115,6 +118,18 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_batch_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_batch_set_wait_limit.argtypes = [P, C.c_uint64]
     lib.brr_batch_get_geometry.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    lib.brr_multi_create.argtypes = [C.POINTER(BrrConfig), C.c_int32, C.POINTER(P)]
+    lib.brr_multi_destroy.argtypes = [P]
+    lib.brr_multi_pack_bed.argtypes = [P, C.c_int32, C.POINTER(C.c_uint8), C.c_int64]
+    lib.brr_multi_pack_bed_device.argtypes = [P, C.c_int32, P, C.c_int64]
+    lib.brr_multi_set_groups.argtypes = [P, C.c_int32, C.POINTER(C.c_int32)]
+    lib.brr_multi_set_phenotype.argtypes = [P, C.c_int32, C.POINTER(C.c_float)]
+    lib.brr_multi_init.argtypes = [P]
+    lib.brr_multi_tune.argtypes = [P, C.c_int32]
+    lib.brr_multi_iterate.argtypes = [P, C.c_int32]
+    lib.brr_multi_get_state.argtypes = [P, C.c_int32, C.POINTER(BrrState)]
+    lib.brr_multi_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     for name in EXPORTS:
         if name != "brr_last_error":
             getattr(lib, name).restype = C.c_int
@@ -407,3 +422,89 @@ class Batch:
         g, sl, sm = C.c_int32(), C.c_int32(), C.c_int64()
         self._check(self.lib.brr_batch_get_geometry(self.h, C.byref(g), C.byref(sl), C.byref(sm)))
         return dict(ctas=g.value, slice=sl.value, smem=sm.value)
+
+
+class Multi:
+    """Independent regressions of different sizes (each its own ChainConfig:
+    N, M, kind, groups, S, seed, chain; one sweep form) swept together, one
+    cooperative launch per iteration, behind the C ABI."""
+
+    def __init__(self, cfgs: Sequence[ChainConfig], lib: Optional[C.CDLL] = None):
+        self.cfgs = list(cfgs)
+        self.n = len(self.cfgs)
+        self.lib = lib or load_library()
+        arr = (BrrConfig * self.n)(*[c.to_c() for c in self.cfgs])
+        self._arr = arr
+        h = C.c_void_p()
+        self._check(self.lib.brr_multi_create(arr, self.n, C.byref(h)))
+        self.h = h
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise BrrError(rc, self.lib.brr_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.brr_multi_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def pack_bed(self, i: int, bed_payload: np.ndarray):
+        a = np.ascontiguousarray(bed_payload, dtype=np.uint8)
+        self._check(self.lib.brr_multi_pack_bed(self.h, int(i), _ptr(a, C.c_uint8), a.size))
+
+    def pack_bed_device(self, i: int, dev_ptr: int, nbytes: int):
+        self._check(self.lib.brr_multi_pack_bed_device(self.h, int(i), C.c_void_p(dev_ptr), nbytes))
+
+    def set_groups(self, i: int, group: np.ndarray):
+        g = np.ascontiguousarray(group, dtype=np.int32)
+        self._check(self.lib.brr_multi_set_groups(self.h, int(i), _ptr(g, C.c_int32)))
+
+    def set_phenotype(self, i: int, y: np.ndarray):
+        a = np.ascontiguousarray(y, dtype=np.float32)
+        self._check(self.lib.brr_multi_set_phenotype(self.h, int(i), _ptr(a, C.c_float)))
+
+    def init(self):
+        self._check(self.lib.brr_multi_init(self.h))
+
+    def tune(self, rounds: int = 2):
+        self._check(self.lib.brr_multi_tune(self.h, int(rounds)))
+
+    def iterate(self, n: int = 1):
+        self._check(self.lib.brr_multi_iterate(self.h, int(n)))
+
+    def state(self, i: int) -> dict:
+        cfg = self.cfgs[i]
+        M, N = cfg.M, cfg.N
+        beta = np.zeros(M, np.float64)
+        comp = np.zeros(M, np.int32)
+        acum = np.zeros(M, np.float64)
+        eps = np.zeros(N, np.float64)
+        st = BrrState()
+        st.beta, st.comp, st.acum, st.eps = (_ptr(beta, C.c_double), _ptr(comp, C.c_int32),
+                                             _ptr(acum, C.c_double), _ptr(eps, C.c_double))
+        self._check(self.lib.brr_multi_get_state(self.h, int(i), C.byref(st)))
+        G = len(cfg.S)
+        return dict(beta=beta, comp=comp, acum=acum, eps=eps, mu=st.mu, sigmaE=st.sigmaE, epsSum=st.epsSum,
+                    sigmaG=np.array(st.sigmaG[:G]),
+                    pi=np.array(st.pi[:]).reshape(MAX_GROUPS, MAX_K)[:G].copy(), iteration=st.iteration)
+
+    def timing(self):
+        sw, tot = C.c_double(), C.c_double()
+        ctas = np.zeros(self.n, np.int32)
+        width = np.zeros(self.n, np.int32)
+        ms = np.zeros(self.n, np.float64)
+        self._check(self.lib.brr_multi_get_timing(self.h, C.byref(sw), C.byref(tot), _ptr(ctas, C.c_int32),
+                                                  _ptr(width, C.c_int32), _ptr(ms, C.c_double)))
+        return dict(sweep_ms=sw.value, total_ms=tot.value, ctas=ctas, width=width, inst_ms=ms)

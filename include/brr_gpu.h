@@ -231,6 +231,30 @@ int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns);
 /* CTAs of the sweep, individuals per slice and shared memory per CTA. */
 int brr_batch_get_geometry(brr_batch *b, int32_t *ctas, int32_t *slice, int64_t *smem_bytes);
 
+/* ---- Uneven batch: independent regressions of different sizes (C5 form) ----
+ * Up to 32 instances, each with its own configuration (N, M, kind, groups, S,
+ * seed, chain) but one sweep form and device, swept together: per iteration
+ * one cooperative launch runs every instance's sweep on its own group of CTAs.
+ * Per instance the chain is the single-chain one (the same draws and results
+ * as brr_iterate up to the order of floating-point sums).  brr_multi_tune runs
+ * 3 + rounds real iterations to choose each instance's round width and CTAs. */
+typedef struct brr_multi brr_multi;
+int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out);
+int brr_multi_destroy(brr_multi *m);
+int brr_multi_pack_bed(brr_multi *m, int32_t i, const uint8_t *bed, int64_t nbytes);
+int brr_multi_pack_bed_device(brr_multi *m, int32_t i, const uint8_t *d_bed, int64_t nbytes);
+int brr_multi_set_groups(brr_multi *m, int32_t i, const int32_t *group);
+int brr_multi_set_phenotype(brr_multi *m, int32_t i, const float *y);
+int brr_multi_init(brr_multi *m);
+int brr_multi_tune(brr_multi *m, int32_t rounds);
+int brr_multi_iterate(brr_multi *m, int32_t n_iter);
+int brr_multi_get_state(brr_multi *m, int32_t i, brr_state *st);
+/* Device time of the multi-instance sweeps and wall time of the last
+ * brr_multi_iterate call (ms); per instance (optional, n values each): CTAs,
+ * round width and the last sweep's time (ms). */
+int brr_multi_get_timing(brr_multi *m, double *sweep_ms, double *total_ms, int32_t *ctas, int32_t *width,
+                         double *inst_ms);
+
 /* Per-phase SM cycles of the sweeps of the last brr_iterate / brr_sweep call,
  * measured on the first CTA (the counterpart of the reference's per-column
  * timing log, src/BayesRBase.cpp:381-389), 16 values.  Restart sweep: [0] ring

@@ -92,3 +92,15 @@ def test_batch_without_gpu_is_a_device_error():
     h = C.c_void_p()
     cfg = gpu.ChainConfig(N=100, M=5).to_c()
     assert lib.brr_batch_create(C.byref(cfg), 64, C.byref(h)) == -8
+
+
+def test_multi_config_rejected_before_the_device():
+    lib = gpu.load_library()
+    h = C.c_void_p()
+    one = (gpu.BrrConfig * 1)(gpu.ChainConfig(N=100, M=5).to_c())
+    assert lib.brr_multi_create(one, 0, C.byref(h)) == -1
+    assert lib.brr_multi_create(one, 33, C.byref(h)) == -1
+    mixed = (gpu.BrrConfig * 2)(gpu.ChainConfig(N=100, M=5).to_c(),
+                                gpu.ChainConfig(N=100, M=5, form=gpu.FORM_FP32C).to_c())
+    assert lib.brr_multi_create(mixed, 2, C.byref(h)) == -1
+    assert b"sweep form" in lib.brr_last_error()
