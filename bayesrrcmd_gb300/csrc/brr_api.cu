@@ -1097,6 +1097,17 @@ int brr_synth_bed_device(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, do
     return BRR_OK;
 }
 
+int brr_synth_bed_device_beta(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, double a, double b, double p_lo,
+                              double p_hi, double missing)
+{
+    if (!d_bed || N < 2 || M < 1 || !(a > 0.0) || !(b > 0.0) || !(p_lo > 0.0) || !(p_hi <= 0.5) ||
+        !(p_lo <= p_hi) || !(missing >= 0.0) || !(missing < 0.5))
+        return fail(BRR_ERR_ARG, "invalid synthetic genotype parameters");
+    BRR_CUDA(launch_synth_bed(d_bed, N, M, seed, p_lo, p_hi, missing, 0, a, b));
+    BRR_CUDA(cudaDeviceSynchronize());
+    return BRR_OK;
+}
+
 int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, double *out)
 {
     if (!ctx || !ctx->packed || (n > 0 && (!idx || !b)) || !out || n < 0 || n > ctx->cfg.M)

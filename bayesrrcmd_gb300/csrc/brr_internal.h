@@ -214,7 +214,7 @@ cudaError_t launch_refresh(int form, int kind, int64_t N, const double *ystd, do
                            const uint32_t *nz_j, const double *nz_beta, int64_t n_nz, double *eps,
                            float *eps_hi, float *eps_lo, cudaStream_t st);
 cudaError_t launch_synth_bed(uint8_t *out, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
-                             double miss, cudaStream_t st);
+                             double miss, cudaStream_t st, double beta_a = 0.0, double beta_b = 0.0);
 cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st);
 size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a);
 cudaError_t noalloc_xbeta(int dev, cudaStream_t st, int kind, int64_t N, const uint8_t *codes, int64_t col_stride,

@@ -215,10 +215,10 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
         return bail(api_fail(BRR_ERR_DEVICE, "no usable device"));
     m->sms = prop.multiProcessorCount;
     m->smem_limit = prop.sharedMemPerBlockOptin - 4096;   // static shared memory of the multi kernel
-    // instances are created on one CTA each and sliced once all are known
+    // instances are created with a provisional slicing and sliced again once all are known
     for (int i = 0; i < n; ++i) {
         brr_config c = cfgs[i];
-        c.grid = 1;
+        c.grid = 0;
         c.gram = -1;
         brr_ctx *x = nullptr;
         const int rc = brr_ctx_create(&c, &x);
@@ -228,16 +228,26 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
         for (int g = 0; g < c.n_groups; ++g)
             m->kmax = std::max(m->kmax, c.K[g]);
     }
-    // first split of the SMs: at least what the slices need, the rest by N*M
+    // first split of the SMs: at least what the slices need, the rest by N*M;
+    // when the default round widths need more CTAs than there are SMs, every
+    // instance starts at the narrowest width (the smallest code ring)
     std::vector<double> work(n);
-    std::vector<int> mins(n), maxs(n), G;
-    for (int i = 0; i < n; ++i) {
-        const brr_ctx *c = m->inst[i];
-        work[i] = (double)c->cfg.N * (double)c->cfg.M;
-        mins[i] = min_ctas(c, c->B, m->smem_limit);
-        maxs[i] = (int)((c->cfg.N + kChunkInd - 1) / kChunkInd);
-        if (mins[i] == 0)
-            return bail(api_fail(BRR_ERR_ARG, "instance " + std::to_string(i) + " does not fit shared memory"));
+    std::vector<int> mins(n), maxs(n), G, widths(n);
+    const int narrowest = 8;
+    for (int pass = 0; pass < 2; ++pass) {
+        int need = 0;
+        for (int i = 0; i < n; ++i) {
+            const brr_ctx *c = m->inst[i];
+            widths[i] = pass == 0 ? c->B : narrowest;
+            work[i] = (double)c->cfg.N * (double)c->cfg.M;
+            mins[i] = min_ctas(c, widths[i], m->smem_limit);
+            maxs[i] = (int)((c->cfg.N + kChunkInd - 1) / kChunkInd);
+            if (mins[i] == 0)
+                return bail(api_fail(BRR_ERR_ARG, "instance " + std::to_string(i) + " does not fit shared memory"));
+            need += mins[i];
+        }
+        if (need <= m->sms)
+            break;
     }
     if (!allocate(work, mins, maxs, m->sms, G))
         return bail(api_fail(BRR_ERR_ARG, "the instances need more CTAs than the GPU has SMs"));
@@ -246,6 +256,7 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
         brr_config cf = c->cfg;
         brr_ctx_destroy(c);
         cf.grid = G[i];
+        cf.spec_width = widths[i];
         brr_ctx *x = nullptr;
         const int rc = brr_ctx_create(&cf, &x);
         m->inst[i] = x;
@@ -344,8 +355,7 @@ int brr_multi_tune(brr_multi *m, int32_t rounds)
         return api_fail(BRR_ERR_ARG, "instances not initialised");
     MULTI_CUDA(cudaSetDevice(m->dev));
     const int n = m->n;
-    const int cand[3] = {m->form == BRR_FORM_FP64 ? 8 : 16, m->form == BRR_FORM_FP64 ? 16 : 32,
-                         m->form == BRR_FORM_FP64 ? 32 : 64};
+    const int cand[3] = {8, 16, 32};
     std::vector<double> best(n, 1e300);
     std::vector<int> bestB(n);
     for (int i = 0; i < n; ++i)

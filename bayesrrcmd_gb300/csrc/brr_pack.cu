@@ -328,12 +328,28 @@ namespace brr {
 // Bernoulli(p_j) draws, missing at rate `miss`.  Every byte is a function of
 // (seed, j, byte index) through the same Philox stream as the sampler.
 __global__ void k_synth_bed(uint8_t *__restrict__ out, int64_t N, int64_t M, uint32_t seed, double p_lo,
-                            double p_hi, double miss)
+                            double p_hi, double miss, double beta_a, double beta_b)
 {
     const int64_t cb = (N + 3) >> 2;
     for (int64_t j = blockIdx.x; j < M; j += gridDim.x) {
-        const U4 pb = philox4x32_10((uint32_t)j, 0u, 9u, 0u, seed, 0x5EEDu);
-        const float p = (float)(p_lo + (p_hi - p_lo) * u53(pb.x, pb.y));
+        float p;
+        if (beta_a > 0.0) {
+            // p ~ Beta(a, b) = X / (X + Y), X ~ Gamma(a), Y ~ Gamma(b), clipped to [p_lo, p_hi]
+            __shared__ double s_p;
+            if (threadIdx.x == 0) {
+                double x = 1.0, y = 1.0;
+                const StreamKey k{seed, 0x5EEDu};
+                gamma_draw(k, (uint32_t)j, 12u, 0u, beta_a, &x);
+                gamma_draw(k, (uint32_t)j, 12u, 1u, beta_b, &y);
+                s_p = fmin(fmax(x / (x + y), p_lo), p_hi);
+            }
+            __syncthreads();
+            p = (float)s_p;
+            __syncthreads();
+        } else {
+            const U4 pb = philox4x32_10((uint32_t)j, 0u, 9u, 0u, seed, 0x5EEDu);
+            p = (float)(p_lo + (p_hi - p_lo) * u53(pb.x, pb.y));
+        }
         const uint32_t t1 = (uint32_t)fminf(4294967040.f, p * 4294967296.f);
         const uint32_t tm = (uint32_t)fminf(4294967040.f, (float)miss * 4294967296.f);
         for (int64_t b = threadIdx.x; b < cb; b += blockDim.x) {
@@ -367,10 +383,10 @@ __global__ void k_synth_bed(uint8_t *__restrict__ out, int64_t N, int64_t M, uin
 }
 
 cudaError_t launch_synth_bed(uint8_t *out, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
-                             double miss, cudaStream_t st)
+                             double miss, cudaStream_t st, double beta_a, double beta_b)
 {
     const int blocks = (int)imin64(M, 152 * 32);
-    k_synth_bed<<<blocks, kThreads, 0, st>>>(out, N, M, seed, p_lo, p_hi, miss);
+    k_synth_bed<<<blocks, kThreads, 0, st>>>(out, N, M, seed, p_lo, p_hi, miss, beta_a, beta_b);
     return cudaGetLastError();
 }
 

@@ -68,7 +68,7 @@ EXPORTS = [
     "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_get_geometry",
     "brr_multi_create", "brr_multi_destroy", "brr_multi_pack_bed", "brr_multi_pack_bed_device",
     "brr_multi_set_groups", "brr_multi_set_phenotype", "brr_multi_init", "brr_multi_tune", "brr_multi_iterate",
-    "brr_multi_get_state", "brr_multi_get_timing",
+    "brr_multi_get_state", "brr_multi_get_timing", "brr_synth_bed_device_beta",
 ]
 
 
@@ -106,6 +106,8 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
     lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
+    lib.brr_synth_bed_device_beta.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double,
+                                              C.c_double, C.c_double, C.c_double]
     lib.brr_batch_create.argtypes = [C.POINTER(BrrConfig), C.c_int32, C.POINTER(P)]
     lib.brr_batch_destroy.argtypes = [P]
     lib.brr_batch_pack_bed.argtypes = [P, C.POINTER(C.c_uint8), C.c_int64]
@@ -143,6 +145,15 @@ def synth_bed_device(dev_ptr: int, N: int, M: int, seed: int, p_lo: float, p_hi:
     """Fill a device buffer of M*ceil(N/4) bytes with a seeded synthetic BED payload."""
     lib = lib or load_library()
     rc = lib.brr_synth_bed_device(C.c_void_p(dev_ptr), N, M, seed & 0xFFFFFFFF, p_lo, p_hi, missing)
+    if rc != 0:
+        raise BrrError(rc, lib.brr_last_error().decode())
+
+
+def synth_bed_device_beta(dev_ptr: int, N: int, M: int, seed: int, a: float, b: float, p_lo: float, p_hi: float,
+                          missing: float = 0.0, lib: Optional[C.CDLL] = None):
+    """As synth_bed_device with allele frequencies ~ Beta(a, b) clipped to [p_lo, p_hi]."""
+    lib = lib or load_library()
+    rc = lib.brr_synth_bed_device_beta(C.c_void_p(dev_ptr), N, M, seed & 0xFFFFFFFF, a, b, p_lo, p_hi, missing)
     if rc != 0:
         raise BrrError(rc, lib.brr_last_error().decode())
 

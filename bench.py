@@ -264,6 +264,79 @@ def run_batched(lib, gpu, torch, device, steps, warmup):
                 cycles=(cyc / steps / nblocks).tolist(), geometry=geo)
 
 
+# Uneven batch: 32 independent regressions of different sizes in one launch per
+# iteration; N log-uniform in [1,000, 200,000], M log-uniform in [5,000, 500,000],
+# allele frequencies Beta(0.5, 2) clipped to [0.001, 0.5], 1 % missing, h2 ~ U(0.2, 0.6),
+# 0.5 % causal markers; the FP32C restart form with the FP64 refresh every 50 sweeps.
+U_N = (1_000, 200_000)
+U_M = (5_000, 500_000)
+U_WORKLOAD = ("uneven batch of 32 regressions in one launch per iteration: N log-U[1k, 200k], M log-U[5k, 500k], "
+              "p~Beta(0.5,2) clipped [0.001,0.5], 1% missing, h2~U(0.2,0.6), 0.5% causal, dense or ragged per "
+              "instance, FP32C restart form, S=0.01,0.001,0.0001")
+
+
+def uneven_instances(seed, scale=1.0):
+    rng = np.random.default_rng(seed)
+    n = 32
+    N = np.exp(rng.uniform(np.log(U_N[0]), np.log(U_N[1]), n)) * scale
+    M = np.exp(rng.uniform(np.log(U_M[0]), np.log(U_M[1]), n)) * scale
+    N = np.maximum(N.astype(np.int64), 256)
+    M = np.maximum(M.astype(np.int64), 200)
+    h2 = rng.uniform(0.2, 0.6, n)
+    return N, M, h2
+
+
+def run_uneven(lib, gpu, torch, device, steps, tune_rounds, scale=1.0):
+    """Aggregate marker-updates/s of 32 regressions of different sizes swept
+    together (one cooperative launch per iteration, CTAs and round widths from
+    the autotuner)."""
+    S = [[0.01, 0.001, 0.0001]]
+    seed = SEED + 11
+    N, M, h2 = uneven_instances(seed, scale)
+    # dense or ragged by storage: ragged index lists take 4 bytes per non-zero
+    # genotype, dense columns N/4 bytes; with p ~ Beta(0.5, 2) clipped to
+    # [0.001, 0.5] the expected non-zero fraction E[1 - (1 - p)^2] decides
+    ps = np.clip(np.random.default_rng(seed + 1).beta(0.5, 2.0, 200_000), 0.001, 0.5)
+    nz = float(np.mean(1.0 - (1.0 - ps) ** 2))
+    kinds = [gpu.KIND_RAGGED if 4.0 * nz < 0.25 else gpu.KIND_DENSE for _ in range(len(N))]
+    cfgs = [gpu.ChainConfig(N=int(N[i]), M=int(M[i]), kind=kinds[i], form=gpu.FORM_FP32C, S=S, seed=seed,
+                            chain=i, refresh_every=REFRESH, device=device) for i in range(len(N))]
+    mm = gpu.Multi(cfgs, lib=lib)
+    rng = np.random.default_rng(seed + 2)
+    for i in range(len(N)):
+        n_i, m_i = int(N[i]), int(M[i])
+        d_bed = torch.empty(m_i * ((n_i + 3) // 4), dtype=torch.uint8, device=device)
+        gpu.synth_bed_device_beta(d_bed.data_ptr(), n_i, m_i, seed + i, 0.5, 2.0, 0.001, 0.5, 0.01, lib=lib)
+        probe = gpu.Chain(gpu.ChainConfig(N=n_i, M=m_i, S=S, device=device), lib=lib)
+        probe.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+        n_c = max(1, int(0.005 * m_i))
+        causal = np.sort(rng.choice(m_i, n_c, replace=False)).astype(np.uint32)
+        b = rng.normal(0.0, np.sqrt(h2[i] / n_c), n_c)
+        y = (probe.xbeta(causal, b) + rng.normal(0.0, np.sqrt(1.0 - h2[i]), n_i)).astype(np.float32)
+        probe.close()
+        mm.pack_bed_device(i, d_bed.data_ptr(), d_bed.numel())
+        mm.set_phenotype(i, y)
+        del d_bed
+    torch.cuda.empty_cache()
+    mm.init()
+    t0 = mm.timing()
+    mm.tune(tune_rounds)
+    tuned = mm.timing()
+    mm.iterate(steps)
+    t = mm.timing()
+    mm.close()
+    total_m = int(M.sum())
+    inst = t["inst_ms"]
+    return dict(rate=total_m * steps / (t["total_ms"] / 1e3), ms_per_step=t["total_ms"] / steps,
+                sweep_ms=t["sweep_ms"] / steps, instances=len(N), total_markers=total_m,
+                total_genotypes=float((N.astype(float) * M.astype(float)).sum()),
+                kinds={"dense": kinds.count(gpu.KIND_DENSE), "ragged": kinds.count(gpu.KIND_RAGGED)},
+                ctas_first=t0["ctas"].tolist(), ctas=t["ctas"].tolist(), widths=t["width"].tolist(),
+                inst_ms=[round(x, 3) for x in inst.tolist()],
+                balance_max_over_mean=float(inst.max() / max(inst.mean(), 1e-9)),
+                N=N.tolist(), M=M.tolist())
+
+
 def numpy_sample(m_sample, seed):
     """A CPU-generated sample of the workload: N individuals, m_sample markers."""
     from bayesrrcmd_gb300 import plink
@@ -317,6 +390,9 @@ def main():
     ap.add_argument("--batch-only", action="store_true",
                     help="only the batching-form leg (profiling); --batch-markers sets its M")
     ap.add_argument("--batch-markers", type=int, default=None)
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (32 regressions) measurement")
+    ap.add_argument("--uneven-only", action="store_true", help="only the uneven-batch leg; --uneven-scale shrinks it")
+    ap.add_argument("--uneven-scale", type=float, default=1.0)
     ap.add_argument("--small", action="store_true",
                     help="profiling case: N=100,000 x M=8,192 (200 MB of codes, above L2), same settings")
     args = ap.parse_args()
@@ -354,6 +430,11 @@ def main():
     lib = gpu.load_library()
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
+    if args.uneven_only:
+        uu = run_uneven(lib, gpu, torch, device, args.steps, 2, args.uneven_scale)
+        if rank == 0:
+            print(json.dumps({"uneven_only": True, **uu}))
+        return
     if args.batch_only:
         global B_M
         if args.batch_markers:
@@ -416,6 +497,18 @@ def main():
                                                  bb["cycles"])),
             "geometry": bb["geometry"],
         }
+    uneven = None
+    if not args.no_uneven and not args.small:
+        usteps = int(os.environ.get("BRR_UNEVEN_STEPS", "3"))
+        uu = run_uneven(lib, gpu, torch, device, usteps, 2)
+        uneven = {"workload": U_WORKLOAD, "value": uu["rate"] * world,
+                  "unit": "marker-updates/s (all instances)", "steps": usteps, "ms_per_step": uu["ms_per_step"],
+                  "sweep_ms": uu["sweep_ms"], "instances": uu["instances"], "total_markers": uu["total_markers"],
+                  "total_genotypes": uu["total_genotypes"], "kinds": uu["kinds"],
+                  "autotuner": {"ctas_initial": uu["ctas_first"], "ctas": uu["ctas"], "round_widths": uu["widths"],
+                                "instance_sweep_ms": uu["inst_ms"],
+                                "slowest_over_mean": uu["balance_max_over_mean"]},
+                  "sizes": {"N": uu["N"], "M": uu["M"]}}
     if rank != 0:
         return
     cpu = None
@@ -470,6 +563,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": e2e,
         "batched": batched,
+        "uneven": uneven,
     }
     print(json.dumps(line))
 

@@ -173,6 +173,9 @@ int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, dou
  * source for benchmarks at sizes where host generation is too slow. */
 int brr_synth_bed_device(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
                          double missing);
+/* The same with allele frequencies p_j ~ Beta(a, b) clipped to [p_lo, p_hi]. */
+int brr_synth_bed_device_beta(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, double a, double b, double p_lo,
+                              double p_hi, double missing);
 
 /* Allocation-free genetic values.  No counterpart in the reference: it serves
  * callers that cannot allocate device memory when they need the values (a
