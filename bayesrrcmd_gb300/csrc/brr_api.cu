@@ -121,6 +121,10 @@ void free_all(brr_ctx *c)
     cudaFreeHost(c->h_order);
     cudaFreeHost(c->h_stats);
     cudaFreeHost(c->h_part);
+    cudaFreeHost(c->h_gc);
+    cudaFreeHost(c->h_gK);
+    cudaFreeHost(c->h_vstat);
+    cudaFreeHost(c->h_misc);
     for (auto &e : c->ev)
         if (e)
             cudaEventDestroy(e);
@@ -302,25 +306,41 @@ int brr::reslice(brr_ctx *c, int G, int B)
     return BRR_OK;
 }
 
-// Sampler constants, records in sweep order and the sweep arguments for the
-// order in d_order and the draws in d_u/d_z.
-int brr::sweep_prepare(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, size_t &smem)
+// The sampler constants of the current sigmaE, sigmaG and pi into the pinned
+// staging the sweep's inputs are copied from.
+void brr::sweep_stage(brr_ctx *c)
 {
-    const brr_config &cf = c->cfg;
     std::vector<double> gc;
     std::vector<int32_t> gK;
     group_constants(c, gc, gK);
-    BRR_CUDA(cudaMemcpyAsync(c->d_gconst, gc.data(), sizeof(double) * gc.size(), cudaMemcpyHostToDevice, c->st));
-    BRR_CUDA(cudaMemcpyAsync(c->d_gK, gK.data(), sizeof(int32_t) * gK.size(), cudaMemcpyHostToDevice, c->st));
+    std::memcpy(c->h_gc, gc.data(), sizeof(double) * gc.size());
+    std::memcpy(c->h_gK, gK.data(), sizeof(int32_t) * gK.size());
+}
+
+// Device work before the sweep, on stream st: the staged constants, the records
+// in sweep order (order in d_order, draws in d_u/d_z), cleared accumulators.
+int brr::sweep_enqueue_inputs(brr_ctx *c, double eps_total, cudaStream_t st)
+{
+    const brr_config &cf = c->cfg;
+    const size_t ng = (size_t)cf.n_groups;
+    BRR_CUDA(cudaMemcpyAsync(c->d_gconst, c->h_gc, sizeof(double) * ng * kMaxK * 4, cudaMemcpyHostToDevice, st));
+    BRR_CUDA(cudaMemcpyAsync(c->d_gK, c->h_gK, sizeof(int32_t) * ng, cudaMemcpyHostToDevice, st));
     if (c->blocked)
         BRR_CUDA(launch_gather_block(c->d_order, cf.M, cf.N, c->d_table, c->d_scale, c->d_beta, c->d_u, c->d_z,
-                                     c->d_group, eps_total, c->d_brec, c->st));
+                                     c->d_group, eps_total, c->d_brec, st));
     else
         BRR_CUDA(launch_gather(cf.form, c->kind, c->d_order, cf.M, c->d_table, c->d_scale, c->d_beta, c->d_u,
-                               c->d_z, c->d_group, c->d_colsum, c->d_rec, c->st));
-    BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + kCounterWords), c->st));
-    BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+                               c->d_z, c->d_group, c->d_colsum, c->d_rec, st));
+    BRR_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * (kAccWords + kCounterWords), st));
+    BRR_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
+    BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 16, st));
+    return BRR_OK;
+}
 
+// The sweep kernel's arguments and shared memory.
+void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, size_t &smem)
+{
+    const brr_config &cf = c->cfg;
     a = SweepArgs{};
     a.N = cf.N;
     a.M = cf.M;
@@ -369,32 +389,55 @@ int brr::sweep_prepare(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a
     a.brec = c->d_brec;
     a.beta_df = c->d_bdf;
     a.acum_df = c->d_bdf ? c->d_bdf + cf.M : nullptr;
-    BRR_CUDA(cudaMemsetAsync(c->d_prof, 0, sizeof(long long) * 16, c->st));
     smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, c->kind, a);
+}
+
+// Sampler constants, records in sweep order and the sweep arguments for the
+// order in d_order and the draws in d_u/d_z.
+int brr::sweep_prepare(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, size_t &smem)
+{
+    sweep_stage(c);
+    const int rc = sweep_enqueue_inputs(c, eps_total, c->st);
+    if (rc)
+        return rc;
+    sweep_args(c, mu_new, eps_total, a, smem);
     return BRR_OK;
 }
 
 
-// Statistics of the sweep just run: component counts, squared betas, residual
-// sums, rounds, device status.
-int brr::sweep_finish(brr_ctx *c, brr_sweep_out *out)
+// Device work after the sweep, on stream st: the statistics kernel and the
+// read-back of counts, square sums, residual sums, rounds, cycles and status
+// into pinned staging.
+int brr::sweep_enqueue_outputs(brr_ctx *c, cudaStream_t st)
 {
     const brr_config &cf = c->cfg;
     const int ng = cf.n_groups;
-    BRR_CUDA(launch_sweep_stats(cf.M, c->d_group, c->d_comp, c->d_chosen, c->d_beta, ng, c->d_vstat, c->st));
+    BRR_CUDA(launch_sweep_stats(cf.M, c->d_group, c->d_comp, c->d_chosen, c->d_beta, ng, c->d_vstat, st));
     const size_t nv = (size_t)ng * kMaxK + 2 * ng;
-    std::vector<unsigned long long> vstat(nv);
-    BRR_CUDA(cudaMemcpyAsync(vstat.data(), c->d_vstat, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, c->st));
-    BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double), cudaMemcpyDeviceToHost, c->st));
-    BRR_CUDA(cudaMemcpyAsync(c->h_part, c->d_part, sizeof(double) * 2 * c->G, cudaMemcpyDeviceToHost, c->st));
-    long long rounds = 0, prof[16] = {};
-    BRR_CUDA(cudaMemcpyAsync(&rounds, c->d_rounds, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
-    BRR_CUDA(cudaMemcpyAsync(prof, c->d_prof, sizeof(prof), cudaMemcpyDeviceToHost, c->st));
-    const int rc = check_device_status(c);
-    if (rc)
-        return rc;
+    BRR_CUDA(cudaMemcpyAsync(c->h_vstat, c->d_vstat, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, st));
+    BRR_CUDA(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(double), cudaMemcpyDeviceToHost, st));
+    BRR_CUDA(cudaMemcpyAsync(c->h_part, c->d_part, sizeof(double) * 2 * c->G, cudaMemcpyDeviceToHost, st));
+    BRR_CUDA(cudaMemcpyAsync(c->h_misc, c->d_rounds, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    BRR_CUDA(cudaMemcpyAsync(c->h_misc + 1, c->d_prof, sizeof(long long) * 16, cudaMemcpyDeviceToHost, st));
+    BRR_CUDA(cudaMemcpyAsync(c->h_misc + 17, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    return BRR_OK;
+}
+
+// Statistics of the sweep just run from the staging, once the stream is synchronised.
+int brr::sweep_collect(brr_ctx *c, brr_sweep_out *out)
+{
+    const brr_config &cf = c->cfg;
+    const int ng = cf.n_groups;
+    int h = 0;
+    std::memcpy(&h, c->h_misc + 17, sizeof(int));
+    if (h == kDevTimeout)
+        return fail(BRR_ERR_TIMEOUT, "a grid barrier of the sweep exceeded its wait limit");
+    if (h == kDevRange)
+        return fail(BRR_ERR_RANGE, "a partial dot product left the fixed-point exchange range");
+    const unsigned long long *vstat = c->h_vstat;
+    const long long rounds = c->h_misc[0];
     for (int k = 0; k < 16; ++k)
-        c->phase[k] += prof[k];
+        c->phase[k] += c->h_misc[1 + k];
 
     for (int g = 0; g < ng; ++g)
         for (int k = 0; k < BRR_MAX_K; ++k)
@@ -413,6 +456,17 @@ int brr::sweep_finish(brr_ctx *c, brr_sweep_out *out)
         c->epsSum = c->h_stats[0];
     c->sweeps += 1;
     return BRR_OK;
+}
+
+// Statistics of the sweep just run: component counts, squared betas, residual
+// sums, rounds, device status.
+int brr::sweep_finish(brr_ctx *c, brr_sweep_out *out)
+{
+    int rc = sweep_enqueue_outputs(c, c->st);
+    if (rc)
+        return rc;
+    BRR_CUDA(cudaStreamSynchronize(c->st));
+    return sweep_collect(c, out);
 }
 
 namespace {
@@ -581,9 +635,20 @@ int refresh_eps_impl(brr_ctx *c)
 // (src/BayesRBase.cpp:196-198) of iteration it.
 int brr::iter_pre(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total)
 {
+    int rc = iter_pre_dev(c, it);
+    if (rc)
+        return rc;
+    BRR_CUDA(cudaStreamSynchronize(c.st));
+    rc = iter_pre_host(c, it, mu_new, eps_total);
+    if (rc)
+        return rc;
+    return iter_enqueue_draws(c, it, c.st);
+}
+
+// Device part of updateMu: FP64 refresh when due, the residual total into h_part.
+int brr::iter_pre_dev(brr_ctx &c, uint32_t it)
+{
     const brr_config &cf = c.cfg;
-    const int64_t N = cf.N, M = cf.M;
-    const double Nd = (double)N;
     if (c.perm_next_it != it)
         schedule_permutation(&c, it);
     if (cf.form == BRR_FORM_FP32C && cf.refresh_every > 0 && c.sweeps > 0 && c.sweeps % cf.refresh_every == 0) {
@@ -591,12 +656,22 @@ int brr::iter_pre(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total)
         if (rc)
             return rc;
     }
+    BRR_CUDA(launch_mu_prep(cf.form, cf.N, c.mu, c.d_eps, c.d_eps_hi, c.d_eps_lo, c.d_part, kPartBlocks, c.st));
+    if (cf.kind == BRR_KIND_DENSE)
+        BRR_CUDA(cudaMemcpyAsync(c.h_part, c.d_part, sizeof(double) * kPartBlocks, cudaMemcpyDeviceToHost, c.st));
+    return BRR_OK;
+}
+
+// Host part of updateMu (after the stream is synchronised) and the sweep order
+// of iteration it into the pinned order buffer.
+int brr::iter_pre_host(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total)
+{
+    const brr_config &cf = c.cfg;
+    const int64_t N = cf.N, M = cf.M;
+    const double Nd = (double)N;
     const double old_mu = c.mu;
-    BRR_CUDA(launch_mu_prep(cf.form, N, old_mu, c.d_eps, c.d_eps_hi, c.d_eps_lo, c.d_part, kPartBlocks, c.st));
     double mean, esum = 0.0;
     if (cf.kind == BRR_KIND_DENSE) {
-        BRR_CUDA(cudaMemcpyAsync(c.h_part, c.d_part, sizeof(double) * kPartBlocks, cudaMemcpyDeviceToHost, c.st));
-        BRR_CUDA(cudaStreamSynchronize(c.st));
         for (int b = 0; b < kPartBlocks; ++b)
             esum += c.h_part[b];
         mean = esum / Nd;
@@ -607,13 +682,21 @@ int brr::iter_pre(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total)
     c.mu = mean + std::sqrt(c.sigmaE / Nd) * normal_mu(c.key(), it);
     if (c.kind == BRR_KIND_RAGGED)
         c.epsSum -= c.mu * Nd;
-    BRR_CUDA(launch_draws(cf.seed, cf.chain, it, M, c.d_u, c.d_z, c.st));
     c.perm_future.wait();
     std::memcpy(c.h_order, c.perm_next.data(), sizeof(uint32_t) * M);
-    BRR_CUDA(cudaMemcpyAsync(c.d_order, c.h_order, sizeof(uint32_t) * M, cudaMemcpyHostToDevice, c.st));
     schedule_permutation(&c, it + 1);
     mu_new = c.mu;
     eps_total = esum - c.mu * Nd;
+    return BRR_OK;
+}
+
+// Device work of the draws, on stream st: the per-marker draws of iteration it
+// and the sweep order from the pinned buffer.
+int brr::iter_enqueue_draws(brr_ctx &c, uint32_t it, cudaStream_t st)
+{
+    const brr_config &cf = c.cfg;
+    BRR_CUDA(launch_draws(cf.seed, cf.chain, it, cf.M, c.d_u, c.d_z, st));
+    BRR_CUDA(cudaMemcpyAsync(c.d_order, c.h_order, sizeof(uint32_t) * cf.M, cudaMemcpyHostToDevice, st));
     return BRR_OK;
 }
 
@@ -757,7 +840,12 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
         if (cudaMallocHost((void **)&c.h_order, sizeof(uint32_t) * M) != cudaSuccess ||
             cudaMallocHost((void **)&c.h_stats, sizeof(double) * ((size_t)cf.n_groups * kMaxK + cf.n_groups + 1)) !=
                 cudaSuccess ||
-            cudaMallocHost((void **)&c.h_part, sizeof(double) * std::max(2 * c.G, kPartBlocks)) != cudaSuccess)
+            cudaMallocHost((void **)&c.h_part, sizeof(double) * std::max(2 * c.G, kPartBlocks)) != cudaSuccess ||
+            cudaMallocHost((void **)&c.h_gc, sizeof(double) * (size_t)cf.n_groups * kMaxK * 4) != cudaSuccess ||
+            cudaMallocHost((void **)&c.h_gK, sizeof(int32_t) * (size_t)cf.n_groups) != cudaSuccess ||
+            cudaMallocHost((void **)&c.h_vstat, sizeof(unsigned long long) * ((size_t)cf.n_groups * kMaxK + 2 * cf.n_groups)) !=
+                cudaSuccess ||
+            cudaMallocHost((void **)&c.h_misc, sizeof(long long) * 18) != cudaSuccess)
             return fail(BRR_ERR_OOM, "pinned host allocation failed");
         BRR_CUDA(cudaMemset(c.d_group, 0, sizeof(int32_t) * M));
         c.group.assign(M, 0);

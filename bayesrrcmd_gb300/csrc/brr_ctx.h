@@ -68,6 +68,10 @@ struct brr_ctx {
     uint32_t *h_order = nullptr;
     double *h_stats = nullptr;
     double *h_part = nullptr;
+    double *h_gc = nullptr;               // sampler constants for the next sweep
+    int32_t *h_gK = nullptr;
+    unsigned long long *h_vstat = nullptr;   // sweep statistics read back
+    long long *h_misc = nullptr;          // [0] rounds, [1..16] cycles, [17] device status
 
     // host chain state
     std::vector<int32_t> group;
@@ -103,13 +107,26 @@ constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
 // Phases of one iteration of a chain (BayesRBase::runGibbs loop body,
 // src/BayesRBase.cpp:186-247), as brr_iterate runs them:
 //   iter_pre      FP64 refresh when due, updateMu, per-marker draws, permutation
+//                 (= iter_pre_dev, synchronise, iter_pre_host, iter_enqueue_draws)
 //   sweep_prepare sampler constants, records in sweep order, sweep arguments
+//                 (= sweep_stage, sweep_enqueue_inputs, sweep_args)
 //   (the sweep kernel launch)
 //   sweep_finish  sweep statistics, residual sums, device status
+//                 (= sweep_enqueue_outputs, synchronise, sweep_collect)
 //   iter_post     sigmaE, sigmaG and pi draws, next iteration
+// The enqueue steps do device work only, from and to pinned staging, on the
+// given stream, so that the multi-instance driver can capture them in a graph.
 int iter_pre(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total);
+int iter_pre_dev(brr_ctx &c, uint32_t it);
+int iter_pre_host(brr_ctx &c, uint32_t it, double &mu_new, double &eps_total);
+int iter_enqueue_draws(brr_ctx &c, uint32_t it, cudaStream_t st);
 int sweep_prepare(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, size_t &smem);
+void sweep_stage(brr_ctx *c);
+int sweep_enqueue_inputs(brr_ctx *c, double eps_total, cudaStream_t st);
+void sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, size_t &smem);
 int sweep_finish(brr_ctx *c, brr_sweep_out *out);
+int sweep_enqueue_outputs(brr_ctx *c, cudaStream_t st);
+int sweep_collect(brr_ctx *c, brr_sweep_out *out);
 int iter_post(brr_ctx &c, const brr_sweep_out &so, uint32_t it);
 // New slicing (G CTAs) and, if B > 0, round width of a packed chain.
 int reslice(brr_ctx *c, int G, int B);

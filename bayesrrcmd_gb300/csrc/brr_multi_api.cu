@@ -49,6 +49,8 @@ struct brr_multi {
     std::vector<cudaEvent_t> ready;
     std::vector<brr_ctx *> inst;
     unsigned long long *d_t = nullptr;       // [n][2] device timer at sweep start and end
+    unsigned long long *h_t = nullptr;       // pinned copy
+    cudaGraphExec_t exec = nullptr;          // the iteration's graph, updated each iteration
     std::vector<double> inst_ms;             // last sweep time of each instance
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
     bool inited = false;
@@ -69,6 +71,9 @@ void free_multi(brr_multi *m)
     if (m->done)
         cudaEventDestroy(m->done);
     cudaFree(m->d_t);
+    cudaFreeHost(m->h_t);
+    if (m->exec)
+        cudaGraphExecDestroy(m->exec);
     if (m->st)
         cudaStreamDestroy(m->st);
 }
@@ -127,59 +132,112 @@ bool allocate(const std::vector<double> &work, const std::vector<int> &mins, con
     return true;
 }
 
-// One iteration of every instance with one launch of the multi-instance sweep.
+// Ends a stream capture that failed part way, so the stream is usable again.
+int abandon_capture(brr_multi *m, int rc)
+{
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(m->st, &g);
+    if (g)
+        cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc;
+}
+
+// One iteration of every instance: the host parts of updateMu, then one CUDA
+// graph holding all instances' draws, sweep orders, constants and records,
+// the one launch of the multi-instance sweep, and all instances' statistics
+// and read-backs; the graph is captured each iteration (the launch arguments
+// carry the new updateMu shifts) and updated in place.
 int run_iteration(brr_multi *m)
 {
     const int n = m->n;
     std::vector<SweepArgs> args(n);
     std::vector<brr_sweep_out> so(n);
     std::vector<uint32_t> its(n);
+    std::vector<double> et(n);
+    for (int i = 0; i < n; ++i) {
+        its[i] = m->inst[i]->iteration;
+        const int rc = iter_pre_dev(*m->inst[i], its[i]);
+        if (rc)
+            return rc;
+    }
     size_t smem = 0;
     MultiSweepArgs ma{};
     ma.n = n;
     ma.cta_start[0] = 0;
     for (int i = 0; i < n; ++i) {
         brr_ctx &c = *m->inst[i];
-        its[i] = c.iteration;
-        double mu_new = 0.0, eps_total = 0.0;
-        int rc = iter_pre(c, its[i], mu_new, eps_total);
+        MULTI_CUDA(cudaStreamSynchronize(c.st));
+        double mu_new = 0.0;
+        const int rc = iter_pre_host(c, its[i], mu_new, et[i]);
         if (rc)
             return rc;
+        sweep_stage(&c);
         size_t si = 0;
-        rc = sweep_prepare(&c, mu_new, eps_total, args[i], si);
-        if (rc)
-            return rc;
+        sweep_args(&c, mu_new, et[i], args[i], si);
         args[i].t_out = m->d_t + 2 * i;
         smem = std::max(smem, si);
         ma.cta_start[i + 1] = ma.cta_start[i] + c.G;
         ma.kind[i] = c.kind == BRR_KIND_DENSE ? 0 : 1;
         ma.inst[i] = args[i];
-        MULTI_CUDA(cudaEventRecord(m->ready[i], c.st));
-        MULTI_CUDA(cudaStreamWaitEvent(m->st, m->ready[i], 0));
     }
+    // occupancy check; also sets the kernel's shared-memory attribute outside the capture
     const int per_sm = sweep_multi_max_ctas_per_sm(m->form, m->kmax, smem);
     if (per_sm < 1 || (int64_t)per_sm * m->sms < ma.cta_start[n])
         return api_fail(BRR_ERR_ARG, "the instances need " + std::to_string(ma.cta_start[n]) +
                                          " co-resident CTAs with " + std::to_string(smem) + " bytes of shared memory");
-    MULTI_CUDA(cudaEventRecord(m->ev[0], m->st));
-    MULTI_CUDA(launch_sweep_multi(m->form, m->kmax, ma, smem, m->st));
-    MULTI_CUDA(cudaEventRecord(m->ev[1], m->st));
-    MULTI_CUDA(cudaEventRecord(m->done, m->st));
+    MULTI_CUDA(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < n; ++i) {
         brr_ctx &c = *m->inst[i];
-        MULTI_CUDA(cudaStreamWaitEvent(c.st, m->done, 0));
-        int rc = sweep_finish(&c, &so[i]);
+        int rc = iter_enqueue_draws(c, its[i], m->st);
+        if (!rc)
+            rc = sweep_enqueue_inputs(&c, et[i], m->st);
+        if (rc)
+            return abandon_capture(m, rc);
+    }
+    cudaError_t e = launch_sweep_multi(m->form, m->kmax, ma, smem, m->st);
+    if (e != cudaSuccess)
+        return abandon_capture(m, api_fail(BRR_ERR_CUDA, std::string("multi-instance sweep: ") + cudaGetErrorString(e)));
+    for (int i = 0; i < n; ++i) {
+        const int rc = sweep_enqueue_outputs(m->inst[i], m->st);
+        if (rc)
+            return abandon_capture(m, rc);
+    }
+    e = cudaMemcpyAsync(m->h_t, m->d_t, sizeof(unsigned long long) * 2 * n, cudaMemcpyDeviceToHost, m->st);
+    if (e != cudaSuccess)
+        return abandon_capture(m, api_fail(BRR_ERR_CUDA, cudaGetErrorString(e)));
+    cudaGraph_t graph = nullptr;
+    MULTI_CUDA(cudaStreamEndCapture(m->st, &graph));
+    if (m->exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(m->exec, graph, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(m->exec);
+            m->exec = nullptr;
+        }
+    }
+    if (!m->exec && (e = cudaGraphInstantiate(&m->exec, graph, 0)) != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        m->exec = nullptr;
+        return api_fail(BRR_ERR_CUDA, std::string("graph instantiation: ") + cudaGetErrorString(e));
+    }
+    cudaGraphDestroy(graph);
+    MULTI_CUDA(cudaEventRecord(m->ev[0], m->st));
+    MULTI_CUDA(cudaGraphLaunch(m->exec, m->st));
+    MULTI_CUDA(cudaEventRecord(m->ev[1], m->st));
+    MULTI_CUDA(cudaStreamSynchronize(m->st));
+    for (int i = 0; i < n; ++i) {
+        brr_ctx &c = *m->inst[i];
+        int rc = sweep_collect(&c, &so[i]);
         if (rc)
             return rc;
         rc = iter_post(c, so[i], its[i]);
         if (rc)
             return rc;
     }
-    std::vector<unsigned long long> t(2 * (size_t)n);
-    MULTI_CUDA(cudaMemcpy(t.data(), m->d_t, sizeof(unsigned long long) * t.size(), cudaMemcpyDeviceToHost));
     m->inst_ms.assign(n, 0.0);
     for (int i = 0; i < n; ++i)
-        m->inst_ms[i] = t[2 * i + 1] >= t[2 * i] ? (double)(t[2 * i + 1] - t[2 * i]) / 1e6 : 0.0;
+        m->inst_ms[i] = m->h_t[2 * i + 1] >= m->h_t[2 * i] ? (double)(m->h_t[2 * i + 1] - m->h_t[2 * i]) / 1e6 : 0.0;
     float ms = 0.f;
     MULTI_CUDA(cudaEventElapsedTime(&ms, m->ev[0], m->ev[1]));
     m->last_sweep_ms += ms;
@@ -273,6 +331,8 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
         e = cudaEventCreateWithFlags(&m->ready[i], cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&m->d_t, sizeof(unsigned long long) * 2 * n);
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **)&m->h_t, sizeof(unsigned long long) * 2 * n);
     if (e != cudaSuccess)
         return bail(api_fail(BRR_ERR_CUDA, cudaGetErrorString(e)));
     *out = m;
@@ -416,9 +476,10 @@ int brr_multi_get_state(brr_multi *m, int32_t i, brr_state *st)
     return brr_get_state(m->inst[i], st);
 }
 
-// Sweep time (device, all instances in one launch) and wall time of the last
-// brr_multi_iterate call; per instance (optional, n values each): CTAs, round
-// width and the last sweep's time on the device timer (ms).
+// Device time of the iteration graphs (all instances' draws, records, the one
+// sweep launch and the statistics) and wall time of the last brr_multi_iterate
+// call; per instance (optional, n values each): CTAs, round width and the last
+// sweep's time on the device timer (ms).
 int brr_multi_get_timing(brr_multi *m, double *sweep_ms, double *total_ms, int32_t *ctas, int32_t *width,
                          double *inst_ms)
 {

@@ -947,13 +947,12 @@ int sweep_multi_max_ctas_per_sm(int form, int kmax, size_t smem)
 }
 
 // The cooperative launch goes through cudaLaunchKernelEx with the cooperative
-// attribute, which stream capture records as a cooperative graph node.
+// attribute, which stream capture records as a cooperative graph node.  The
+// shared-memory attribute is set by sweep_multi_max_ctas_per_sm beforehand,
+// outside any capture.
 cudaError_t launch_sweep_multi(int form, int kmax, const MultiSweepArgs &m, size_t smem, cudaStream_t st)
 {
     const void *fn = multi_fn(form, kmax);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess)
-        return e;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)m.cta_start[m.n]);
     cfg.blockDim = dim3(kThreads);

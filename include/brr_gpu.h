@@ -237,7 +237,8 @@ int brr_batch_get_geometry(brr_batch *b, int32_t *ctas, int32_t *slice, int64_t 
 /* ---- Uneven batch: independent regressions of different sizes (C5 form) ----
  * Up to 32 instances, each with its own configuration (N, M, kind, groups, S,
  * seed, chain) but one sweep form and device, swept together: per iteration
- * one cooperative launch runs every instance's sweep on its own group of CTAs.
+ * one CUDA graph holds every instance's draws, records and statistics and one
+ * cooperative launch that runs every instance's sweep on its own group of CTAs.
  * Per instance the chain is the single-chain one (the same draws and results
  * as brr_iterate up to the order of floating-point sums).  brr_multi_tune runs
  * 3 + rounds real iterations to choose each instance's round width and CTAs. */
@@ -252,7 +253,7 @@ int brr_multi_init(brr_multi *m);
 int brr_multi_tune(brr_multi *m, int32_t rounds);
 int brr_multi_iterate(brr_multi *m, int32_t n_iter);
 int brr_multi_get_state(brr_multi *m, int32_t i, brr_state *st);
-/* Device time of the multi-instance sweeps and wall time of the last
+/* Device time of the iteration graphs and wall time of the last
  * brr_multi_iterate call (ms); per instance (optional, n values each): CTAs,
  * round width and the last sweep's time (ms). */
 int brr_multi_get_timing(brr_multi *m, double *sweep_ms, double *total_ms, int32_t *ctas, int32_t *width,
