@@ -184,6 +184,7 @@ struct MultiSweepArgs {
     SweepArgs inst[kMaxInstances];
 };
 int sweep_multi_max_ctas_per_sm(int form, int kmax, size_t smem);
+size_t sweep_multi_static_smem(int form, int kmax);
 cudaError_t launch_sweep_multi(int form, int kmax, const MultiSweepArgs &m, size_t smem, cudaStream_t st);
 
 // Kernel launchers (defined in brr_pack.cu / brr_sweep.cu).

@@ -272,7 +272,6 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
     if (cudaSetDevice(m->dev) != cudaSuccess || cudaGetDeviceProperties(&prop, m->dev) != cudaSuccess)
         return bail(api_fail(BRR_ERR_DEVICE, "no usable device"));
     m->sms = prop.multiProcessorCount;
-    m->smem_limit = prop.sharedMemPerBlockOptin - 4096;   // static shared memory of the multi kernel
     // instances are created with a provisional slicing and sliced again once all are known
     for (int i = 0; i < n; ++i) {
         brr_config c = cfgs[i];
@@ -286,6 +285,8 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
         for (int g = 0; g < c.n_groups; ++g)
             m->kmax = std::max(m->kmax, c.K[g]);
     }
+    // dynamic shared memory: what a CTA may use beside the kernel's static arrays
+    m->smem_limit = prop.sharedMemPerBlockOptin - sweep_multi_static_smem(m->form, m->kmax);
     // first split of the SMs: at least what the slices need, the rest by N*M;
     // when the default round widths need more CTAs than there are SMs, every
     // instance starts at the narrowest width (the smallest code ring)

@@ -178,6 +178,7 @@ struct SmemPlan {
     size_t ring_roff;       // ragged: R x 8 int32
     size_t gconst;          // n_groups x kMaxK x 4 doubles
     size_t gk;              // n_groups ints
+    size_t gcf;             // FP32C: FP32 sampler constants, n_groups x kMaxK x 2 floats
     size_t gtab;            // FP32C dense: 256 float4 + 256 bytes
     size_t total;
 };
@@ -207,6 +208,9 @@ __host__ __device__ inline SmemPlan make_plan(int form, int kind, int slice_max,
     o += align16((size_t)n_groups * kMaxK * 4 * sizeof(double));
     p.gk = o;
     o += align16((size_t)n_groups * sizeof(int32_t));
+    p.gcf = o;
+    if (form != kFormFP64)
+        o += align16((size_t)n_groups * kMaxK * 2 * sizeof(float));
     p.gtab = o;
     if (form != kFormFP64 && kind == kKindDense)
         o += 256 * 16 + 256;
@@ -268,6 +272,9 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     __shared__ double s_delta[4];         // update coefficients of the current round
     __shared__ float s_dfl[8];            // double-float split of the update coefficients
     __shared__ double s_red[kThreads / 32][2];
+    // a chain on one CTA exchanges nothing: its round's sums stay in shared memory
+    __shared__ unsigned long long s_acc[kMaxSpec * 4];
+    const bool solo = a.G == 1 && a.phantom == 0;
 
     const int B = a.B;
     const int lpm = kThreads / B;
@@ -289,6 +296,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     int32_t *ring_roff = reinterpret_cast<int32_t *>(smem + plan.ring_roff);
     double *gconst = reinterpret_cast<double *>(smem + plan.gconst);
     int32_t *gk = reinterpret_cast<int32_t *>(smem + plan.gk);
+    float *gcf = reinterpret_cast<float *>(smem + plan.gcf);
     float4 *gtab = reinterpret_cast<float4 *>(smem + plan.gtab);
     uint8_t *mtab = smem + plan.gtab + 256 * 16;
 
@@ -313,6 +321,15 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         gconst[i] = a.gconst[i];
     for (int i = tid; i < a.n_groups; i += kThreads)
         gk[i] = a.gK[i];
+    if (FORM != kFormFP64) {
+        // FP32 constants of the certified sampler: logL_k - logL_0 constant and h_k
+        for (int i = tid; i < a.n_groups * kMaxK; i += kThreads) {
+            const int k = i % kMaxK;
+            const double *row = a.gconst + (size_t)(i / kMaxK) * kMaxK * 4;
+            gcf[2 * i] = k == 0 ? 0.f : __double2float_rn(row[4 * k] - row[0]);
+            gcf[2 * i + 1] = k == 0 ? 0.f : __double2float_rn(row[4 * k + 2]);
+        }
+    }
     if (FORM != kFormFP64 && KIND == kKindDense) {
         for (int v = tid; v < 256; v += kThreads) {
             float g[4];
@@ -410,9 +427,16 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     };
     auto publish = [&](unsigned long long *acc, __int128 x) {
         const Fx f = fx_split(x);
-        red_add_u64(acc, (unsigned long long)f.hi);
-        red_add_u64(acc + 1, f.lo);
+        if (solo) {
+            atomicAdd(acc, (unsigned long long)f.hi);
+            atomicAdd(acc + 1, f.lo);
+        } else {
+            red_add_u64(acc, (unsigned long long)f.hi);
+            red_add_u64(acc + 1, f.lo);
+        }
     };
+    for (int i = tid; i < kMaxSpec * 4; i += kThreads)
+        s_acc[i] = 0ull;
 
     unsigned start = 0;
     long long r = 0;
@@ -432,7 +456,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         if (team < nb) {
             const unsigned slot = (start + team) & Rm;
             const SweepRec &rc = ring_rec[slot];
-            unsigned long long *acc = a.acc + (rb * kMaxSpec + team) * 4;
+            unsigned long long *acc = solo ? s_acc + team * 4 : a.acc + (rb * kMaxSpec + team) * 4;
             bool ok = true;
             if (KIND == kKindDense) {
                 const uint8_t *cb = ring_codes + slot * a.slot_bytes;
@@ -562,7 +586,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         // ---- grid barrier: one counter; release orders this CTA's
         // accumulator updates (ordered before it by bar.sync), acquire orders
         // the reads below.  The wait is bounded.
-        if (tid == 0) {
+        if (tid == 0 && !solo) {
             red_release_add_u64(a.counter, 1ull);
             const unsigned long long target = (unsigned long long)(a.G + a.phantom) * (unsigned long long)(r + 1);
             const uint64_t t0 = global_timer_ns();
@@ -585,14 +609,15 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         // ---- redundant sampling of the round's markers in every CTA, one thread per marker
         if (tid < nb) {
             const SweepRec &rc = ring_rec[(start + tid) & Rm];
-            const unsigned long long *acc = a.acc + (rb * kMaxSpec + tid) * 4;
-            const double tot = fx_join((long long)ld_relaxed_u64(acc), ld_relaxed_u64(acc + 1));
+            const unsigned long long *acc = solo ? s_acc + tid * 4 : a.acc + (rb * kMaxSpec + tid) * 4;
+            auto ldacc = [&](int k) -> unsigned long long { return solo ? acc[k] : ld_relaxed_u64(acc + k); };
+            const double tot = fx_join((long long)ldacc(0), ldacc(1));
             double num;
             if (KIND == kKindDense) {
                 if (FORM == kFormFP64) {
                     num = tot + rc.beta_old * Nm1;
                 } else {
-                    const double sm = fx_join((long long)ld_relaxed_u64(acc + 2), ld_relaxed_u64(acc + 3));
+                    const double sm = fx_join((long long)ldacc(2), ldacc(3));
                     const double sigma = rc.t[0], cm = rc.t[1], xm = rc.t[2];
                     num = (sigma * (tot - cm * (s_scal[2] - sm)) + xm * sm) + rc.beta_old * Nm1;
                 }
@@ -603,12 +628,29 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                 // the mean; Zsum includes the imputed values, which carries the
                 // pending uniform shift over the missing genotypes too
                 const double t12 =
-                    a.eigen ? tot + mean * fx_join((long long)ld_relaxed_u64(acc + 2), ld_relaxed_u64(acc + 3)) : tot;
+                    a.eigen ? tot + mean * fx_join((long long)ldacc(2), ldacc(3)) : tot;
                 num = (rc.beta_old * ((double)a.N - 1.0) - mean * s_scal[1] * isd) + (t12 + s_scal[0] * Zsum) * isd;
             }
             const int g = rc.group;
-            const Pick pk = pick_marker<FORM != kFormFP64, KM>(num, rc.u, rc.z, rc.beta_old,
-                                                           gconst + (size_t)g * kMaxK * 4, gk[g]);
+            const double *gcg = gconst + (size_t)g * kMaxK * 4;
+            Pick pk;
+            if (FORM == kFormFP64) {
+                pk = pick_marker<false, KM>(num, rc.u, rc.z, rc.beta_old, gcg, gk[g]);
+            } else {
+                // certified FP32 decision; FP64 where the bound cannot certify it
+                float xh, xl, a0;
+                int comp;
+                df_from_double(num, xh, xl);
+                if (pick_f32<KM>(xh, xl, __double2float_rn(rc.u), gcf + (size_t)g * kMaxK * 2, gk[g], comp, a0)) {
+                    pk.comp = comp;
+                    pk.acum0 = (double)a0;
+                    pk.beta = comp == 0 ? 0.0 : rc.beta_old;
+                    if (comp > 0)
+                        pk.beta = __dadd_rn(__dmul_rn(rc.z, gcg[4 * comp + 3]), __dmul_rn(num, gcg[4 * comp + 1]));
+                } else {
+                    pk = pick_marker<true, KM>(num, rc.u, rc.z, rc.beta_old, gcg, gk[g]);
+                }
+            }
             s_beta[tid] = pk.beta;
             s_acum[tid] = pk.acum0;
             s_comp[tid] = pk.comp;
@@ -635,6 +677,9 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             if (tid < 4 * kMaxSpec)
                 a.acc[((rb + 2) % 3) * kMaxSpec * 4 + tid] = 0ull;
         }
+        if (solo)   // the sampling has read this round's sums (barrier above)
+            for (int i = tid; i < kMaxSpec * 4; i += kThreads)
+                s_acc[i] = 0ull;
 
         // ---- apply the residual update of the first changing marker
         if (first < nb) {
@@ -932,6 +977,16 @@ static const void *multi_fn(int form, int kmax)
     if (form == kFormFP64)
         return kmax <= 4 ? (const void *)k_sweep_multi<kFormFP64, 4> : (const void *)k_sweep_multi<kFormFP64, kMaxK>;
     return kmax <= 4 ? (const void *)k_sweep_multi<kFormFP32C, 4> : (const void *)k_sweep_multi<kFormFP32C, kMaxK>;
+}
+
+size_t sweep_multi_static_smem(int form, int kmax)
+{
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, multi_fn(form, kmax)) != cudaSuccess) {
+        cudaGetLastError();
+        return 16384;
+    }
+    return fa.sharedSizeBytes;
 }
 
 int sweep_multi_max_ctas_per_sm(int form, int kmax, size_t smem)
