@@ -380,7 +380,7 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     a.part = c->d_part;
     a.err = c->d_err;
     a.rounds_out = c->d_rounds;
-    a.prof = c->d_prof;
+    a.prof = c->profile ? c->d_prof : nullptr;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
     a.gram = c->d_gram;
@@ -1274,6 +1274,14 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
         *build_ms = ctx->gram_ms;
     if (bytes)
         *bytes = ctx->d_gram ? (int64_t)(ctx->cfg.M * (ctx->cfg.M - 1) / 2) * (int64_t)sizeof(double) : 0;
+    return BRR_OK;
+}
+
+int brr_set_profiling(brr_ctx *ctx, int32_t on)
+{
+    if (!ctx || (on != 0 && on != 1))
+        return fail(BRR_ERR_ARG, "profiling is 0 or 1");
+    ctx->profile = on != 0;
     return BRR_OK;
 }
 

@@ -20,39 +20,59 @@
 // dot products move by dBeta_p * G[p, t] (exact sequential chain up to
 // rounding).  The block's rank-U residual update follows.
 //
-// Pipelining: block q+1's dot products are computed against the residual
-// before block q's update, while block q is being resolved; when block q+1 is
-// resolved, the updates of block q enter through the cross Gram entries
-// G[p, t], p in block q, t in block q+1.  So per CTA
-//   warps 0-7 (dot warps):  dots of block r+1, publish, stage Gram entries of
-//                           block r+2, arrive at barrier r+1;
-//   warp 8 (resolve warp):  wait for barrier r (arrived one iteration
-//                           earlier), bulk-copy block r+1's Gram entries
-//                           into shared memory (TMA, mbarrier), assemble block
-//                           r's dot products with the corrections of block
-//                           r-1, resolve block r;
-//   all warps:              rank-U update of block r.
-// The grid barrier is polled about one iteration after its last arrival, so
-// its latency leaves the critical path.
+// Pipelining, two blocks deep: block q+2's dot products are computed against
+// the residual that holds the updates of blocks q-1 and earlier, while block q
+// is being resolved.  When block t is resolved, the updates of blocks t-2 and
+// t-1 enter through the cross Gram entries G[p, t'] (p in block t-2: "far",
+// p in block t-1: "near", t' in block t).  Per CTA and iteration r:
+//   8 dot warps:            rank-U update of block r-1; cp.async of block
+//                           r+3's code slices into the slot block r-1 held;
+//                           dots of block r+2, publish, arrive at barrier r+2;
+//   the resolve warp:       near corrections of block r-1 (Gram entries in
+//                           shared memory, bulk-copied one iteration ahead),
+//                           resolve block r;
+//   the chore warp:         bulk copy (TMA) of block r+1's triangle and near
+//                           entries into shared memory; staged Gram entries of
+//                           block r+3; zeroed accumulators of block r+4 (first
+//                           CTA); a non-blocking arrival on the dot warps'
+//                           named barrier; the Gram loads of block r+4;
+//                           outputs of block r-1;
+//   the input warp:         the far corrections of block r-1 for block r+1
+//                           (entries read from the staging slot in L2), then
+//                           wait for barrier r+1 (arrived one iteration
+//                           earlier) and assemble block r+1's inputs from its
+//                           published sums.
+// So neither the grid barrier's latency nor the input assembly is on the path
+// of the dot warps or of the resolve warp.
 //
-// Buffers and why their counts suffice (iteration r: dot side publishes block
-// r+1, stages block r+2, arrives at barrier r+1; resolve side waits for barrier
-// r, reads block r's sums, copies block r+1's Gram entries):
+// Buffers and why their counts suffice (iteration r: the dot warps publish
+// block r+2 and arrive at barrier r+2; the input warp passes barrier r+1 and
+// reads block r+1's sums and staged far entries; a CTA in iteration r has
+// passed barrier r, and every CTA arrives at barrier q+2 only after it passed
+// barrier q):
 //  * two sets of barrier counters, barrier q on set q % 2, each set 8 counters
-//    (CTA s on counter s % 8, target its CTA count * (q / 2 + 1)): a CTA
-//    arrives at barrier q+2 only after it passed barrier q, so two barriers at
-//    most are open;
+//    (CTA s on counter s % 8, target its CTA count * (q / 2 + 1)): arrivals on
+//    a set beyond barrier q come only from CTAs that passed barrier q;
 //  * 8 fixed-point accumulator buffers (block q in buffer q % 8), each with 8
-//    copies (CTA s adds into copy s % 8, the reader sums them): the first
-//    CTA zeroes block q+3's buffer in iteration q before arriving at barrier
-//    q+1, after it passed barrier q-1, which every CTA arrived at after it had
-//    read the sums of block q-3 and earlier (the buffer last held block q-5);
-//    publishes of block q+3 come after barrier q+1;
-//  * 8 Gram staging slots in global memory (block q in slot q % 8), written in
-//    iteration q-2 after barrier q-3, when every CTA has finished copying the
-//    entries of block q-5 and earlier; 2 shared-memory Gram slots;
-//  * ring of 4B records and 4B code slots: iteration r holds blocks r..r+2
-//    (codes) and r..r+3 (records).
+//    copies (CTA s adds into copy s % 8, the reader sums them): the first CTA
+//    zeroes block q+4's buffer in iteration q before arriving at barrier q+2;
+//    every CTA publishes block q+4 in iteration q+2, after it passed barrier
+//    q+2; the buffer last held block q-4, whose sums every CTA read in
+//    iteration q-5, before arriving at barrier q-2 (passed by the first CTA);
+//  * 8 Gram staging slots in global memory (block q in slot q % 8: triangle,
+//    near, far entries), written in iteration q-3 before the arrival at
+//    barrier q-1, read (bulk copy of triangle and near, far loads) in
+//    iteration q-1 after barrier q-1 or, for blocks 0-2, after barrier 0;
+//    slot q % 8 last held block q-8, read in iteration q-9 (its bulk copy
+//    waited for in iteration q-8), before every CTA's arrival at barrier q-5,
+//    which the writers have passed; 2
+//    shared-memory Gram slots (block q copied in iteration q-1, read in
+//    iteration q; the slot's previous block q-2 was read in iteration q-2);
+//  * rings of 4B records and 4B code slots (B markers per block): records of
+//    blocks r..r+3 (block r+3 issued at the top of iteration r, into the slot
+//    of block r-1, read by nobody after iteration r-1); codes of blocks
+//    r-1..r+2, block r+3 issued by the dot warps after the update of block
+//    r-1, into its slot.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -65,10 +85,19 @@ namespace brr {
 
 namespace {
 
+// Roles by warp.  Warp w issues from sub-partition w % 4, so the resolve warp
+// (the latency-bound sampling chain) is placed on sub-partition 3 with the
+// input warp alone; the eight dot warps are 0-2, 4-6, 8 and 9.
 constexpr int kDotWarps = 8;
-constexpr int kResolveWarp = kDotWarps;       // samples the blocks
-constexpr int kChoreWarp = kDotWarps + 1;     // Gram copies and gathers, outputs
-constexpr int kBlockThreads = (kDotWarps + 2) * 32;
+constexpr int kResolveWarp = 3;    // samples the blocks
+constexpr int kInputWarp = 7;      // grid barrier, inputs of the next block
+constexpr int kChoreWarp = 10;     // Gram copies and gathers, outputs
+constexpr int kBlockThreads = (kDotWarps + 3) * 32;
+// index 0..7 of a dot warp, -1 for the other roles
+__host__ __device__ constexpr int dot_index(int w)
+{
+    return (w == kResolveWarp || w == kInputWarp || w == kChoreWarp) ? -1 : w - (w > 3) - (w > 7);
+}
 constexpr int kAccBufs = 8;
 constexpr int kAccCopies = 8;   // CTA s adds into copy s % 8: 19 atomics per address and block, not 152
 constexpr int kAccBufWords = kAccCopies * kMaxSpec * 4;
@@ -80,9 +109,13 @@ constexpr int kStageSlots = 8;
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-// Gram entries of one block: the triangle G[p, t], p < t within the block,
-// then the cross entries G[p, t] of the previous block's p and this block's t.
+// Gram entries of one block in shared memory: the triangle G[p, t], p < t
+// within the block, then the near entries G[p, t] of the previous block's p and
+// this block's t.
 __host__ __device__ inline size_t block_gram_entries(int B) { return (size_t)B * (B - 1) / 2 + (size_t)B * B; }
+// A staging slot adds the far entries G[p, t], p in the block before the
+// previous one.
+__host__ __device__ inline size_t block_stage_entries(int B) { return block_gram_entries(B) + (size_t)B * B; }
 
 struct PipePlan {
     size_t planes;          // residual limb planes: 8 words per 4 individuals
@@ -173,8 +206,20 @@ __device__ __forceinline__ long long clk()
 
 __device__ __forceinline__ void dot_warps_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
-// The dot warps and the chore warp before the arrival at a grid barrier.
+// Before the arrival at a grid barrier the dot warps wait on named barrier 2
+// for their own work and for the chore warp's staging stores; the chore warp
+// only signals it and goes on.
 __device__ __forceinline__ void arrive_sync() { asm volatile("bar.sync 2, 288;" ::: "memory"); }
+__device__ __forceinline__ void chore_signal() { asm volatile("bar.arrive 2, 288;" ::: "memory"); }
+
+// A double-float written by another CTA before a grid barrier this thread has
+// passed (read at L2, not from a stale L1 line).
+__device__ __forceinline__ float2 ld_relaxed_f2(const float2 *p)
+{
+    float2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p) : "memory");
+    return v;
+}
 
 // ---- fixed-point residual: E = eps * 2^kFrac, |E| < 2^62, as four balanced
 // 16-bit limbs E = l0 + l1 2^16 + l2 2^32 + l3 2^48 (l_k in [-2^15, 2^15)).
@@ -448,12 +493,14 @@ __device__ __forceinline__ void write_block_outputs(const SweepArgs &a, const Bl
     }
 }
 
-// One CTA of 10 warps per SM (8 dot warps, the resolve warp, the chore warp).
-// The register file is split between the SM's four sub-partitions (16K
-// registers each) and warps are placed round-robin, so the sub-partitions
+// One CTA of 11 warps per SM (8 dot warps, the resolve, chore and input
+// warps).  The register file is split between the SM's four sub-partitions
+// (16K registers each) and warps are placed round-robin, so the sub-partitions
 // holding three warps bound every thread to 168 registers: the launch bound is
-// stated for 12 warps to give the compiler that limit.
-template <int KM, bool MISS>
+// stated for 12 warps to give the compiler that limit.  PROF: the variant that
+// counts phase cycles on the first CTA (the clock reads constrain the code's
+// scheduling, so the plain variant has none).
+template <int KM, bool MISS, bool PROF>
 __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -482,13 +529,16 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     const int sidx = blockIdx.x;
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
+    const int dw = dot_index(warp);                       // dot warps: 0..7
+    const int dtid = dw >= 0 ? dw * 32 + lane : kBlockThreads;   // dot warps: 0..255
     const int lo = a.slice_lo[sidx];
     const int ns = a.slice_lo[sidx + 1] - lo;
     const int nbytes = ((ns + kChunk - 1) / kChunk) * 16;
     const int64_t byte_lo = lo / 4;
     const PipePlan plan = make_pipe_plan(a.slice_max, a.slot_bytes, B, a.n_groups);
     const int npairs = B * (B - 1) / 2;
-    const unsigned gent = (unsigned)block_gram_entries(B);
+    const unsigned gent = (unsigned)block_gram_entries(B);    // per shared-memory Gram slot
+    const unsigned gst = (unsigned)block_stage_entries(B);    // per staging slot
     const unsigned M32 = (unsigned)a.M;
     const int nblk = (int)((M32 + Bu - 1) / Bu);
     auto nb_of = [&](int q) { return (int)min(Bu, M32 - (unsigned)q * Bu); };
@@ -575,7 +625,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     __syncthreads();
 
     // ---- ring of records and genotype code slices (cp.async)
-    unsigned rec_issued = 0, code_issued = 0;
+    unsigned rec_issued = 0;
     auto issue_recs = [&](unsigned upto) {
         upto = min(upto, M32);
         if (upto <= rec_issued)
@@ -590,30 +640,54 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         }
         rec_issued = upto;
     };
+    // Code slices of a block, copied by the dot warps: thread t copies chunk
+    // my_c of the block's markers my_q, my_q + per_pass, ...  In the steady
+    // state the marker ids come from the records in global memory, loaded at
+    // the top of the iteration (the block's records are still in flight).
     const unsigned chunks = (unsigned)nbytes / 16u;
-    const unsigned per_pass = chunks ? (unsigned)kBlockThreads / chunks : 0u;
-    const unsigned my_q = chunks ? (unsigned)tid / chunks : 0u;
-    const unsigned my_c = chunks ? (unsigned)tid - my_q * chunks : 0u;
-    auto issue_codes = [&](unsigned upto) {
-        upto = min(upto, M32);
-        if (upto <= code_issued)
+    const unsigned per_pass = chunks ? (unsigned)(kDotWarps * 32) / chunks : 0u;
+    const unsigned my_q = chunks ? (unsigned)dtid / chunks : 0u;
+    const unsigned my_c = chunks ? (unsigned)dtid - my_q * chunks : 0u;
+    constexpr int kCodePasses = 4;
+    uint32_t jpre[kCodePasses] = {0u, 0u, 0u, 0u};
+    auto prefetch_code_ids = [&](int q) {
+        if (q >= nblk || dw < 0 || my_q >= per_pass)
             return;
-        if (my_q < per_pass) {
-            for (unsigned q = code_issued + my_q; q < upto; q += per_pass) {
-                const uint32_t j = ring_rec[q & Rm].j;
-                cp_async16(ring_codes + (q & Rm) * a.slot_bytes + 16 * my_c,
-                           a.codes + (int64_t)j * a.col_stride + byte_lo + 16 * my_c);
-            }
+        const unsigned qb = (unsigned)q * Bu, nbq = (unsigned)nb_of(q);
+#pragma unroll
+        for (int k = 0; k < kCodePasses; ++k) {
+            const unsigned m = my_q + (unsigned)k * per_pass;
+            if (m < nbq)
+                jpre[k] = __ldg(&a.brec[qb + m].j);
         }
-        code_issued = upto;
+    };
+    auto issue_block_codes = [&](int q, bool from_ring) {
+        if (q >= nblk || dw < 0 || my_q >= per_pass)
+            return;
+        const unsigned qb = (unsigned)q * Bu, nbq = (unsigned)nb_of(q);
+        auto copy = [&](unsigned m, uint32_t j) {
+            cp_async16(ring_codes + ((qb + m) & Rm) * a.slot_bytes + 16 * my_c,
+                       a.codes + (int64_t)j * a.col_stride + byte_lo + 16 * my_c);
+        };
+#pragma unroll
+        for (int k = 0; k < kCodePasses; ++k) {
+            const unsigned m = my_q + (unsigned)k * per_pass;
+            if (m < nbq)
+                copy(m, from_ring ? ring_rec[(qb + m) & Rm].j : jpre[k]);
+        }
+        for (unsigned m = my_q + kCodePasses * per_pass; m < nbq; m += per_pass)
+            copy(m, from_ring ? ring_rec[(qb + m) & Rm].j : __ldg(&a.brec[qb + m].j));
     };
 
     // ---- Gram entries of block q (chore warp): CTA s gathers entries
     // e = s + G*(l + 32*i) from the packed Gram into staging slot q % 8.  The
-    // first entry of each thread is loaded one iteration before it is stored,
-    // so that the random reads of the Gram never delay the barrier arrival.
-    double gval = 0.0;
-    int gent_mine = -1;
+    // first kGather entries of each thread are loaded one iteration before they
+    // are stored, so that the random reads of the Gram never delay the
+    // signal before the barrier arrival (more than kGather entries per lane, on
+    // grids below 80 CTAs, are loaded when stored).
+    constexpr int kGather = 4;
+    double gval[kGather] = {0.0, 0.0, 0.0, 0.0};
+    int gent_mine[kGather] = {-1, -1, -1, -1};
     auto gram_entry = [&](int q, unsigned e, double *out) -> bool {
         const unsigned q0 = (unsigned)q * Bu;
         const int nbq = nb_of(q);
@@ -625,14 +699,17 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 return false;
             qa = q0 + pa;
         } else {
-            if (q == 0)
-                return false;
+            // near (block q-1) or far (block q-2) entries; those blocks are full
             const unsigned c = e - (unsigned)npairs;
-            pa = c / Bu;   // position in block q-1 (full: q-1 < nblk-1)
-            pb = c - pa * Bu;
+            const unsigned back = c < Bu * Bu ? 1u : 2u;
+            if ((unsigned)q < back)
+                return false;
+            const unsigned cc = c - (back - 1u) * Bu * Bu;
+            pa = cc / Bu;
+            pb = cc - pa * Bu;
             if ((int)pb >= nbq)
                 return false;
-            qa = q0 - Bu + pa;
+            qa = q0 - back * Bu + pa;
         }
         const int64_t ja = __ldg(&a.brec[qa].j), jb = __ldg(&a.brec[q0 + pb].j);
         const int64_t hi = ja > jb ? ja : jb, lw = ja > jb ? jb : ja;
@@ -640,10 +717,13 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         return true;
     };
     auto gather_load = [&](int q) {
-        gent_mine = -1;
-        const unsigned e = (unsigned)sidx + (unsigned)lane * (unsigned)a.G;
-        if (e < gent && gram_entry(q, e, &gval))
-            gent_mine = (int)e;
+#pragma unroll
+        for (int k = 0; k < kGather; ++k) {
+            gent_mine[k] = -1;
+            const unsigned e = (unsigned)sidx + (unsigned)(lane + 32 * k) * (unsigned)a.G;
+            if (e < gst && gram_entry(q, e, &gval[k]))
+                gent_mine[k] = (int)e;
+        }
     };
     auto split2 = [](double v) {
         float h, l;
@@ -651,10 +731,12 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         return make_float2(h, l);
     };
     auto gather_store = [&](int q) {
-        float2 *slot = gstage + (size_t)(q % kStageSlots) * gent;
-        if (gent_mine >= 0)
-            slot[gent_mine] = split2(gval);
-        for (unsigned e = (unsigned)sidx + (unsigned)(lane + 32) * (unsigned)a.G; e < gent;
+        float2 *slot = gstage + (size_t)(q % kStageSlots) * gst;
+#pragma unroll
+        for (int k = 0; k < kGather; ++k)
+            if (gent_mine[k] >= 0)
+                slot[gent_mine[k]] = split2(gval[k]);
+        for (unsigned e = (unsigned)sidx + (unsigned)(lane + 32 * kGather) * (unsigned)a.G; e < gst;
              e += 32u * (unsigned)a.G) {
             double v;
             if (gram_entry(q, e, &v))
@@ -686,7 +768,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         for (int k = 0; k < MPW; ++k) {
             // markers past the end of a short block read a stale slot; their
             // sums are never published
-            const unsigned m = (unsigned)warp + 8u * ((unsigned)k ^ (unsigned)(lane >> 2));
+            const unsigned m = (unsigned)dw + 8u * ((unsigned)k ^ (unsigned)(lane >> 2));
             cofs[k] = ((q0 + m) & Rm) * (unsigned)a.slot_bytes;
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
@@ -746,7 +828,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         };
         const __int128 T = combine(A[0]);
         const __int128 Tm = MISS ? combine(Mx[0]) : (__int128)0;
-        const int m = warp + 8 * (lane >> 2);
+        const int m = dw + 8 * (lane >> 2);
         if (limb == 0 && m < nbq) {
             unsigned long long *acc =
                 a.acc + (size_t)(q % kAccBufs) * kAccBufWords + ((size_t)(sidx % kAccCopies) * kMaxSpec + m) * 4;
@@ -760,9 +842,10 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                             1ull);
     };
 
-    // profiling (first CTA): dot side on thread 0, resolve side on warp 8 lane 0
-    const bool prof_d = a.prof != nullptr && sidx == 0 && tid == 0;
-    const bool prof_r = a.prof != nullptr && sidx == 0 && tid == kDotWarps * 32;
+    // profiling (first CTA): dot side on thread 0, resolve side on the resolve
+    // warp's lane 0
+    const bool prof_d = PROF && sidx == 0 && tid == 0;
+    const bool prof_r = PROF && sidx == 0 && tid == kResolveWarp * 32;
     long long ph[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     long long tp = (prof_d || prof_r) ? clk() : 0;
     auto mark = [&](bool on, int k) {
@@ -772,11 +855,9 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             tp = t;
         }
     };
-    unsigned long long *fb_counter = a.prof ? reinterpret_cast<unsigned long long *>(a.prof + 8) : nullptr;
+    unsigned long long *fb_counter = PROF ? reinterpret_cast<unsigned long long *>(a.prof + 8) : nullptr;
     long long steps = 0;
-    long long tdl = 0;   // profiling: dot products of the second warp
-    const bool prof_w1 = a.prof != nullptr && sidx == 0 && tid == 32;
-    const bool prof_h = a.prof != nullptr && sidx == 0 && tid == (kDotWarps - 1) * 32;
+    const bool prof_h = PROF && sidx == 0 && tid == kInputWarp * 32;
     int cp_issued = -1, cp_waited = -1;   // resolve warp: Gram copies issued / waited for
 
     // ---- rank-U residual update of block q (dot warps, run at the start of the
@@ -788,8 +869,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         if (U == 0)
             return;
         const unsigned qb = (unsigned)q * Bu;
-        if (tid < 4 * U) {
-            const int u = tid >> 2, code = tid & 3;
+        if (dtid < 4 * U) {
+            const int u = dtid >> 2, code = dtid & 3;
             const float2 dB = s_dB[par][u];
             const float4 xv = s_x[par][u][code >> 1];
             const float xh = (code & 1) ? xv.z : xv.x, xl = (code & 1) ? xv.w : xv.y;
@@ -804,7 +885,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         // The sum of the residual is left as it was at the sweep start: the
         // standardised columns sum to zero, so a dense update moves it only
         // by rounding (dBeta times a column sum of order 1e-11).
-        for (int b = tid; b < nbytes; b += kDotWarps * 32) {
+        for (int b = dtid; b < nbytes; b += kDotWarps * 32) {
             const longlong2 e01 = reinterpret_cast<const longlong2 *>(fix)[2 * b];
             const longlong2 e23 = reinterpret_cast<const longlong2 *>(fix)[2 * b + 1];
             long long E[4] = {e01.x, e01.y, e23.x, e23.y};
@@ -831,15 +912,50 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         dot_warps_sync();
     };
 
-    constexpr int kHelperWarp = kDotWarps - 1;   // polls the grid barrier, assembles the next block's inputs
     constexpr int kCopyThread = kChoreWarp * 32; // issues the Gram bulk copies
 
-    // ---- inputs of block q (the helper warp, after its dot products): wait
-    // for barrier q (lane c < 8 polls counter c), then per marker
-    // num = sigma * sum(g*eps) + cst + dm * sum_missing(eps) as double-float,
-    // with the FP32 sampler's per-marker values.
+    // ---- inputs of block q (the input warp, one iteration before block q is
+    // resolved): first the far corrections dBeta_p * G[p, t] of block q-2's
+    // residual-changing markers p (their updates are not in the residual the
+    // dot products saw; block q-2's decisions and block q's staged entries are
+    // known before barrier q, so they are read while the last CTAs arrive);
+    // then wait for barrier q (lane c < 8 polls counter c) and form per marker
+    // num = sigma * sum(g*eps) + cst + dm * sum_missing(eps) + far as
+    // double-float, with the FP32 sampler's per-marker values.
     long long th_poll = 0, th_in = 0;
     auto prepare_inputs = [&](int q, bool prof) {
+        const int par = q & 1, nbq = nb_of(q);
+        const unsigned qb = (unsigned)q * Bu;
+        // far corrections (block q-2 has the parity of q), eight rows of
+        // entries in flight at a time
+        float fh[2] = {0.f, 0.f}, fl[2] = {0.f, 0.f};
+        if (q >= 2) {
+            const int Uf = s_nupd[par];
+            const float2 *gfar = gstage + (size_t)(q % kStageSlots) * gst + gent;
+            for (int u0 = 0; u0 < Uf; u0 += 8) {
+                float2 g[8][2];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int p = u0 + k < Uf ? s_upd[par][u0 + k] : 0;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        g[k][h] = u0 + k < Uf ? ld_relaxed_f2(gfar + (size_t)p * B + lane + 32 * h)
+                                              : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    if (u0 + k >= Uf)
+                        break;
+                    const float2 dB = s_dB[par][u0 + k];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        float ph2, pl2;
+                        df_mul(dB.x, dB.y, g[k][h].x, g[k][h].y, ph2, pl2);
+                        df_add(fh[h], fl[h], ph2, pl2);
+                    }
+                }
+            }
+        }
         const long long t0 = prof ? clk() : 0;
         bool ok = true;
         if (lane < kCounters) {
@@ -869,8 +985,25 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         const long long t1 = prof ? clk() : 0;
         if (!ok)
             return;
-        const int par = q & 1, nbq = nb_of(q);
-        const unsigned qb = (unsigned)q * Bu;
+        // the published sums of the lane's two markers, every load issued
+        // before the first use; the copies' 56-bit low words sum to less than
+        // 2^64 (152 parts at most)
+        const unsigned long long *accb = a.acc + (size_t)(q % kAccBufs) * kAccBufWords;
+        long long th64[2] = {0, 0}, sh64[2] = {0, 0};
+        unsigned long long tl64[2] = {0ull, 0ull}, sl64[2] = {0ull, 0ull};
+#pragma unroll
+        for (int c = 0; c < kAccCopies; ++c) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const unsigned long long *ac = accb + ((size_t)c * kMaxSpec + lane + 32 * h) * 4;
+                th64[h] += (long long)ld_relaxed_u64(ac);
+                tl64[h] += ld_relaxed_u64(ac + 1);
+                if (MISS) {
+                    sh64[h] += (long long)ld_relaxed_u64(ac + 2);
+                    sl64[h] += ld_relaxed_u64(ac + 3);
+                }
+            }
+        }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int m = lane + 32 * h;
@@ -878,30 +1011,17 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             unsigned meta = 2u << 8;
             if (m < nbq) {
                 const BlockRec &rc = ring_rec[(qb + m) & Rm];
-                const unsigned long long *acc = a.acc + (size_t)(q % kAccBufs) * kAccBufWords + (size_t)m * 4;
-                // the copies' 56-bit low words sum to less than 2^64 (152 parts at most)
-                long long th64 = 0, sh64 = 0;
-                unsigned long long tl64 = 0, sl64 = 0;
-#pragma unroll
-                for (int c = 0; c < kAccCopies; ++c) {
-                    const unsigned long long *ac = acc + (size_t)c * kMaxSpec * 4;
-                    th64 += (long long)ld_relaxed_u64(ac);
-                    tl64 += ld_relaxed_u64(ac + 1);
-                    if (MISS) {
-                        sh64 += (long long)ld_relaxed_u64(ac + 2);
-                        sl64 += ld_relaxed_u64(ac + 3);
-                    }
-                }
                 float th, tl;
-                fx_to_df(th64, tl64, th, tl);
+                fx_to_df(th64[h], tl64[h], th, tl);
                 df_mul(rc.sig[0], rc.sig[1], th, tl, nh, nl);
                 df_add(nh, nl, rc.cst[0], rc.cst[1]);
                 if (MISS) {
                     float sh, sl, qh, ql;
-                    fx_to_df(sh64, sl64, sh, sl);
+                    fx_to_df(sh64[h], sl64[h], sh, sl);
                     df_mul(rc.dm[0], rc.dm[1], sh, sl, qh, ql);
                     df_add(nh, nl, qh, ql);
                 }
+                df_add(nh, nl, fh[h], fl[h]);
                 uf = rc.uf;
                 meta = (unsigned)rc.group | ((unsigned)s_gk[rc.group] << 8) | (rc.bnz ? 1u << 16 : 0u);
             }
@@ -916,58 +1036,71 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         }
     };
 
-    // ---- first blocks: records 0..2 and codes 0..1 resident, block 0's dot
-    // products and the Gram entries of blocks 0 and 1 staged, barrier 0
-    issue_recs(3u * Bu);
+    // ---- first blocks: records 0..3 and codes 0..2 resident; the Gram entries
+    // of blocks 0..2 staged and blocks 0 and 1's dot products published before
+    // the arrivals at barriers 0 and 1; block 0's inputs assembled
+    issue_recs(4u * Bu);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
-    issue_codes(2u * Bu);
+    for (int q = 0; q < 3; ++q)
+        issue_block_codes(q, true);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
-    if (warp < kDotWarps) {
+    if (dw >= 0) {
         dot_block(0);
+        if (nblk > 1)
+            dot_block(1);
         arrive_sync();
-        if (tid == 0)
+        if (tid == 0) {
             arrive(0);
-        if (warp == kHelperWarp)
-            prepare_inputs(0, false);
-    } else if (warp == kChoreWarp) {
-        gather_load(0);
-        gather_store(0);
-        if (nblk > 1) {
-            gather_load(1);
-            gather_store(1);
+            if (nblk > 1)
+                arrive(1);
         }
-        if (nblk > 2)
-            gather_load(2);
-        arrive_sync();
+    } else if (warp == kChoreWarp) {
+        for (int q = 0; q < 3 && q < nblk; ++q) {
+            gather_load(q);
+            gather_store(q);
+        }
+        if (nblk > 3)
+            gather_load(3);
+        __syncwarp();
+        chore_signal();
+    } else if (warp == kInputWarp) {
+        prepare_inputs(0, false);
     }
 
     int r = 0;
     if (prof_d || prof_r)
         tp = clk();
+    // profiling: per role, the clock from the iteration's start to the end of
+    // its work (dot side on thread 0, chore warp, resolve warp)
+    long long t_it = 0, t_end = 0;
+    const bool prof_e = PROF && sidx == 0 && (tid & 31) == 0 &&
+                        (tid == 0 || warp == kChoreWarp || warp == kResolveWarp || warp == kInputWarp);
     for (; r < nblk; ++r) {
         cp_async_wait_all();
         __syncthreads();
         if (s_abort)
             break;
+        if (prof_e)
+            t_it = clk();
         mark(prof_d, 0);
-        issue_codes((unsigned)(r + 3) * Bu);
         issue_recs((unsigned)(r + 4) * Bu);
         cp_async_commit();
         const unsigned q0 = (unsigned)r * Bu;
         const int nb = nb_of(r);
 
         if (warp == kChoreWarp) {
-            // ---- chore warp: Gram copy of block r+1 (its staging was published by
-            // barrier r, which the helper warp passed in the previous iteration),
-            // issued early so that the L2 burst of 152 CTAs copying the same slot
-            // overlaps the dot products; staged Gram entries of block r+2 (loaded
-            // in the previous iteration) and the zeroed accumulators of block r+3,
-            // written before the arrival; then the Gram loads of block r+3 and the
-            // outputs of block r-1
+            // ---- chore warp: Gram copy of block r+1 (its staging was published
+            // by barrier r, which this warp passed in the previous iteration;
+            // blocks 0..2 by barrier 0), issued early so that the L2 burst of
+            // 152 CTAs copying the same slot overlaps the dot products; staged
+            // Gram entries of block r+3 (loaded in the previous iteration) and
+            // the zeroed accumulators of block r+4, signalled to the dot warps
+            // before their arrival at barrier r+2; then the Gram loads of
+            // block r+4 and the outputs of block r-1
             if (lane == 0) {
                 fence_proxy_async();
                 if (r == 0) {
@@ -978,41 +1111,42 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 if (r + 1 < nblk) {
                     const int q = r + 1;
                     mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
-                    bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gent,
+                    bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gst,
                                   (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
                     cp_issued = q;
                 }
             }
-            if (r + 2 < nblk)
-                gather_store(r + 2);
-            if (sidx == 0 && r + 3 < nblk)
-                for (int i = lane; i < kAccBufWords; i += 32)
-                    a.acc[(size_t)((r + 3) % kAccBufs) * kAccBufWords + i] = 0ull;
-            arrive_sync();
             if (r + 3 < nblk)
-                gather_load(r + 3);
+                gather_store(r + 3);
+            if (sidx == 0 && r + 4 < nblk)
+                for (int i = lane; i < kAccBufWords; i += 32)
+                    a.acc[(size_t)((r + 4) % kAccBufs) * kAccBufWords + i] = 0ull;
+            __syncwarp();
+            chore_signal();
+            if (r + 4 < nblk)
+                gather_load(r + 4);
             if (r >= 1 && sidx == (r - 1) % a.G)
                 write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
-        } else if (warp < kDotWarps) {
-            // ---- dot side: update of block r-1, dots of block r+1 and their
-            // publication, then the inputs of block r+1
-            if (r >= 1) {
-                apply_update(r - 1);
-                mark(prof_d, 4);
-            }
-            const long long td0 = prof_w1 ? clk() : 0;
+        } else if (warp == kInputWarp) {
+            // ---- input warp: block r+1's inputs
             if (r + 1 < nblk)
-                dot_block(r + 1);
-            const long long td1 = prof_w1 ? clk() : 0;
-            arrive_sync();
-            if (prof_w1)
-                tdl += td1 - td0;
-            if (tid == 0 && r + 1 < nblk)
-                arrive(r + 1);
-            mark(prof_d, 1);
-            // inputs of block r+1, once barrier r+1 has passed
-            if (warp == kHelperWarp && r + 1 < nblk)
                 prepare_inputs(r + 1, prof_h);
+        } else if (dw >= 0) {
+            // ---- dot side: update of block r-1, the code slices of block r+3
+            // into the slot block r-1 held, dots of block r+2 and their
+            // publication
+            prefetch_code_ids(r + 3);
+            if (r >= 1)
+                apply_update(r - 1);
+            mark(prof_d, 4);
+            issue_block_codes(r + 3, false);
+            cp_async_commit();
+            if (r + 2 < nblk)
+                dot_block(r + 2);
+            arrive_sync();
+            if (tid == 0 && r + 2 < nblk)
+                arrive(r + 2);
+            mark(prof_d, 1);
         } else {
             // ---- resolve side
             mark(prof_r, 8);
@@ -1231,6 +1365,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 }
             }
         }
+        if (prof_e)
+            t_end += clk() - t_it;
         __syncthreads();
         mark(prof_d, 11);
         if (s_abort)
@@ -1238,7 +1374,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     }
     // the last block: residual update and outputs
     if (!s_abort && r == nblk) {
-        if (warp < kDotWarps)
+        if (dw >= 0)
             apply_update(nblk - 1);
         else if (warp == kChoreWarp && sidx == (nblk - 1) % a.G)
             write_block_outputs<KM>(a, s_out[(nblk - 1) & 1], gcf, s_gk, gbf, lane);
@@ -1254,8 +1390,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         a.prof[2] = th_poll;
         a.prof[11] = th_in;
     }
-    if (prof_w1)
-        a.prof[15] = tdl;
+    if (prof_e)
+        a.prof[tid == 0 ? 12 : (warp == kChoreWarp ? 13 : (warp == kResolveWarp ? 14 : 15))] = t_end;
     if (prof_r) {
         a.prof[3] = ph[3];
         a.prof[6] = steps;
@@ -1270,7 +1406,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     if (tid == kCopyThread)
         s_cp_issued = cp_issued;
     __syncthreads();
-    if (tid == kDotWarps * 32) {
+    if (tid == kResolveWarp * 32) {
         for (int q = cp_waited + 1; q <= s_cp_issued; ++q)
             mbar_wait(&mbar[q & 1], (unsigned)((q >> 1) & 1), a.timeout_ns);
     }
@@ -1345,21 +1481,20 @@ size_t sweep_block_smem_bytes(const SweepArgs &a)
     return make_pipe_plan(a.slice_max, a.slot_bytes, a.B, a.n_groups).total;
 }
 
-size_t sweep_block_stage_bytes(int B) { return (size_t)kStageSlots * block_gram_entries(B) * sizeof(float2); }
+size_t sweep_block_stage_bytes(int B) { return (size_t)kStageSlots * block_stage_entries(B) * sizeof(float2); }
 
 int sweep_block_threads() { return kBlockThreads; }
 
 template <int KM, bool MISS>
 static cudaError_t launch_block_km(const SweepArgs &a, size_t smem, cudaStream_t st)
 {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_sweep_block<KM, MISS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const void *f = a.prof ? (const void *)k_sweep_block<KM, MISS, true> : (const void *)k_sweep_block<KM, MISS, false>;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     SweepArgs args = a;
     void *params[] = {&args};
-    return cudaLaunchCooperativeKernel((const void *)k_sweep_block<KM, MISS>, dim3(a.G), dim3(kBlockThreads), params,
-                                       smem, st);
+    return cudaLaunchCooperativeKernel(f, dim3(a.G), dim3(kBlockThreads), params, smem, st);
 }
 
 cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st)
@@ -1372,8 +1507,10 @@ cudaError_t launch_sweep_block(const SweepArgs &a, size_t smem, cudaStream_t st)
 int sweep_block_max_ctas_per_sm(size_t smem, std::string *why)
 {
     int n = 1 << 30;
-    const void *fs[4] = {(const void *)k_sweep_block<4, false>, (const void *)k_sweep_block<4, true>,
-                         (const void *)k_sweep_block<kMaxK, false>, (const void *)k_sweep_block<kMaxK, true>};
+    const void *fs[8] = {(const void *)k_sweep_block<4, false, false>,     (const void *)k_sweep_block<4, true, false>,
+                         (const void *)k_sweep_block<kMaxK, false, false>, (const void *)k_sweep_block<kMaxK, true, false>,
+                         (const void *)k_sweep_block<4, false, true>,      (const void *)k_sweep_block<4, true, true>,
+                         (const void *)k_sweep_block<kMaxK, false, true>,  (const void *)k_sweep_block<kMaxK, true, true>};
     for (const void *f : fs) {
         int m = 0;
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

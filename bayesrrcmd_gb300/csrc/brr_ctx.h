@@ -87,6 +87,7 @@ struct brr_ctx {
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
     int64_t last_rounds = 0;
     long long phase[16] = {};   // summed over the sweeps of the last call
+    bool profile = false;       // phase counters on (brr_set_profiling)
     uint64_t wait_limit_ns = 2000000000ull;
     int phantom = 0;
 

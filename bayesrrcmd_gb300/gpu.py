@@ -61,7 +61,7 @@ EXPORTS = [
     "brr_last_error", "brr_ctx_create", "brr_ctx_destroy", "brr_pack_bed", "brr_pack_bed_device",
     "brr_get_marker_table", "brr_get_ragged_lists", "brr_set_groups", "brr_set_phenotype", "brr_init_chain",
     "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing", "brr_get_phase_cycles",
-    "brr_set_wait_limit", "brr_xbeta", "brr_synth_bed_device", "brr_xbeta_noalloc",
+    "brr_set_wait_limit", "brr_set_profiling", "brr_xbeta", "brr_synth_bed_device", "brr_xbeta_noalloc",
     "brr_get_gram_info",
     "brr_batch_create", "brr_batch_destroy", "brr_batch_pack_bed", "brr_batch_pack_bed_device",
     "brr_batch_set_groups", "brr_batch_set_phenotypes", "brr_batch_init", "brr_batch_iterate",
@@ -102,6 +102,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_get_phase_cycles.argtypes = [P, C.POINTER(C.c_int64)]
     lib.brr_set_wait_limit.argtypes = [P, C.c_uint64, C.c_int32]
+    lib.brr_set_profiling.argtypes = [P, C.c_int32]
     lib.brr_get_gram_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
@@ -330,6 +331,10 @@ class Chain:
 
     def set_wait_limit(self, timeout_ns: int, phantom_arrivals: int = 0):
         self._check(self.lib.brr_set_wait_limit(self.h, int(timeout_ns), int(phantom_arrivals)))
+
+    def set_profiling(self, on: bool):
+        """Phase counters (phase_cycles) on or off; timed runs keep them off."""
+        self._check(self.lib.brr_set_profiling(self.h, 1 if on else 0))
 
     def gram_info(self):
         b, ms, n = C.c_int32(), C.c_double(), C.c_int64()

@@ -46,6 +46,7 @@ P_LO, P_HI = 0.01, 0.5
 N_CAUSAL, H2 = 1000, 0.4
 SEED = 20261203
 REFRESH = 50
+PROFILE_STEPS = 2
 METRIC = "marker-updates/sec at N=100k on 1 GB300, chosen vs plain FP64 GPU at matched beta error"
 WORKLOAD = ("dense 2-bit BayesR, N=100,000 x M=100,000, two groups (S1=0.01,0.001,0.0001; S2=0.1,0.01), "
             "1,000 causal, h2=0.4")
@@ -152,7 +153,7 @@ def make_problem(lib, gpu, torch, device, chain_id):
     return d_bed, y, group
 
 
-def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chain_id):
+def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chain_id, profile=False):
     cfg = gpu.ChainConfig(N=N_IND, M=M_SNP, S=S_GROUPS, form=form, seed=SEED + chain_id, chain=chain_id,
                           refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device)
     ch = gpu.Chain(cfg, lib=lib)
@@ -168,8 +169,14 @@ def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chai
     torch.cuda.synchronize(device)
     wall = time.perf_counter() - t0
     sweep_ms, total_ms, rounds = ch.timing()
-    phases = ch.phase_cycles()
     st = ch.state()
+    # phase counters from PROFILE_STEPS further iterations of the counting
+    # variant, after the timed steps and the state read
+    phases = np.zeros(16, np.int64)
+    if profile:
+        ch.set_profiling(True)
+        ch.iterate(PROFILE_STEPS)
+        phases = ch.phase_cycles()
     ch.close()
     return dict(total_ms=total_ms, sweep_ms=sweep_ms, rounds=rounds, wall_s=wall, phases=phases.tolist(),
                 beta=st["beta"], sigmaE=st["sigmaE"], sigmaG=st["sigmaG"].tolist(), gram=gram)
@@ -454,7 +461,8 @@ def main():
 
     barrier()
     with ClockSampler(device) as clk:
-        fp32c = run_form(lib, gpu, torch, device, d_bed, y, group, gpu.FORM_FP32C, args.steps, args.warmup, rank)
+        fp32c = run_form(lib, gpu, torch, device, d_bed, y, group, gpu.FORM_FP32C, args.steps, args.warmup, rank,
+                         profile=True)
     barrier()
     fp64 = run_form(lib, gpu, torch, device, d_bed, y, group, gpu.FORM_FP64, args.steps, args.warmup, rank)
     barrier()
@@ -552,9 +560,12 @@ def main():
                                  zip(["ring_wait", "dot_side", "barrier_wait", "sample", "update", "block_inputs",
                                       "of_sample_picks", "of_sample_steps", "next_block_inputs"],
                                      [*fp32c["phases"][:5], fp32c["phases"][7], *fp32c["phases"][9:12]])},
-        "dot_loop_clk_per_round_warp1": fp32c["phases"][15] / max(fp32c["phases"][5], 1),
+        "phases_source": f"{PROFILE_STEPS} iterations of the phase-counting kernel variant after the timed steps",
+        "role_end_clk_per_round": {k: fp32c["phases"][i] / max(fp32c["phases"][5], 1)
+                                   for k, i in (("dot_warps", 12), ("gram_warp", 13), ("resolve_warp", 14),
+                                                ("input_warp", 15))},
         "sampling_steps_per_round": fp32c["phases"][6] / max(fp32c["phases"][5], 1),
-        "fp64_fallbacks_per_step": fp32c["phases"][8] / args.steps,
+        "fp64_fallbacks_per_step": fp32c["phases"][8] / PROFILE_STEPS,
         "rounds_per_step": fp32c["rounds"] / args.steps,
         "gram": {"blocked_sweep": fp32c["gram"]["blocked"], "build_ms": fp32c["gram"]["build_ms"],
                  "bytes": fp32c["gram"]["bytes"]},

@@ -270,10 +270,17 @@ int brr_multi_get_timing(brr_multi *m, double *sweep_ms, double *total_ms, int32
  * [7] block inputs on the sampling warp (corrections of the previous block,
  * Gram copy wait), [8] samples the FP32 sampler handed to FP64, [9] cycles of
  * [3] in component picks, [10] cycles of [3] resolving steps, [11] assembling
- * the next block's inputs, [15] dot products alone on the second warp.  The
+ * the next block's inputs, [12]-[15] cycles from each iteration's start to the
+ * end of the work of the dot warps, the Gram warp, the sampling warp and the
+ * input warp.  The
  * per-thread clock is read around long code regions, so the values are
  * indicative. */
 int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles);
+/* Phase counters on (1) or off (0, the default).  The counting runs a variant
+ * of the Gram-blocked sweep that reads the SM clock on the first CTA; the
+ * clock reads constrain the scheduling of the sweep's sampling chain, so timed
+ * runs leave the counters off and brr_get_phase_cycles returns zeros. */
+int brr_set_profiling(brr_ctx *ctx, int32_t on);
 
 #ifdef __cplusplus
 }
