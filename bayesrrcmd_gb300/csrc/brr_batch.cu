@@ -225,7 +225,9 @@ __host__ __device__ inline BatchPlan batch_plan(int C, int kext, int G)
     return p;
 }
 
-template <int KM>
+// PROF: the variant that counts phase cycles on CTA 0 (the plain variant reads
+// no clock, whose reads would constrain the scheduling of every CTA's code).
+template <int KM, bool PROF>
 __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
     const int TPP = kTmemCols / R;                  // update tiles per TMEM pass
     const double inv2f = 1.0 / (double)(1ll << kBatchFrac);
     unsigned long long *cnt1 = a.counter, *cnt2 = a.counter + kCounterGap;
-    long long *prof = (a.prof && s == 0) ? a.prof : nullptr;
+    long long *prof = (PROF && s == 0) ? a.prof : nullptr;
     long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
     if (tid == 0) {
@@ -836,13 +838,13 @@ template <int KM>
 cudaError_t launch_batch_km(const BatchArgs &a, cudaStream_t st)
 {
     const size_t smem = batch_smem_bytes(a.C, a.kext, a.G);
-    cudaError_t e = cudaFuncSetAttribute(k_sweep_batch<KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const void *f = a.prof ? (const void *)k_sweep_batch<KM, true> : (const void *)k_sweep_batch<KM, false>;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     BatchArgs args = a;
     void *params[] = {&args};
-    return cudaLaunchCooperativeKernel((const void *)k_sweep_batch<KM>, dim3((unsigned)a.G), dim3(kBT), params, smem,
-                                       st);
+    return cudaLaunchCooperativeKernel(f, dim3((unsigned)a.G), dim3(kBT), params, smem, st);
 }
 
 }  // namespace
@@ -851,11 +853,17 @@ size_t batch_smem_bytes(int C, int kext, int G) { return batch_plan(C, kext, G).
 
 int batch_max_ctas_per_sm(int C, int kext, size_t smem)
 {
-    int n = 0;
-    if (cudaFuncSetAttribute(k_sweep_batch<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_batch<16>, kBT, smem) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
+    int n = 1 << 30;
+    const void *fs[4] = {(const void *)k_sweep_batch<4, false>, (const void *)k_sweep_batch<16, false>,
+                         (const void *)k_sweep_batch<4, true>, (const void *)k_sweep_batch<16, true>};
+    for (const void *f : fs) {
+        int m = 0;
+        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, f, kBT, smem) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        n = m < n ? m : n;
     }
     (void)C;
     (void)kext;

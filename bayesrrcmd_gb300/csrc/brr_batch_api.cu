@@ -82,6 +82,7 @@ struct brr_batch {
     uint32_t perm_next_it = UINT32_MAX;
     double last_sweep_ms = 0.0, last_total_ms = 0.0;
     long long phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    bool profile = false;   // phase counters on (brr_batch_set_profiling)
 
     StreamKey key(int c) const { return StreamKey{cfg.seed, cfg.chain + (uint32_t)c}; }
 };
@@ -525,7 +526,7 @@ int brr_batch_iterate(brr_batch *b, int32_t n_iter)
         a.part = b->d_part;
         a.err = b->d_err;
         a.timeout_ns = b->wait_limit_ns;
-        a.prof = b->d_prof;
+        a.prof = b->profile ? b->d_prof : nullptr;
         BATCH_CUDA(cudaEventRecord(b->ev[0], b->st));
         BATCH_CUDA(launch_sweep_batch(a, kmax, b->st));
         BATCH_CUDA(cudaEventRecord(b->ev[1], b->st));
@@ -644,6 +645,14 @@ int brr_batch_get_timing(brr_batch *b, double *sweep_ms, double *total_ms, int64
     if (cycles)
         for (int k = 0; k < 8; ++k)
             cycles[k] = b->phase[k];
+    return BRR_OK;
+}
+
+int brr_batch_set_profiling(brr_batch *b, int32_t on)
+{
+    if (!b || (on != 0 && on != 1))
+        return api_fail(BRR_ERR_ARG, "profiling is 0 or 1");
+    b->profile = on != 0;
     return BRR_OK;
 }
 

@@ -258,8 +258,10 @@ __device__ __forceinline__ double lut_select(unsigned c, double l0, double l1, d
 // --------------------------------------------------------------------------
 // The sweep of one chain over its G CTAs; sidx is this CTA's slice.  Run by
 // k_sweep (one chain per launch) and k_sweep_multi (several chains of
-// different sizes, each on its own group of CTAs, in one launch).
-template <int FORM, int KIND, int KM>
+// different sizes, each on its own group of CTAs, in one launch).  PROF: the
+// variant that counts phase cycles on the first CTA (the plain variant reads no
+// clock, whose reads would constrain the scheduling of every CTA's code).
+template <int FORM, int KIND, int KM, bool PROF>
 __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -415,7 +417,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     const Team tm = make_team(lpm);
     const int team = tid >> lpm_log2;
     const double Nm1 = (double)(a.N - 1);
-    const bool prof = a.prof != nullptr && sidx == 0 && tid == 0;
+    const bool prof = PROF && sidx == 0 && tid == 0;
     long long ph[6] = {0, 0, 0, 0, 0, 0};
     long long tp = prof ? clock64() : 0;
     auto mark = [&](int k) {
@@ -814,10 +816,10 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     }
 }
 
-template <int FORM, int KIND, int KM>
+template <int FORM, int KIND, int KM, bool PROF>
 __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
 {
-    sweep_body<FORM, KIND, KM>(a, (int)blockIdx.x);
+    sweep_body<FORM, KIND, KM, PROF>(a, (int)blockIdx.x);
 }
 
 // Several independent chains of different sizes in one cooperative launch:
@@ -832,9 +834,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep_multi(const __grid_consta
         ++i;
     const int sidx = (int)blockIdx.x - m.cta_start[i];
     if (m.kind[i] == kKindDense)
-        sweep_body<FORM, kKindDense, KM>(m.inst[i], sidx);
+        sweep_body<FORM, kKindDense, KM, false>(m.inst[i], sidx);
     else
-        sweep_body<FORM, kKindRagged, KM>(m.inst[i], sidx);
+        sweep_body<FORM, kKindRagged, KM, false>(m.inst[i], sidx);
 }
 
 // Sweep statistics from the resolved markers (src/BayesRBase.cpp:353-355):
@@ -934,23 +936,23 @@ size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a)
 template <int FORM, int KIND, int KM>
 static cudaError_t launch_one(const SweepArgs &a, size_t smem, cudaStream_t st)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_sweep<FORM, KIND, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const void *f = a.prof ? (const void *)k_sweep<FORM, KIND, KM, true> : (const void *)k_sweep<FORM, KIND, KM, false>;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     SweepArgs args = a;
     void *params[] = {&args};
-    return cudaLaunchCooperativeKernel((const void *)k_sweep<FORM, KIND, KM>, dim3(a.G), dim3(kThreads), params, smem,
-                                       st);
+    return cudaLaunchCooperativeKernel(f, dim3(a.G), dim3(kThreads), params, smem, st);
 }
 
-template <int KM>
+template <int KM, bool PROF>
 static const void *sweep_fn(int form, int kind)
 {
     if (form == kFormFP64)
-        return kind == kKindDense ? (const void *)k_sweep<kFormFP64, kKindDense, KM>
-                                  : (const void *)k_sweep<kFormFP64, kKindRagged, KM>;
-    return kind == kKindDense ? (const void *)k_sweep<kFormFP32C, kKindDense, KM>
-                              : (const void *)k_sweep<kFormFP32C, kKindRagged, KM>;
+        return kind == kKindDense ? (const void *)k_sweep<kFormFP64, kKindDense, KM, PROF>
+                                  : (const void *)k_sweep<kFormFP64, kKindRagged, KM, PROF>;
+    return kind == kKindDense ? (const void *)k_sweep<kFormFP32C, kKindDense, KM, PROF>
+                              : (const void *)k_sweep<kFormFP32C, kKindRagged, KM, PROF>;
 }
 
 template <int KM>
@@ -1025,14 +1027,17 @@ cudaError_t launch_sweep_multi(int form, int kmax, const MultiSweepArgs &m, size
 
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem)
 {
-    int n = 0, m = 0;
-    const void *f4 = sweep_fn<4>(form, kind), *f16 = sweep_fn<kMaxK>(form, kind);
-    cudaFuncSetAttribute(f4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(f16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f4, kThreads, smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, f16, kThreads, smem) != cudaSuccess)
-        return 0;
-    return n < m ? n : m;
+    int n = 1 << 30;
+    const void *fs[4] = {sweep_fn<4, false>(form, kind), sweep_fn<kMaxK, false>(form, kind),
+                         sweep_fn<4, true>(form, kind), sweep_fn<kMaxK, true>(form, kind)};
+    for (const void *f : fs) {
+        int m = 0;
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, f, kThreads, smem) != cudaSuccess)
+            return 0;
+        n = m < n ? m : n;
+    }
+    return n;
 }
 
 }  // namespace brr

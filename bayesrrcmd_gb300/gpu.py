@@ -65,7 +65,8 @@ EXPORTS = [
     "brr_get_gram_info",
     "brr_batch_create", "brr_batch_destroy", "brr_batch_pack_bed", "brr_batch_pack_bed_device",
     "brr_batch_set_groups", "brr_batch_set_phenotypes", "brr_batch_init", "brr_batch_iterate",
-    "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_get_geometry",
+    "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_set_profiling",
+    "brr_batch_get_geometry",
     "brr_multi_create", "brr_multi_destroy", "brr_multi_pack_bed", "brr_multi_pack_bed_device",
     "brr_multi_set_groups", "brr_multi_set_phenotype", "brr_multi_init", "brr_multi_tune", "brr_multi_iterate",
     "brr_multi_get_state", "brr_multi_get_timing", "brr_synth_bed_device_beta",
@@ -120,6 +121,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_batch_get_chain_state.argtypes = [P, C.c_int32, C.POINTER(BrrState)]
     lib.brr_batch_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_batch_set_wait_limit.argtypes = [P, C.c_uint64]
+    lib.brr_batch_set_profiling.argtypes = [P, C.c_int32]
     lib.brr_batch_get_geometry.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
     lib.brr_multi_create.argtypes = [C.POINTER(BrrConfig), C.c_int32, C.POINTER(P)]
     lib.brr_multi_destroy.argtypes = [P]
@@ -433,6 +435,10 @@ class Batch:
 
     def set_wait_limit(self, timeout_ns: int):
         self._check(self.lib.brr_batch_set_wait_limit(self.h, int(timeout_ns)))
+
+    def set_profiling(self, on: bool):
+        """Phase counters (timing()'s cycles) on or off; timed runs keep them off."""
+        self._check(self.lib.brr_batch_set_profiling(self.h, 1 if on else 0))
 
     def geometry(self):
         g, sl, sm = C.c_int32(), C.c_int32(), C.c_int64()

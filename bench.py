@@ -243,7 +243,11 @@ def run_batched(lib, gpu, torch, device, steps, warmup):
     torch.cuda.synchronize(device)
     bt.iterate(steps)
     torch.cuda.synchronize(device)
-    b_sweep, b_total, cyc = bt.timing()
+    b_sweep, b_total, _ = bt.timing()
+    # phase counters from one further iteration of the counting kernel variant
+    bt.set_profiling(True)
+    bt.iterate(1)
+    cyc = bt.timing()[2]
     bt.close()
     ch = gpu.Chain(gpu.ChainConfig(N=B_N, M=B_M, S=S, seed=seed, form=gpu.FORM_FP64, device=device), lib=lib)
     ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
@@ -268,7 +272,7 @@ def run_batched(lib, gpu, torch, device, steps, warmup):
     return dict(rate=rate, ms_per_step=b_total / steps, sweep_ms=b_sweep / steps, plain=plain,
                 plain_ms=p_total / p_steps, alg_tflops=alg_flop / sweep_s / 1e12,
                 issued_tflops=issued_flop / sweep_s / 1e12,
-                cycles=(cyc / steps / nblocks).tolist(), geometry=geo)
+                cycles=(cyc / nblocks).tolist(), geometry=geo)
 
 
 # Uneven batch: 32 independent regressions of different sizes in one launch per

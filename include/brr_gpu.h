@@ -230,6 +230,9 @@ int brr_batch_get_chain_state(brr_batch *b, int32_t chain, brr_state *st);
  * the resolve phase, the wait for all CTAs' dot products, chain 0's own
  * resolve, chain 0's sampling steps, and the wait for the slowest chain. */
 int brr_batch_get_timing(brr_batch *b, double *sweep_ms, double *total_ms, int64_t *cycles);
+/* Phase counters on (1) or off (0, the default; the cycles then read zero):
+ * the counting runs a variant of the sweep kernel with clock reads. */
+int brr_batch_set_profiling(brr_batch *b, int32_t on);
 int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns);
 /* CTAs of the sweep, individuals per slice and shared memory per CTA. */
 int brr_batch_get_geometry(brr_batch *b, int32_t *ctas, int32_t *slice, int64_t *smem_bytes);

@@ -112,3 +112,23 @@ def test_batch_too_many_individuals_for_64_chains(gpu_lib):
     with pytest.raises(gpu.BrrError) as e:
         gpu.Batch(gpu.ChainConfig(N=200000, M=10), 64)
     assert "does not fit" in str(e.value)
+
+
+def test_batch_phase_counting_variant_changes_no_result(gpu_lib):
+    """The phase-counting variant of the batched sweep computes the same chains
+    bit for bit; with counting off the cycles read zero."""
+    N, M, C = 1500, 200, 32
+    bed, ys = problem(N, M, C, 17)
+    plain = make_batch(bed, N, ys, S1, C, 5)
+    counted = make_batch(bed, N, ys, S1, C, 5)
+    counted.set_profiling(True)
+    plain.iterate(2)
+    counted.iterate(2)
+    for c in (0, 13, C - 1):
+        a, b = plain.state(c), counted.state(c)
+        for k in ("beta", "comp", "eps"):
+            np.testing.assert_array_equal(a[k], b[k])
+    assert (plain.timing()[2] == 0).all()
+    assert (counted.timing()[2] > 0).any()
+    plain.close()
+    counted.close()

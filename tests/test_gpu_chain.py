@@ -274,3 +274,27 @@ def test_gram_blocked_other_widths(gpu_lib, width):
         np.testing.assert_array_equal(s["comp"], o["comp"])
         nz = o["beta"] != 0
         np.testing.assert_allclose(s["beta"][nz], o["beta"][nz], rtol=1e-9, atol=1e-13)
+
+
+@pytest.mark.parametrize("gram,form", [(1, gpu.FORM_FP32C), (-1, gpu.FORM_FP32C), (-1, gpu.FORM_FP64)])
+def test_phase_counting_variant_changes_no_result(gpu_lib, gram, form):
+    """The phase-counting kernel variants (brr_set_profiling) compute the same
+    chain bit for bit; with counting off the counters read zero."""
+    N, M = 2500, 450
+    bed, y = problem(N, M, seed=71)
+    plain = make_gpu(bed, N, y, S1, 0, form=form, seed=6, gram=gram)
+    counted = make_gpu(bed, N, y, S1, 0, form=form, seed=6, gram=gram)
+    counted.set_profiling(True)
+    for _ in range(2):
+        plain.iterate(1)
+        counted.iterate(1)
+        a, b = plain.state(), counted.state()
+        for k in ("beta", "comp", "eps", "sigmaG"):
+            np.testing.assert_array_equal(a[k], b[k])
+        assert a["sigmaE"] == b["sigmaE"] and a["mu"] == b["mu"]
+    assert (plain.phase_cycles() == 0).all()
+    ph = counted.phase_cycles()
+    rounds = counted.timing()[2]
+    assert ph[5] == rounds > 0 and ph[3] > 0
+    plain.close()
+    counted.close()
