@@ -40,7 +40,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 N_IND, M_SNP = 100_000, 100_000
-DRAM_BYTES_PER_MARKER_N100K = 224.709725e9 * 1.312960e-3 / 8192
+DRAM_BYTES_PER_MARKER_N100K = 261.520286e9 * 1.287168e-3 / 8192
 S_GROUPS = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
 P_LO, P_HI = 0.01, 0.5
 N_CAUSAL, H2 = 1000, 0.4
