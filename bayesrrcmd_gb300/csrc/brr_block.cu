@@ -43,7 +43,20 @@
 //                           earlier) and assemble block r+1's inputs from its
 //                           published sums.
 // So neither the grid barrier's latency nor the input assembly is on the path
-// of the dot warps or of the resolve warp.
+// of the dot warps or of the resolve warp.  The ten warps other than the
+// resolve warp iterate in step (named barrier 3 at the top of each iteration);
+// the resolve warp runs on its own, tied to them by two signals in shared
+// memory (mbarriers, two per signal by block parity):
+//   GO(q)        320 arrivals in the others' iteration q-1: the dot threads
+//                after block q-2's update, the input warp after block q's
+//                inputs, the chore warp after block q-2's outputs; so block q
+//                can be resolved while the others finish iteration q-1;
+//   RESOLVED(q)  the resolve warp's 32 lanes after block q's decisions; the
+//                others wait for it at the top of iteration q+1.
+// Block q's decisions (parity q % 2) are read by the others in iteration q+1
+// and overwritten by block q+2, which waits for GO(q+2), i.e. for those reads;
+// a signal's next phase on the same mbarrier needs the other side's progress
+// past the previous one, so no phase is ever skipped.
 //
 // Buffers and why their counts suffice (iteration r: the dot warps publish
 // block r+2 and arrive at barrier r+2; the input warp passes barrier r+1 and
@@ -170,6 +183,24 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *m, unsigned bytes)
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *m)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
+}
+
+// Waits (suspending in hardware for a while) for the phase with the given
+// parity; false when the hardware's time window passed first.
+__device__ __forceinline__ bool mbar_try(uint64_t *m, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(m)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_test(uint64_t *m, unsigned parity)
 {
     unsigned ok;
@@ -211,6 +242,20 @@ __device__ __forceinline__ void dot_warps_sync() { asm volatile("bar.sync 1, 256
 // only signals it and goes on.
 __device__ __forceinline__ void arrive_sync() { asm volatile("bar.sync 2, 288;" ::: "memory"); }
 __device__ __forceinline__ void chore_signal() { asm volatile("bar.arrive 2, 288;" ::: "memory"); }
+
+// The ten warps other than the resolve warp: iteration barrier (named barrier
+// 3) with the OR of a flag over its 320 threads.
+constexpr int kOtherThreads = 320;
+__device__ __forceinline__ bool others_any(bool v)
+{
+    unsigned r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 3, 320, q;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(r)
+                 : "r"((unsigned)v)
+                 : "memory");
+    return r != 0;
+}
 
 // A double-float written by another CTA before a grid barrier this thread has
 // passed (read at L2, not from a stale L1 line).
@@ -521,6 +566,11 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     __shared__ long long s_D[kMaxSpec][4];   // residual change per update and code, fixed point
     __shared__ int s_abort;
     __shared__ int s_cp_issued;
+    // resolve warp <-> other warps: GO(q) on s_mb[q & 1] (320 arrivals: the dot
+    // threads after block q-2's update, the input warp after block q's inputs,
+    // the chore warp after block q-2's outputs), RESOLVED(q) on s_mb[2 + (q & 1)]
+    // (the resolve warp's 32 lanes after block q's decisions)
+    __shared__ __align__(8) uint64_t s_mb[4];
 
     const int B = a.B;
     const unsigned Bu = (unsigned)B;
@@ -531,6 +581,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     const int warp = tid >> 5, lane = tid & 31;
     const int dw = dot_index(warp);                       // dot warps: 0..7
     const int dtid = dw >= 0 ? dw * 32 + lane : kBlockThreads;   // dot warps: 0..255
+    const int otid = tid - (warp > kResolveWarp ? 32 : 0);       // the other warps: 0..319
     const int lo = a.slice_lo[sidx];
     const int ns = a.slice_lo[sidx + 1] - lo;
     const int nbytes = ((ns + kChunk - 1) / kChunk) * 16;
@@ -619,6 +670,10 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         s_nupd[1] = 0;
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
+        mbar_init(&s_mb[0], kOtherThreads);
+        mbar_init(&s_mb[1], kOtherThreads);
+        mbar_init(&s_mb[2], 32);
+        mbar_init(&s_mb[3], 32);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -626,13 +681,13 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
 
     // ---- ring of records and genotype code slices (cp.async)
     unsigned rec_issued = 0;
-    auto issue_recs = [&](unsigned upto) {
+    auto issue_recs = [&](unsigned upto, int idx, int stride) {
         upto = min(upto, M32);
         if (upto <= rec_issued)
             return;
         constexpr unsigned kParts = sizeof(BlockRec) / 16;
         const unsigned n = (upto - rec_issued) * kParts;
-        for (unsigned e = tid; e < n; e += kBlockThreads) {
+        for (unsigned e = (unsigned)idx; e < n; e += (unsigned)stride) {
             const unsigned q = rec_issued + e / kParts;
             const unsigned c = e % kParts;
             cp_async16(reinterpret_cast<unsigned char *>(&ring_rec[q & Rm]) + 16 * c,
@@ -1039,7 +1094,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     // ---- first blocks: records 0..3 and codes 0..2 resident; the Gram entries
     // of blocks 0..2 staged and blocks 0 and 1's dot products published before
     // the arrivals at barriers 0 and 1; block 0's inputs assembled
-    issue_recs(4u * Bu);
+    issue_recs(4u * Bu, tid, kBlockThreads);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
@@ -1075,79 +1130,48 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     if (prof_d || prof_r)
         tp = clk();
     // profiling: per role, the clock from the iteration's start to the end of
-    // its work (dot side on thread 0, chore warp, resolve warp)
+    // its work (dot side on thread 0, chore warp, resolve warp, input warp)
     long long t_it = 0, t_end = 0;
     const bool prof_e = PROF && sidx == 0 && (tid & 31) == 0 &&
                         (tid == 0 || warp == kChoreWarp || warp == kResolveWarp || warp == kInputWarp);
-    for (; r < nblk; ++r) {
-        cp_async_wait_all();
-        __syncthreads();
-        if (s_abort)
-            break;
-        if (prof_e)
-            t_it = clk();
-        mark(prof_d, 0);
-        issue_recs((unsigned)(r + 4) * Bu);
-        cp_async_commit();
-        const unsigned q0 = (unsigned)r * Bu;
-        const int nb = nb_of(r);
-
-        if (warp == kChoreWarp) {
-            // ---- chore warp: Gram copy of block r+1 (its staging was published
-            // by barrier r, which this warp passed in the previous iteration;
-            // blocks 0..2 by barrier 0), issued early so that the L2 burst of
-            // 152 CTAs copying the same slot overlaps the dot products; staged
-            // Gram entries of block r+3 (loaded in the previous iteration) and
-            // the zeroed accumulators of block r+4, signalled to the dot warps
-            // before their arrival at barrier r+2; then the Gram loads of
-            // block r+4 and the outputs of block r-1
-            if (lane == 0) {
-                fence_proxy_async();
-                if (r == 0) {
-                    mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
-                    bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
-                    cp_issued = 0;
-                }
-                if (r + 1 < nblk) {
-                    const int q = r + 1;
-                    mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
-                    bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gst,
-                                  (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
-                    cp_issued = q;
+    // Waits for a role signal, at most the wait limit; false on timeout or
+    // when another warp aborted.
+    auto role_wait = [&](uint64_t *m, unsigned parity) -> bool {
+        if (mbar_test(m, parity))
+            return true;
+        const uint64_t t0 = global_timer_ns();
+        unsigned spins = 0;
+        while (!mbar_try(m, parity)) {
+            if ((++spins & 15u) == 0) {
+                if (*(volatile int *)&s_abort)
+                    return false;
+                if (global_timer_ns() - t0 > a.timeout_ns) {
+                    atomicCAS(a.err, kDevOk, kDevTimeout);
+                    s_abort = 1;
+                    return false;
                 }
             }
-            if (r + 3 < nblk)
-                gather_store(r + 3);
-            if (sidx == 0 && r + 4 < nblk)
-                for (int i = lane; i < kAccBufWords; i += 32)
-                    a.acc[(size_t)((r + 4) % kAccBufs) * kAccBufWords + i] = 0ull;
-            __syncwarp();
-            chore_signal();
-            if (r + 4 < nblk)
-                gather_load(r + 4);
-            if (r >= 1 && sidx == (r - 1) % a.G)
-                write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
-        } else if (warp == kInputWarp) {
-            // ---- input warp: block r+1's inputs
-            if (r + 1 < nblk)
-                prepare_inputs(r + 1, prof_h);
-        } else if (dw >= 0) {
-            // ---- dot side: update of block r-1, the code slices of block r+3
-            // into the slot block r-1 held, dots of block r+2 and their
-            // publication
-            prefetch_code_ids(r + 3);
-            if (r >= 1)
-                apply_update(r - 1);
-            mark(prof_d, 4);
-            issue_block_codes(r + 3, false);
-            cp_async_commit();
-            if (r + 2 < nblk)
-                dot_block(r + 2);
-            arrive_sync();
-            if (tid == 0 && r + 2 < nblk)
-                arrive(r + 2);
-            mark(prof_d, 1);
-        } else {
+        }
+        return true;
+    };
+    // GO(0): block 0's inputs and records are in place
+    cp_async_wait_all();
+    __syncthreads();
+    if (warp != kResolveWarp)
+        mbar_arrive(&s_mb[0]);
+
+    if (warp == kResolveWarp) {
+        // ---- resolve warp: block r once GO(r) (inputs of block r, the
+        // residual-changing markers of block r-2 applied and read, its outputs
+        // read), then RESOLVED(r)
+        for (; r < nblk; ++r) {
+            const bool ok = role_wait(&s_mb[r & 1], (unsigned)((r >> 1) & 1));
+            if (__any_sync(0xffffffffu, !ok || *(volatile int *)&s_abort != 0))
+                break;
+            if (prof_e)
+                t_it = clk();
+            const unsigned q0 = (unsigned)r * Bu;
+            const int nb = nb_of(r);
             // ---- resolve side
             mark(prof_r, 8);
             {
@@ -1364,14 +1388,92 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                     mark(prof_r, 3);
                 }
             }
+            if (prof_e)
+                t_end += clk() - t_it;
+            __syncwarp();
+            mbar_arrive(&s_mb[2 + (r & 1)]);   // RESOLVED(r)
         }
-        if (prof_e)
-            t_end += clk() - t_it;
-        __syncthreads();
-        mark(prof_d, 11);
-        if (s_abort)
-            break;
+    } else {
+        // ---- the other warps, iteration r once block r-1 is resolved (its
+        // decisions, and the ring and shared Gram slots it read, are free);
+        // the iteration ends with the others' barrier (cp.async data of every
+        // thread visible)
+        for (; r < nblk; ++r) {
+            const bool ok = r == 0 || role_wait(&s_mb[2 + ((r - 1) & 1)], (unsigned)(((r - 1) >> 1) & 1));
+            if (others_any(!ok || *(volatile int *)&s_abort != 0))
+                break;
+            if (prof_e)
+                t_it = clk();
+            mark(prof_d, 0);
+            issue_recs((unsigned)(r + 4) * Bu, otid, kOtherThreads);
+            cp_async_commit();
+
+            if (warp == kChoreWarp) {
+                // ---- chore warp: Gram copy of block r+1 (its staging was published
+                // by barrier r, which this warp passed in the previous iteration;
+                // blocks 0..2 by barrier 0), issued early so that the L2 burst of
+                // 152 CTAs copying the same slot overlaps the dot products; staged
+                // Gram entries of block r+3 (loaded in the previous iteration) and
+                // the zeroed accumulators of block r+4, signalled to the dot warps
+                // before their arrival at barrier r+2; then the Gram loads of
+                // block r+4 and the outputs of block r-1
+                if (lane == 0) {
+                    fence_proxy_async();
+                    if (r == 0) {
+                        mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
+                        bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
+                        cp_issued = 0;
+                    }
+                    if (r + 1 < nblk) {
+                        const int q = r + 1;
+                        mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
+                        bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gst,
+                                      (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
+                        cp_issued = q;
+                    }
+                }
+                if (r + 3 < nblk)
+                    gather_store(r + 3);
+                if (sidx == 0 && r + 4 < nblk)
+                    for (int i = lane; i < kAccBufWords; i += 32)
+                        a.acc[(size_t)((r + 4) % kAccBufs) * kAccBufWords + i] = 0ull;
+                __syncwarp();
+                chore_signal();
+                if (r + 4 < nblk)
+                    gather_load(r + 4);
+                if (r >= 1 && sidx == (r - 1) % a.G)
+                    write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
+                mbar_arrive(&s_mb[(r + 1) & 1]);   // GO(r+1): block r-1's outputs read
+            } else if (warp == kInputWarp) {
+                // ---- input warp: block r+1's inputs
+                if (r + 1 < nblk)
+                    prepare_inputs(r + 1, prof_h);
+                mbar_arrive(&s_mb[(r + 1) & 1]);   // GO(r+1): block r+1's inputs
+            } else if (dw >= 0) {
+                // ---- dot side: update of block r-1, the code slices of block r+3
+                // into the slot block r-1 held, dots of block r+2 and their
+                // publication
+                prefetch_code_ids(r + 3);
+                if (r >= 1)
+                    apply_update(r - 1);
+                mbar_arrive(&s_mb[(r + 1) & 1]);   // GO(r+1): block r-1's decisions applied
+                mark(prof_d, 4);
+                issue_block_codes(r + 3, false);
+                cp_async_commit();
+                if (r + 2 < nblk)
+                    dot_block(r + 2);
+                arrive_sync();
+                if (tid == 0 && r + 2 < nblk)
+                    arrive(r + 2);
+                mark(prof_d, 1);
+            }
+            if (prof_e)
+                t_end += clk() - t_it;
+            cp_async_wait_all();
+            mark(prof_d, 11);
+        }
     }
+    __syncthreads();
     // the last block: residual update and outputs
     if (!s_abort && r == nblk) {
         if (dw >= 0)
