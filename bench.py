@@ -136,6 +136,24 @@ def dist_setup(gpus):
     return rank, world, None
 
 
+def max_over_ranks(x: float, dist, device=None) -> float:
+    """The largest of every rank's x (one rank: x itself).  The tensor lives on
+    the rank's GPU under NCCL and on the host under gloo."""
+    if dist is None:
+        return float(x)
+    import torch
+    on = "cpu" if dist.get_backend() == "gloo" else device
+    t = torch.tensor([float(x)], dtype=torch.float64, device=on)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, markers: int, steps: int, seconds: float) -> float:
+    """Whole-job marker-updates/s of `world` replicas that each swept `markers`
+    markers `steps` times, the slowest taking `seconds`."""
+    return world * markers * steps / seconds
+
+
 def make_problem(lib, gpu, torch, device, chain_id):
     """Synthetic BED payload on the device, phenotype from 1,000 causal markers."""
     cb = (N_IND + 3) // 4
@@ -153,7 +171,10 @@ def make_problem(lib, gpu, torch, device, chain_id):
     return d_bed, y, group
 
 
-def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chain_id, profile=False):
+def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chain_id, barrier, profile=False):
+    """Warm-up iterations, then exactly `steps` timed iterations between two
+    barriers (device synchronised on every rank); the time reported is the
+    library's CUDA-event time of those iterations."""
     cfg = gpu.ChainConfig(N=N_IND, M=M_SNP, S=S_GROUPS, form=form, seed=SEED + chain_id, chain=chain_id,
                           refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device)
     ch = gpu.Chain(cfg, lib=lib)
@@ -163,10 +184,10 @@ def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chai
     ch.init()
     gram = ch.gram_info()
     ch.iterate(warmup)
-    torch.cuda.synchronize(device)
+    barrier()
     t0 = time.perf_counter()
     ch.iterate(steps)
-    torch.cuda.synchronize(device)
+    barrier()
     wall = time.perf_counter() - t0
     sweep_ms, total_ms, rounds = ch.timing()
     st = ch.state()
@@ -269,7 +290,8 @@ def run_batched(lib, gpu, torch, device, steps, warmup):
     sweep_s = b_sweep / 1e3 / steps
     rate = B_C * B_M * steps / (b_total / 1e3)
     plain = B_M * p_steps / (p_total / 1e3)
-    return dict(rate=rate, ms_per_step=b_total / steps, sweep_ms=b_sweep / steps, plain=plain,
+    return dict(rate=rate, total_s=b_total / 1e3, ms_per_step=b_total / steps, sweep_ms=b_sweep / steps,
+                plain=plain,
                 plain_ms=p_total / p_steps, alg_tflops=alg_flop / sweep_s / 1e12,
                 issued_tflops=issued_flop / sweep_s / 1e12,
                 cycles=(cyc / nblocks).tolist(), geometry=geo)
@@ -338,7 +360,8 @@ def run_uneven(lib, gpu, torch, device, steps, tune_rounds, scale=1.0):
     mm.close()
     total_m = int(M.sum())
     inst = t["inst_ms"]
-    return dict(rate=total_m * steps / (t["total_ms"] / 1e3), ms_per_step=t["total_ms"] / steps,
+    return dict(rate=total_m * steps / (t["total_ms"] / 1e3), total_s=t["total_ms"] / 1e3,
+                ms_per_step=t["total_ms"] / steps,
                 sweep_ms=t["sweep_ms"] / steps, instances=len(N), total_markers=total_m,
                 total_genotypes=float((N.astype(float) * M.astype(float)).sum()),
                 kinds={"dense": kinds.count(gpu.KIND_DENSE), "ragged": kinds.count(gpu.KIND_RAGGED)},
@@ -466,16 +489,13 @@ def main():
     barrier()
     with ClockSampler(device) as clk:
         fp32c = run_form(lib, gpu, torch, device, d_bed, y, group, gpu.FORM_FP32C, args.steps, args.warmup, rank,
-                         profile=True)
+                         barrier, profile=True)
     barrier()
-    fp64 = run_form(lib, gpu, torch, device, d_bed, y, group, gpu.FORM_FP64, args.steps, args.warmup, rank)
+    fp64 = run_form(lib, gpu, torch, device, d_bed, y, group, gpu.FORM_FP64, args.steps, args.warmup, rank,
+                    barrier)
     barrier()
-    t_chosen = fp32c["total_ms"] / 1e3
-    if dist:
-        t = torch.tensor([t_chosen], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_chosen = float(t.item())
-    value = world * M_SNP * args.steps / t_chosen
+    t_chosen = max_over_ranks(fp32c["total_ms"] / 1e3, dist, device)
+    value = replica_rate(world, M_SNP, args.steps, t_chosen)
     host_t = torch.empty(d_bed.numel(), dtype=torch.uint8, pin_memory=True)
     host_t.copy_(d_bed)
     host_bed = host_t.numpy()
@@ -485,7 +505,8 @@ def main():
         # one-time upload, packing and marker-Gram build are paid once per chain
         e2e_steps = int(os.environ.get("BRR_E2E_STEPS", "200"))
         e = run_e2e(lib, gpu, torch, device, host_bed, y, group, e2e_steps, rank)
-        e2e = {"value": world * M_SNP * e2e_steps / e["wall"], "unit": "marker-updates/s",
+        e2e = {"value": replica_rate(world, M_SNP, e2e_steps, max_over_ranks(e["wall"], dist, device)),
+               "unit": "marker-updates/s",
                "h2d_bytes_per_step": int(e["h2d_per_step"]), "d2h_bytes_per_step": int(e["d2h_per_step"]),
                "includes": f"chain of {e2e_steps} iterations: pinned-host BED upload + device packing + "
                            f"marker Gram + init, then per iteration the sample read-back"}
@@ -495,7 +516,9 @@ def main():
         bb = run_batched(lib, gpu, torch, device, bsteps, max(args.warmup, 2))
         bf16_peak = peaks_bf16()
         batched = {
-            "workload": B_WORKLOAD, "value": bb["rate"] * world, "unit": "marker-updates/s (all chains)",
+            "workload": B_WORKLOAD,
+            "value": replica_rate(world, B_C * B_M, bsteps, max_over_ranks(bb["total_s"], dist, device)),
+            "unit": "marker-updates/s (all chains)",
             "chains": B_C, "steps": bsteps, "ms_per_step": bb["ms_per_step"], "sweep_ms": bb["sweep_ms"],
             "plain_fp64_same_genotypes": {"value": bb["plain"], "unit": "marker-updates/s (one chain)",
                                           "ms_per_step": bb["plain_ms"]},
@@ -513,7 +536,8 @@ def main():
     if not args.no_uneven and not args.small:
         usteps = int(os.environ.get("BRR_UNEVEN_STEPS", "3"))
         uu = run_uneven(lib, gpu, torch, device, usteps, 2)
-        uneven = {"workload": U_WORKLOAD, "value": uu["rate"] * world,
+        u_value = replica_rate(world, uu["total_markers"], usteps, max_over_ranks(uu["total_s"], dist, device))
+        uneven = {"workload": U_WORKLOAD, "value": u_value,
                   "unit": "marker-updates/s (all instances)", "steps": usteps, "ms_per_step": uu["ms_per_step"],
                   "sweep_ms": uu["sweep_ms"], "instances": uu["instances"], "total_markers": uu["total_markers"],
                   "total_genotypes": uu["total_genotypes"], "kinds": uu["kinds"],
@@ -549,7 +573,7 @@ def main():
         "data": "synthetic (seeded, generated on the device)",
         "config": {"workload": WORKLOAD, "form": "fp32c" + (" gram-blocked" if fp32c["gram"]["blocked"] else ""),
                    "refresh_every": REFRESH,
-                   "l2": "inputs larger than L2 (2.5 GB of codes per sweep)", "parallelism": "replicas" if world > 1 else "1 chain"},
+                   "l2": f"inputs larger than L2 ({M_SNP * N_IND / 4 / 1e9:.2g} GB of codes per sweep)", "parallelism": "replicas" if world > 1 else "1 chain"},
         "plain_fp64": {"value": plain_rate, "unit": "marker-updates/s", "ms_per_step": fp64["total_ms"] / args.steps,
                        "speedup_chosen_vs_plain": value / world / plain_rate,
                        "rounds_per_step": fp64["rounds"] / args.steps},
