@@ -200,7 +200,7 @@ def run_form(lib, gpu, torch, device, d_bed, y, group, form, steps, warmup, chai
         phases = ch.phase_cycles()
     ch.close()
     return dict(total_ms=total_ms, sweep_ms=sweep_ms, rounds=rounds, wall_s=wall, phases=phases.tolist(),
-                beta=st["beta"], sigmaE=st["sigmaE"], sigmaG=st["sigmaG"].tolist(), gram=gram)
+                beta=st["beta"], comp=st["comp"], sigmaE=st["sigmaE"], sigmaG=st["sigmaG"].tolist(), gram=gram)
 
 
 def run_e2e(lib, gpu, torch, device, host_bed, y, group, steps, chain_id):
@@ -579,6 +579,11 @@ def main():
                        "rounds_per_step": fp64["rounds"] / args.steps},
         "matched_error": {"beta_max_abs_diff_vs_plain": float(np.abs(fp32c["beta"] - fp64["beta"]).max()),
                           "sigmaE_rel_diff_vs_plain": abs(fp32c["sigmaE"] / fp64["sigmaE"] - 1),
+                          "sigmaG_max_rel_diff_vs_plain": float(np.max(np.abs(np.asarray(fp32c["sigmaG"]) /
+                                                                               np.asarray(fp64["sigmaG"]) - 1))),
+                          "component_mismatches_vs_plain": int(np.count_nonzero(fp32c["comp"] != fp64["comp"])),
+                          "component_counts_plain": np.bincount(fp64["comp"], minlength=4).tolist(),
+                          "compared": "final state after the warm-up and timed iterations (same draws)",
                           "nonzero_beta_plain": int(nzb.sum())},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
