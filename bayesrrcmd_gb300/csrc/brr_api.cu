@@ -77,6 +77,65 @@ void make_permutation(StreamKey key, uint32_t it, uint32_t M, uint32_t *perm)
 
 namespace {
 
+template <class T>
+void drop_dev(T *&p)
+{
+    cudaFree(p);
+    p = nullptr;
+}
+
+template <class T>
+void drop_host(T *&p)
+{
+    cudaFreeHost(p);
+    p = nullptr;
+}
+
+// Releases the buffers the first brr_pack_bed_device call allocates and
+// nulls their pointers, so that a call that ran out of memory part-way leaves
+// the context as before and a later call allocates them all again.
+void release_pack_buffers(brr_ctx &c)
+{
+    drop_dev(c.d_codes);
+    drop_dev(c.d_counts);
+    drop_dev(c.d_table);
+    drop_dev(c.d_scale);
+    drop_dev(c.d_colsum);
+    drop_dev(c.d_chosen);
+    drop_dev(c.d_vstat);
+    drop_dev(c.d_slice_lo);
+    drop_dev(c.d_beta);
+    drop_dev(c.d_comp);
+    drop_dev(c.d_acum);
+    drop_dev(c.d_order);
+    drop_dev(c.d_u);
+    drop_dev(c.d_z);
+    drop_dev(c.d_rec);
+    drop_dev(c.d_acc);
+    drop_dev(c.d_gconst);
+    drop_dev(c.d_gK);
+    drop_dev(c.d_stats);
+    drop_dev(c.d_part);
+    drop_dev(c.d_err);
+    drop_dev(c.d_rounds);
+    drop_dev(c.d_prof);
+    drop_dev(c.d_gstage);
+    drop_dev(c.d_group);
+    drop_dev(c.d_ystd);
+    drop_dev(c.d_nzj);
+    drop_dev(c.d_nzb);
+    drop_dev(c.d_eps);
+    drop_dev(c.d_eps_hi);
+    drop_dev(c.d_eps_lo);
+    drop_host(c.h_order);
+    drop_host(c.h_stats);
+    drop_host(c.h_part);
+    drop_host(c.h_gc);
+    drop_host(c.h_gK);
+    drop_host(c.h_vstat);
+    drop_host(c.h_misc);
+}
+
 void free_all(brr_ctx *c)
 {
     if (c->perm_future.valid())
@@ -828,14 +887,20 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
             dalloc(&c.d_stats, (size_t)cf.n_groups * kMaxK + cf.n_groups + 1) ||
             dalloc(&c.d_part, (size_t)std::max(2 * c.G, kPartBlocks)) || dalloc(&c.d_err, 1) ||
             dalloc(&c.d_rounds, 1) || dalloc(&c.d_prof, 16) || dalloc(&c.d_gstage, sweep_block_stage_bytes(kMaxSpec) / sizeof(double)) || dalloc(&c.d_group, (size_t)M) || dalloc(&c.d_ystd, (size_t)cf.N) ||
-            dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M))
+            dalloc(&c.d_nzj, (size_t)M) || dalloc(&c.d_nzb, (size_t)M)) {
+            release_pack_buffers(c);
             return fail(BRR_ERR_OOM, "device allocation failed");
+        }
         if (cf.form == BRR_FORM_FP64) {
-            if (dalloc(&c.d_eps, (size_t)cf.N))
+            if (dalloc(&c.d_eps, (size_t)cf.N)) {
+                release_pack_buffers(c);
                 return fail(BRR_ERR_OOM, "device allocation failed");
+            }
         } else {
-            if (dalloc(&c.d_eps_hi, (size_t)cf.N) || dalloc(&c.d_eps_lo, (size_t)cf.N))
+            if (dalloc(&c.d_eps_hi, (size_t)cf.N) || dalloc(&c.d_eps_lo, (size_t)cf.N)) {
+                release_pack_buffers(c);
                 return fail(BRR_ERR_OOM, "device allocation failed");
+            }
         }
         if (cudaMallocHost((void **)&c.h_order, sizeof(uint32_t) * M) != cudaSuccess ||
             cudaMallocHost((void **)&c.h_stats, sizeof(double) * ((size_t)cf.n_groups * kMaxK + cf.n_groups + 1)) !=
@@ -845,8 +910,10 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
             cudaMallocHost((void **)&c.h_gK, sizeof(int32_t) * (size_t)cf.n_groups) != cudaSuccess ||
             cudaMallocHost((void **)&c.h_vstat, sizeof(unsigned long long) * ((size_t)cf.n_groups * kMaxK + 2 * cf.n_groups)) !=
                 cudaSuccess ||
-            cudaMallocHost((void **)&c.h_misc, sizeof(long long) * 18) != cudaSuccess)
+            cudaMallocHost((void **)&c.h_misc, sizeof(long long) * 18) != cudaSuccess) {
+            release_pack_buffers(c);
             return fail(BRR_ERR_OOM, "pinned host allocation failed");
+        }
         BRR_CUDA(cudaMemset(c.d_group, 0, sizeof(int32_t) * M));
         c.group.assign(M, 0);
     }
@@ -856,16 +923,19 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     if (dalloc(&d_bad, 1))
         return fail(BRR_ERR_OOM, "device allocation failed");
     const int big = INT_MAX;
-    cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
-    if (cf.kind == BRR_KIND_DENSE) {
-        BRR_CUDA(launch_dense_tables(c.d_counts, cf.N, M, c.d_table, c.d_scale, c.d_colsum, d_bad, c.st));
-    } else {
-        BRR_CUDA(launch_ragged_stats(c.d_counts, cf.N, M, c.eigen ? 1 : 0, c.d_table, d_bad, c.st));
-    }
     int bad = INT_MAX;
-    cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c.st);
-    cudaStreamSynchronize(c.st);
+    cudaError_t le = cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
+    if (le == cudaSuccess)
+        le = cf.kind == BRR_KIND_DENSE
+                 ? launch_dense_tables(c.d_counts, cf.N, M, c.d_table, c.d_scale, c.d_colsum, d_bad, c.st)
+                 : launch_ragged_stats(c.d_counts, cf.N, M, c.eigen ? 1 : 0, c.d_table, d_bad, c.st);
+    if (le == cudaSuccess)
+        le = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c.st);
+    if (le == cudaSuccess)
+        le = cudaStreamSynchronize(c.st);
     cudaFree(d_bad);
+    if (le != cudaSuccess)
+        return fail(BRR_ERR_CUDA, std::string("marker statistics: ") + cudaGetErrorString(le));
     BRR_CUDA(cudaGetLastError());
     if (bad != INT_MAX)
         return fail(BRR_ERR_MARKER, "marker " + std::to_string(bad) +

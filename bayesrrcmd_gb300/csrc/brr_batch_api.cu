@@ -107,6 +107,51 @@ void free_batch(brr_batch *b)
         cudaStreamDestroy(b->st);
 }
 
+template <class T>
+void drop_dev(T *&p)
+{
+    cudaFree(p);
+    p = nullptr;
+}
+
+// Releases the buffers the first pack call allocates and nulls their
+// pointers, so that a call that ran out of memory part-way leaves the batch as
+// before and a later call allocates them all again.
+void release_pack_buffers(brr_batch *b)
+{
+    drop_dev(b->d_codes);
+    drop_dev(b->d_counts);
+    drop_dev(b->d_lut);
+    drop_dev(b->d_scale);
+    drop_dev(b->d_colsum);
+    drop_dev(b->d_slice_lo);
+    drop_dev(b->d_group);
+    drop_dev(b->d_gK);
+    drop_dev(b->d_order);
+    drop_dev(b->d_rec);
+    drop_dev(b->d_crec);
+    drop_dev(b->d_gcf);
+    drop_dev(b->d_gdf);
+    drop_dev(b->d_beta);
+    drop_dev(b->d_acum);
+    drop_dev(b->d_comp);
+    drop_dev(b->d_chosen);
+    drop_dev(b->d_gconst);
+    drop_dev(b->d_E);
+    drop_dev(b->d_dmu);
+    drop_dev(b->d_sumE);
+    drop_dev(b->d_wx);
+    drop_dev(b->d_prof);
+    drop_dev(b->d_acc);
+    drop_dev(b->d_counter);
+    drop_dev(b->d_stats);
+    drop_dev(b->d_pacc);
+    drop_dev(b->d_part);
+    drop_dev(b->d_err);
+    cudaFreeHost(b->h_order);
+    b->h_order = nullptr;
+}
+
 size_t acc_words(int C) { return (size_t)kBatchCopies * C * kBatchBlock; }
 size_t pacc_words() { return (size_t)2 * kBatchPCopies * kBatchBlock * kBatchBlock; }
 size_t stats_words(int C, int ng) { return (size_t)C * (ng * kMaxK + 2 * ng); }
@@ -299,6 +344,7 @@ int brr_batch_pack_bed_device(brr_batch *b, const uint8_t *d_bed, int64_t nbytes
             balloc(&b->d_part, (size_t)b->G * C * 2) || balloc(&b->d_err, 1) ||
             cudaMallocHost((void **)&b->h_order, sizeof(uint32_t) * M) != cudaSuccess) {
             cudaGetLastError();
+            release_pack_buffers(b);
             return api_fail(BRR_ERR_OOM, "device allocation for the batched chains failed");
         }
         BATCH_CUDA(cudaMemset(b->d_group, 0, sizeof(int32_t) * M));
@@ -310,12 +356,17 @@ int brr_batch_pack_bed_device(brr_batch *b, const uint8_t *d_bed, int64_t nbytes
     if (balloc(&d_bad, 1))
         return api_fail(BRR_ERR_OOM, "device allocation failed");
     const int big = INT_MAX;
-    cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
-    BATCH_CUDA(launch_dense_tables(b->d_counts, cf.N, M, b->d_lut, b->d_scale, b->d_colsum, d_bad, b->st));
     int bad = INT_MAX;
-    cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, b->st);
-    cudaStreamSynchronize(b->st);
+    cudaError_t le = cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
+    if (le == cudaSuccess)
+        le = launch_dense_tables(b->d_counts, cf.N, M, b->d_lut, b->d_scale, b->d_colsum, d_bad, b->st);
+    if (le == cudaSuccess)
+        le = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, b->st);
+    if (le == cudaSuccess)
+        le = cudaStreamSynchronize(b->st);
     cudaFree(d_bad);
+    if (le != cudaSuccess)
+        return api_fail(BRR_ERR_CUDA, std::string("marker statistics: ") + cudaGetErrorString(le));
     BATCH_CUDA(cudaGetLastError());
     if (bad != INT_MAX)
         return api_fail(BRR_ERR_MARKER, "marker " + std::to_string(bad) +
