@@ -37,6 +37,28 @@
  *                         with caller-supplied per-marker draws
  *   brr_get_state /       the BayesRBase members written to the sample file
  *   brr_set_state         (src/BayesRBase.hpp:63-96, src/BayesRBase.cpp:251)
+ *   brr_ctx_create /      construction of the analysis from Data and Options
+ *   brr_ctx_destroy       (src/BayesRBase.cpp:18, src/DenseBayesRRmz.cpp:13,
+ *                         src/SparseBayesRRG.cpp:8; the option fields used are
+ *                         those of src/options.hpp:21-105)
+ *   brr_pack_bed_device   brr_pack_bed with the payload already on the device
+ *   brr_get_timing        the per-iteration and flow-graph durations runGibbs
+ *                         measures and prints (src/BayesRBase.cpp:178-184,
+ *                         :208-210, :257-260, :277-282)
+ *   brr_refresh_eps       no counterpart: the FP64 residual refresh of the
+ *                         FP32-compensated form (the reference keeps eps in FP64)
+ *   brr_xbeta             no counterpart: genetic values X b of the packed
+ *                         markers, for simulating phenotypes and for prediction
+ *   brr_synth_bed_device* no counterpart: seeded synthetic BED payloads on the
+ *                         device, a data source for benchmarks
+ *   brr_set_wait_limit,   no counterpart: limits of the device-side waits, the
+ *   brr_get_gram_info,    marker Gram of the blocked sweep, and phase counters
+ *   brr_get_phase_cycles, (the device counterpart of the timing log above)
+ *   brr_set_profiling
+ *   brr_batch_*,          no single counterpart: each chain (instance) is
+ *   brr_multi_*           BayesRBase::runGibbs (src/BayesRBase.cpp:186-274) on its
+ *                         own phenotype and seed; the reference runs them as
+ *                         separate processes
  */
 #ifndef BRR_GPU_H
 #define BRR_GPU_H
