@@ -323,6 +323,9 @@ private:
 // src/BayesRBase.cpp:130-285)
 bool ppbayes(const Options &opt)
 {
+    if (opt.fixedEffectNumber != 0)
+        throw std::string("Error: --fixedEffectNumber " + std::to_string(opt.fixedEffectNumber) +
+                          ": fixed effects are not supported by the GPU sampler");
     Data data;
     readMetaData(data, opt);
     if (opt.S.empty())
@@ -348,6 +351,22 @@ bool ppbayes(const Options &opt)
     std::ofstream iterLog;
     if (opt.iterLog)
         iterLog.open(opt.iterLogFile);
+    // The reference's column log holds per-marker microseconds of num, beta and
+    // the epsilon update (src/BayesRBase.cpp:381-389).  On the GPU markers are
+    // swept in blocks by many warps at once, so its counterpart is the sweep's
+    // phase counters: the counting kernel variant (the same chain bit for bit)
+    // and one row per iteration of the 16 counters of brr_get_phase_cycles.
+    std::ofstream colLog;
+    if (opt.colLog) {
+        colLog.open(opt.colLogFile);
+        if (!colLog)
+            throw std::string("Error: cannot open the column log " + opt.colLogFile);
+        check(brr_set_profiling(ctx.h, 1), "brr_set_profiling");
+        colLog << "iter";
+        for (int k = 0; k < 16; ++k)
+            colLog << ",phase" << k;
+        colLog << std::endl;
+    }
     std::vector<double> beta(M), acum(M), eps(N);
     std::vector<int32_t> comp(M);
     brr_state st{};
@@ -373,6 +392,14 @@ bool ppbayes(const Options &opt)
         std::cout << secs << "s (" << sweep_ms / 1000.0 << "s)" << std::endl;
         meanIter += secs;
         meanSweep += sweep_ms / 1000.0;
+        if (opt.colLog) {
+            int64_t cyc[16] = {0};
+            check(brr_get_phase_cycles(ctx.h, cyc), "brr_get_phase_cycles");
+            colLog << it;
+            for (int k = 0; k < 16; ++k)
+                colLog << "," << cyc[k];
+            colLog << std::endl;
+        }
         if (opt.iterLog) {
             brr_state sc{};
             check(brr_get_state(ctx.h, &sc), "brr_get_state");
@@ -397,7 +424,8 @@ void printOptions(const Options &o)
               << ", \"data\": \"" << o.dataFile << "\", \"pheno\": \"" << o.phenotypeFile << "\", \"chain\": "
               << o.chainLength << ", \"burnin\": " << o.burnin << ", \"thin\": " << o.thin << ", \"seed\": " << o.seed
               << ", \"samples\": \"" << o.mcmcSampleFile << "\", \"sparse\": " << (int)o.preprocessDataType
-              << ", \"form\": \"" << o.form << "\", \"S\": [";
+              << ", \"form\": \"" << o.form << "\", \"colLog\": \"" << (o.colLog ? o.colLogFile : "")
+              << "\", \"fixed\": " << o.fixedEffectNumber << ", \"failure\": \"" << o.failureFile << "\", \"S\": [";
     for (std::size_t g = 0; g < o.S.size(); ++g) {
         std::cout << (g ? ", " : "") << "[";
         for (std::size_t k = 0; k < o.S[g].size(); ++k)

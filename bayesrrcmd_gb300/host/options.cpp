@@ -195,6 +195,13 @@ void Options::inputOptions(int argc, const char *argv[])
         } else if (!std::strcmp(a, "--iterLog")) {
             iterLog = true;
             iterLogFile = need(i);
+        } else if (!std::strcmp(a, "--colLog")) {
+            colLog = true;
+            colLogFile = need(i);
+        } else if (!std::strcmp(a, "--fixedEffectNumber")) {
+            fixedEffectNumber = (unsigned)std::atoi(need(i));
+        } else if (!std::strcmp(a, "--failure")) {
+            failureFile = need(i);
         } else if (!std::strcmp(a, "--marker-cache")) {
             useMarkerCache = true;
         } else if (!std::strcmp(a, "--v0E")) {

@@ -42,6 +42,10 @@ struct Options {
     PreprocessDataType preprocessDataType = PreprocessDataType::Dense;
     std::string iterLogFile;
     bool iterLog = false;
+    std::string colLogFile;                // src/options.hpp:57-58
+    bool colLog = false;
+    unsigned fixedEffectNumber = 0;        // src/options.hpp:44: fixed effects are not on this path
+    std::string failureFile;               // src/options.hpp:40: BayesW only
     bool useMarkerCache = false;
     unsigned numThread = 0;
     double v0E = 0.0001, s02E = 0.0001, v0G = 0.0001, s02G = 0.0001;

@@ -86,3 +86,17 @@ def test_option_file(brr, tmp_path):
     assert r.returncode == 0, r.stderr
     o = json.loads(r.stdout.strip().splitlines()[-1])
     assert (o["chain"], o["thin"], o["S"]) == (7, 2, [[0.5, 0.05]])
+
+
+def test_logs_fixed_effects_and_failure_options(brr):
+    """--colLog, --fixedEffectNumber and --failure are parsed as the reference
+    does (src/options.cpp:167-174, :230-233)."""
+    o = opts(brr, "--colLog", "cols.csv", "--fixedEffectNumber", "0", "--failure", "fail.txt")
+    assert (o["colLog"], o["fixed"], o["failure"]) == ("cols.csv", 0, "fail.txt")
+    assert (opts(brr)["colLog"], opts(brr)["fixed"]) == ("", 0)
+
+
+def test_fixed_effects_are_refused_before_any_work(brr):
+    r = subprocess.run([brr, "--analysis-type", "ppbayes", "--fixedEffectNumber", "2", "--bfile", "missing"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "fixed effects are not supported" in r.stderr

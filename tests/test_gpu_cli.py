@@ -196,3 +196,24 @@ def test_ppbayes_eigen_marker_with_mean_one(brr, dataset):
         v = np.array([float(t) for t in line.split(", ")])
         np.testing.assert_allclose(v[2:2 + M], s["beta"], rtol=1e-5, atol=1e-9)
         np.testing.assert_array_equal(v[5 + M:5 + 2 * M], s["comp"])
+
+
+def test_ppbayes_column_log(brr, dataset):
+    """--colLog runs the phase-counting sweep variant and writes one row of its
+    16 counters per iteration (the GPU counterpart of the reference's
+    per-column timing log, src/BayesRBase.cpp:381-389); the chain, and so the
+    sample file, is the same as without the log."""
+    d = dataset
+    chain = 4
+    common = ["--analysis-type", "ppbayes", "--bfile", str(d["prefix"]), "--pheno", str(d["dir"] / "toy.phen"),
+              "--chain-length", str(chain), "--burn-in", "0", "--thin", "1", "--seed", "3"]
+    logged, plain, cols = d["dir"] / "logged.csv", d["dir"] / "plain.csv", d["dir"] / "cols.csv"
+    run(brr, *common, "--mcmc-samples", str(logged), "--colLog", str(cols))
+    run(brr, *common, "--mcmc-samples", str(plain))
+    assert logged.read_text() == plain.read_text()
+    rows = cols.read_text().splitlines()
+    assert rows[0].split(",") == ["iter"] + [f"phase{k}" for k in range(16)]
+    v = np.array([[int(t) for t in r.split(",")] for r in rows[1:]])
+    assert v.shape == (chain, 17)
+    np.testing.assert_array_equal(v[:, 0], np.arange(chain))
+    assert (v[:, 1 + 5] > 0).all() and (v[:, 1 + 3] > 0).all()   # grid rounds, sampling cycles
