@@ -2,7 +2,7 @@
 
 Cases of test/optionstest.cpp:5-184 (variance components from the command
 line and from a file, input type from the extension, analysis type), plus the
-additions of this build: --bfile and per-group mixture sizes.
+additions of this CLI: --bfile and per-group mixture sizes.
 """
 import json
 import subprocess
