@@ -1,0 +1,155 @@
+"""A second restatement of the reference sampler, in numpy, against the oracle.
+
+The oracle (oracle/oracle.c) is the checker of every GPU kernel, so it is
+itself checked here against an independent restatement written from the
+reference sources: one sweep of BayesRBase::processColumn
+(src/BayesRBase.cpp:287-392) over dense markers (DenseRKernel,
+src/densebayesrkernel.cpp:10-20, on the columns of the DenseMarkerBuilder
+standardisation) and over ragged markers (SparseBayesRKernel and
+RaggedBayesRKernel, src/sparsebayesrkernel.cpp:10-34,
+src/raggedbayesrkernel.cpp:10-35, statistics of src/sparsemarker.cpp:8-19 and
+src/raggedsparsemarkerbuilder.cpp:45-55, running epsilon sum of
+src/SparseBayesRRG.cpp:76-92), replayed marker by marker in the oracle's sweep
+order with its draws u, z and its state before the sweep.  Checked:
+P(component 0) of every marker, every component and beta, the residual and
+the epsilon sum after the sweep, and the sweep statistics v (component counts
+per group) and betasqnG.  Only the order of floating-point sums differs
+between the two, so components must agree exactly and values to 1e-10.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from bayesrrcmd_gb300 import plink
+
+S2 = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
+
+
+def process_column(num, beta_old, u, z, sigmaE, sigmaG, pi, S, N):
+    """The per-marker sampler of src/BayesRBase.cpp:306-364 for a given num:
+    returns P(component 0), the component (None when the walk ends without
+    one, which leaves beta unchanged) and the new beta."""
+    K = len(S) + 1
+    cva = np.asarray(S, np.float64)
+    denom = (N - 1.0) + (sigmaE / sigmaG) * (1.0 / cva)
+    muk = np.concatenate([[0.0], num / denom])
+    scale = sigmaG / sigmaE * (N - 1.0)
+    logL = np.log(np.asarray(pi[:K], np.float64))
+    logL[1:] = logL[1:] - 0.5 * np.log(scale * cva + 1.0) + 0.5 * (muk[1:] * num) / sigmaE
+
+    def prob(k):
+        if np.any(np.abs(logL[1:] - logL[k]) > 700):
+            return 0.0
+        return 1.0 / np.exp(logL - logL[k]).sum()
+
+    acum = prob(0)
+    a0 = acum
+    for k in range(K):
+        if u <= acum:
+            beta = 0.0 if k == 0 else z * np.sqrt(sigmaE / denom[k - 1]) + muk[k]
+            return a0, k, beta
+        if k + 1 < K:
+            acum += prob(k + 1)
+    return a0, None, beta_old
+
+
+def ragged_statistics(g):
+    """mean over all N (missing included), sd, Zsum of the ragged marker."""
+    N = g.shape[1]
+    val = np.where(g > 0, g, 0).astype(np.float64)
+    zsum = val.sum(1)
+    sqrdz = (val * val).sum(1)
+    mean = zsum / N
+    sd = np.sqrt((sqrdz - 2.0 * mean * zsum + N * mean * mean) / (N - 1.0))
+    return mean, sd, zsum
+
+
+def sweep_once(kind, N, M, miss, seed, strong=False):
+    g, _ = plink.synth_genotypes(N, M, seed=seed, missing=miss)
+    bed = plink.encode_bed(g)
+    if strong:
+        # one marker carries almost all of the variance: sigmaE becomes small,
+        # its num large, and the 700 guards of the log-likelihoods fire
+        x0 = plink.standardize_dense(g[:1])[0]
+        y = (3.0 * x0 + np.random.default_rng(seed).normal(0.0, 0.05, N)).astype(np.float32)
+    else:
+        y, _, _ = plink.synth_phenotype(g, seed, max(2, M // 8), 0.6)
+    group = (np.arange(M) % 2).astype(np.int32)
+    oc = O.OracleChain(bed, N, y, S2, kind=kind, group=group, seed=seed)
+    # the strong marker's guards fire while sigmaE is small, in the first iterations
+    for it in range(1 if strong else 3):
+        oc.iterate(it)
+    s0 = oc.state()
+    order = O.permutation(seed, 0, 77, M)
+    u, z = O.marker_draws(seed, 0, 77, M)
+    oc.sweep(order, u, z)
+    return g, group, s0, order, u, z, oc.state()
+
+
+def replay(kind, g, group, s0, order, u, z):
+    M, N = g.shape
+    beta, comp, acum = s0["beta"].copy(), s0["comp"].copy(), s0["acum"].copy()
+    eps, eps_sum = s0["eps"].copy(), s0["epsSum"]
+    v = np.zeros((len(S2), 4))
+    bsq = np.zeros(len(S2))
+    if kind == 0:
+        x = plink.standardize_dense(g)
+    else:
+        mean, sd, zsum = ragged_statistics(g)
+        ones, twos, missing = g == 1, g == 2, g < 0
+    for j in order:
+        gr = group[j]
+        b_old = beta[j]
+        if kind == 0:
+            num = x[j] @ eps + b_old * (N - 1.0)
+        else:
+            num = b_old * (N - 1.0) - mean[j] * eps_sum / sd[j] + (eps[ones[j]].sum() + 2.0 * eps[twos[j]].sum()) / sd[j]
+        a0, k, b_new = process_column(num, b_old, u[j], z[j], s0["sigmaE"], s0["sigmaG"][gr], s0["pi"][gr], S2[gr], N)
+        acum[j] = a0
+        if k is not None:
+            beta[j] = b_new
+            comp[j] = k
+            v[gr, k] += 1.0
+            if k > 0:
+                bsq[gr] += b_new * b_new
+        if b_old == 0.0 and beta[j] == 0.0:
+            continue
+        d = b_old - beta[j]
+        if kind == 0:
+            eps += d * x[j]
+        else:
+            eps_sum += d * zsum[j] / sd[j] - d * mean[j] * N / sd[j]
+            adj = d * mean[j] / sd[j]
+            delta = np.full(N, -adj)
+            delta[ones[j]] += d / sd[j]
+            delta[twos[j]] += 2.0 * d / sd[j]
+            delta[missing[j]] += adj
+            eps += delta
+    return dict(beta=beta, comp=comp, acum=acum, eps=eps, epsSum=eps_sum, v=v, betasqnG=bsq)
+
+
+@pytest.mark.parametrize("kind,N,M,miss,seed,strong", [
+    (0, 640, 160, 0.0, 21, False),
+    (0, 333, 120, 0.02, 22, False),
+    (1, 640, 160, 0.0, 23, False),
+    (1, 501, 140, 0.03, 24, False),
+    (0, 640, 60, 0.0, 25, True),
+    (1, 640, 60, 0.02, 26, True),
+])
+def test_oracle_sweep_equals_numpy_restatement(kind, N, M, miss, seed, strong):
+    g, group, s0, order, u, z, s1 = sweep_once(kind, N, M, miss, seed, strong)
+    r = replay(kind, g, group, s0, order, u, z)
+    np.testing.assert_array_equal(s1["comp"], r["comp"])
+    np.testing.assert_array_equal(s1["beta"] != 0, r["beta"] != 0)
+    np.testing.assert_allclose(s1["beta"], r["beta"], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(s1["acum"], r["acum"], rtol=1e-10, atol=1e-15)
+    np.testing.assert_allclose(s1["eps"], r["eps"], rtol=0, atol=1e-10)
+    np.testing.assert_array_equal(s1["v"][:, :4], r["v"])
+    np.testing.assert_allclose(s1["betasqnG"], r["betasqnG"], rtol=1e-10)
+    if kind == 1:
+        np.testing.assert_allclose(s1["epsSum"], r["epsSum"], rtol=0, atol=1e-9)
+    # the sweep moved the chain: some markers changed component
+    assert np.count_nonzero(s1["comp"] != s0["comp"]) > 0
+    if strong:
+        # the guards fired: P(component 0) is exactly zero for the strong marker
+        assert s1["acum"][0] == 0.0
