@@ -13,7 +13,9 @@ src/SparseBayesRRG.cpp:76-92), replayed marker by marker in the oracle's sweep
 order with its draws u, z and its state before the sweep.  Checked:
 P(component 0) of every marker, every component and beta, the residual and
 the epsilon sum after the sweep, and the sweep statistics v (component counts
-per group) and betasqnG.  Only the order of floating-point sums differs
+per group) and betasqnG.  A second test replays whole iterations of the
+runGibbs loop body (updateMu, the sweep, the sigmaE, sigmaG and pi draws) from
+the same stream variates.  Only the order of floating-point sums differs
 between the two, so components must agree exactly and values to 1e-10.
 """
 import numpy as np
@@ -86,12 +88,12 @@ def sweep_once(kind, N, M, miss, seed, strong=False):
     return g, group, s0, order, u, z, oc.state()
 
 
-def replay(kind, g, group, s0, order, u, z):
+def replay(kind, g, group, s0, order, u, z, S=S2):
     M, N = g.shape
     beta, comp, acum = s0["beta"].copy(), s0["comp"].copy(), s0["acum"].copy()
     eps, eps_sum = s0["eps"].copy(), s0["epsSum"]
-    v = np.zeros((len(S2), 4))
-    bsq = np.zeros(len(S2))
+    v = np.zeros((len(S), 4))
+    bsq = np.zeros(len(S))
     if kind == 0:
         x = plink.standardize_dense(g)
     else:
@@ -104,7 +106,7 @@ def replay(kind, g, group, s0, order, u, z):
             num = x[j] @ eps + b_old * (N - 1.0)
         else:
             num = b_old * (N - 1.0) - mean[j] * eps_sum / sd[j] + (eps[ones[j]].sum() + 2.0 * eps[twos[j]].sum()) / sd[j]
-        a0, k, b_new = process_column(num, b_old, u[j], z[j], s0["sigmaE"], s0["sigmaG"][gr], s0["pi"][gr], S2[gr], N)
+        a0, k, b_new = process_column(num, b_old, u[j], z[j], s0["sigmaE"], s0["sigmaG"][gr], s0["pi"][gr], S[gr], N)
         acum[j] = a0
         if k is not None:
             beta[j] = b_new
@@ -153,3 +155,87 @@ def test_oracle_sweep_equals_numpy_restatement(kind, N, M, miss, seed, strong):
     if strong:
         # the guards fired: P(component 0) is exactly zero for the strong marker
         assert s1["acum"][0] == 0.0
+
+
+# Two groups with the same number of components, as the reference's K x groups
+# matrices of mixture variances and counts require (src/BayesRBase.cpp:200).
+S_EQ = [[0.01, 0.001, 0.0001], [0.1, 0.01, 0.001]]
+PRIOR = 1e-4   # v0E = s02E = v0G = s02G, the reference's defaults (src/options.hpp:86-89)
+P_MU, P_SIGMAE, P_SIGMAG, P_PI = 2, 5, 6, 7   # stream purposes of the scalar draws
+
+
+def u53(a, b):
+    return ((a >> 5) * 67108864.0 + (b >> 6) + 0.5) / 9007199254740992.0
+
+
+def std_gamma(seed, chain, it, purpose, sub, shape):
+    rc, x = O.gamma(seed, chain, it, purpose, sub, shape)
+    assert rc == 0
+    return x
+
+
+def inv_scaled_chisq(seed, chain, it, purpose, sub, dof, scale):
+    """src/distributions_boost.cpp:45-60: 1 / Gamma(dof/2, scale 1/(dof*scale/2))."""
+    return 1.0 / (std_gamma(seed, chain, it, purpose, sub, 0.5 * dof) / (0.5 * dof * scale))
+
+
+def iterate_numpy(kind, g, group, s, seed, chain, it):
+    """One pass of the runGibbs loop body (src/BayesRBase.cpp:186-247):
+    updateMu (dense src/DenseBayesRRmz.cpp:36-42, sparse
+    src/SparseBayesRRG.cpp:106-113), the sweep, sigmaE, then per group sigmaG
+    and the Dirichlet draw of pi."""
+    M, N = g.shape
+    eps = s["eps"] + s["mu"]
+    eps_sum = s["epsSum"]
+    if kind == 0:
+        mean = eps.sum() / N
+    else:
+        eps_sum = eps_sum + s["mu"] * N
+        mean = eps_sum / N
+    b = O.philox([0, it, P_MU, 0], [seed, chain])
+    zmu = np.sqrt(-2.0 * np.log(u53(b[0], b[1]))) * np.cos(2.0 * np.pi * u53(b[2], b[3]))
+    mu = mean + np.sqrt(s["sigmaE"] / N) * zmu
+    eps = eps - mu
+    if kind != 0:
+        eps_sum -= mu * N
+    order = O.permutation(seed, chain, it, M)
+    u, z = O.marker_draws(seed, chain, it, M)
+    r = replay(kind, g, group, dict(s, eps=eps, epsSum=eps_sum, mu=mu), order, u, z, S_EQ)
+    dof = PRIOR + N
+    sigmaE = inv_scaled_chisq(seed, chain, it, P_SIGMAE, 0, dof, ((r["eps"] ** 2).sum() + PRIOR * PRIOR) / dof)
+    sigmaG = np.zeros(len(S_EQ))
+    pi = np.zeros((len(S_EQ), 4))
+    for gr in range(len(S_EQ)):
+        v = r["v"][gr]
+        m0 = v.sum() - v[0]
+        sigmaG[gr] = inv_scaled_chisq(seed, chain, it, P_SIGMAG, gr, PRIOR + m0,
+                                      (r["betasqnG"][gr] * m0 + PRIOR * PRIOR) / (PRIOR + m0))
+        d = np.array([std_gamma(seed, chain, it, P_PI, gr * 256 + k, v[k] + 1.0) for k in range(4)])
+        pi[gr] = d / d.sum()
+    return dict(r, mu=mu, sigmaE=sigmaE, sigmaG=sigmaG, pi=pi)
+
+
+@pytest.mark.parametrize("kind,miss,seed", [(0, 0.0, 31), (0, 0.02, 32), (1, 0.0, 33), (1, 0.03, 34)])
+def test_oracle_iteration_equals_numpy_restatement(kind, miss, seed):
+    N, M = 480, 140
+    g, _ = plink.synth_genotypes(N, M, seed=seed, missing=miss)
+    bed = plink.encode_bed(g)
+    y, _, _ = plink.synth_phenotype(g, seed, 12, 0.5)
+    group = (np.arange(M) % 2).astype(np.int32)
+    oc = O.OracleChain(bed, N, y, S_EQ, kind=kind, group=group, seed=seed, chain=3)
+    for it in range(2):
+        oc.iterate(it)
+    for it in range(2, 5):
+        s = oc.state()
+        r = iterate_numpy(kind, g, group, s, seed, 3, it)
+        oc.iterate(it)
+        o = oc.state()
+        np.testing.assert_array_equal(o["comp"], r["comp"], err_msg=f"iteration {it}")
+        np.testing.assert_allclose(o["beta"], r["beta"], rtol=1e-10, atol=1e-14)
+        np.testing.assert_allclose(o["eps"], r["eps"], rtol=0, atol=1e-10)
+        np.testing.assert_allclose(o["mu"], r["mu"], rtol=1e-10, atol=1e-13)
+        np.testing.assert_allclose(o["sigmaE"], r["sigmaE"], rtol=1e-10)
+        np.testing.assert_allclose(o["sigmaG"], r["sigmaG"], rtol=1e-10)
+        np.testing.assert_allclose(o["pi"][:, :4], r["pi"], rtol=1e-10)
+        if kind == 1:
+            np.testing.assert_allclose(o["epsSum"], r["epsSum"], rtol=0, atol=1e-9)
