@@ -9,7 +9,8 @@ standardisation) and over ragged markers (SparseBayesRKernel and
 RaggedBayesRKernel, src/sparsebayesrkernel.cpp:10-34,
 src/raggedbayesrkernel.cpp:10-35, statistics of src/sparsemarker.cpp:8-19 and
 src/raggedsparsemarkerbuilder.cpp:45-55, running epsilon sum of
-src/SparseBayesRRG.cpp:76-92), replayed marker by marker in the oracle's sweep
+src/SparseBayesRRG.cpp:76-92) and over Eigen sparse markers
+(src/eigenbayesrkernel.cpp:10-20, src/eigensparsemarkerbuilder.cpp:40-56), replayed marker by marker in the oracle's sweep
 order with its draws u, z and its state before the sweep.  Checked:
 P(component 0) of every marker, every component and beta, the residual and
 the epsilon sum after the sweep, and the sweep statistics v (component counts
@@ -66,6 +67,20 @@ def ragged_statistics(g):
     return mean, sd, zsum
 
 
+def eigen_statistics(g):
+    """The Eigen sparse marker (src/eigensparsemarkerbuilder.cpp:40-56): Zg with
+    missing genotypes imputed at mean = (sum over non-missing) / N; sqrdZ,
+    Zsum and sd include the imputed values."""
+    N = g.shape[1]
+    val = np.where(g > 0, g, 0).astype(np.float64)
+    mean = val.sum(1) / N
+    zg = np.where(g < 0, mean[:, None], val)
+    zsum = zg.sum(1)
+    sqrdz = (zg * zg).sum(1)
+    sd = np.sqrt((sqrdz - 2.0 * mean * zsum + N * mean * mean) / (N - 1.0))
+    return zg, mean, sd, zsum
+
+
 def sweep_once(kind, N, M, miss, seed, strong=False):
     g, _ = plink.synth_genotypes(N, M, seed=seed, missing=miss)
     bed = plink.encode_bed(g)
@@ -96,16 +111,20 @@ def replay(kind, g, group, s0, order, u, z, S=S2):
     bsq = np.zeros(len(S))
     if kind == 0:
         x = plink.standardize_dense(g)
-    else:
+    elif kind == 1:
         mean, sd, zsum = ragged_statistics(g)
         ones, twos, missing = g == 1, g == 2, g < 0
+    else:
+        zg, mean, sd, zsum = eigen_statistics(g)
     for j in order:
         gr = group[j]
         b_old = beta[j]
         if kind == 0:
             num = x[j] @ eps + b_old * (N - 1.0)
-        else:
+        elif kind == 1:
             num = b_old * (N - 1.0) - mean[j] * eps_sum / sd[j] + (eps[ones[j]].sum() + 2.0 * eps[twos[j]].sum()) / sd[j]
+        else:
+            num = b_old * (N - 1.0) - mean[j] * eps_sum / sd[j] + zg[j] @ eps / sd[j]
         a0, k, b_new = process_column(num, b_old, u[j], z[j], s0["sigmaE"], s0["sigmaG"][gr], s0["pi"][gr], S[gr], N)
         acum[j] = a0
         if k is not None:
@@ -119,6 +138,9 @@ def replay(kind, g, group, s0, order, u, z, S=S2):
         d = b_old - beta[j]
         if kind == 0:
             eps += d * x[j]
+        elif kind == 2:
+            eps_sum += d * zsum[j] / sd[j] - d * mean[j] * N / sd[j]
+            eps += d * zg[j] / sd[j] - d * mean[j] / sd[j]
         else:
             eps_sum += d * zsum[j] / sd[j] - d * mean[j] * N / sd[j]
             adj = d * mean[j] / sd[j]
@@ -137,6 +159,8 @@ def replay(kind, g, group, s0, order, u, z, S=S2):
     (1, 501, 140, 0.03, 24, False),
     (0, 640, 60, 0.0, 25, True),
     (1, 640, 60, 0.02, 26, True),
+    (2, 501, 140, 0.03, 27, False),
+    (2, 640, 60, 0.02, 28, True),
 ])
 def test_oracle_sweep_equals_numpy_restatement(kind, N, M, miss, seed, strong):
     g, group, s0, order, u, z, s1 = sweep_once(kind, N, M, miss, seed, strong)
@@ -148,7 +172,7 @@ def test_oracle_sweep_equals_numpy_restatement(kind, N, M, miss, seed, strong):
     np.testing.assert_allclose(s1["eps"], r["eps"], rtol=0, atol=1e-10)
     np.testing.assert_array_equal(s1["v"][:, :4], r["v"])
     np.testing.assert_allclose(s1["betasqnG"], r["betasqnG"], rtol=1e-10)
-    if kind == 1:
+    if kind != 0:
         np.testing.assert_allclose(s1["epsSum"], r["epsSum"], rtol=0, atol=1e-9)
     # the sweep moved the chain: some markers changed component
     assert np.count_nonzero(s1["comp"] != s0["comp"]) > 0
@@ -215,7 +239,7 @@ def iterate_numpy(kind, g, group, s, seed, chain, it):
     return dict(r, mu=mu, sigmaE=sigmaE, sigmaG=sigmaG, pi=pi)
 
 
-@pytest.mark.parametrize("kind,miss,seed", [(0, 0.0, 31), (0, 0.02, 32), (1, 0.0, 33), (1, 0.03, 34)])
+@pytest.mark.parametrize("kind,miss,seed", [(0, 0.0, 31), (0, 0.02, 32), (1, 0.0, 33), (1, 0.03, 34), (2, 0.03, 35)])
 def test_oracle_iteration_equals_numpy_restatement(kind, miss, seed):
     N, M = 480, 140
     g, _ = plink.synth_genotypes(N, M, seed=seed, missing=miss)
@@ -237,5 +261,5 @@ def test_oracle_iteration_equals_numpy_restatement(kind, miss, seed):
         np.testing.assert_allclose(o["sigmaE"], r["sigmaE"], rtol=1e-10)
         np.testing.assert_allclose(o["sigmaG"], r["sigmaG"], rtol=1e-10)
         np.testing.assert_allclose(o["pi"][:, :4], r["pi"], rtol=1e-10)
-        if kind == 1:
+        if kind != 0:
             np.testing.assert_allclose(o["epsSum"], r["epsSum"], rtol=0, atol=1e-9)
