@@ -397,10 +397,12 @@ def cpu_reference(steps_ref, bed, y, group, warmup_ref=0):
     """FP64 restatement of the reference sampler on the host, on a sample of
     the markers of the workload (a sweep costs O(N) per marker, so the
     per-marker cost of the sample is that of the full M), one core: the
-    reference's sampling node is serial.  warmup_ref untimed iterations come
-    first."""
+    reference's sampling node is serial.  The restatement is the build with
+    the reference's fast release flags (-O3 -ffast-math -funroll-loops).
+    warmup_ref untimed iterations come first."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as O
+    O.use_timing_build()
     m_sample = bed.shape[0]
     oc = O.OracleChain(np.ascontiguousarray(bed), N_IND, y, S_GROUPS, kind=0, group=group, seed=SEED)
     for it in range(warmup_ref):
@@ -451,7 +453,8 @@ def main():
                 "config": {"workload": WORKLOAD, "sample_markers": m_sample},
                 "cpu_baseline": {"value": rate, "unit": "marker-updates/s", "cores": 1, "kind": "port",
                                  "sample": f"{m_sample} markers x N={N_IND}, {steps} Gibbs iterations of the FP64 "
-                                           f"restatement of the reference sampler ({dt:.1f} s); the reference "
+                                           f"restatement of the reference sampler built with the reference's fast "
+                                           f"flags -O3 -ffast-math -funroll-loops ({dt:.1f} s); the reference "
                                            f"itself needs Eigen/Boost.Random/TBB, absent here"},
                 "e2e": {"value": rate, "unit": "marker-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -555,7 +558,8 @@ def main():
         rate, m_sample, dt = cpu_reference(it_sample, bed_s, y, group[:m_sample])
         cpu = {"value": rate, "unit": "marker-updates/s", "cores": 1, "kind": "port",
                "sample": f"first {m_sample} markers x N={N_IND} of the same data, {it_sample} Gibbs iterations of "
-                         f"the FP64 restatement of the reference sampler ({dt:.1f} s)"}
+                         f"the FP64 restatement of the reference sampler built with the reference's fast flags "
+                         f"-O3 -ffast-math -funroll-loops ({dt:.1f} s)"}
     hbm, peak_kind = peaks()
     sweep_s = fp32c["sweep_ms"] / 1e3 / args.steps
     bytes_per_sweep = M_SNP * (N_IND / 4.0)      # 2-bit genotype bytes per marker-update x M

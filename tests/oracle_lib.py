@@ -10,7 +10,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
 
-from oracle.build import build_oracle  # noqa: E402
+from oracle.build import build_oracle, build_oracle_timing  # noqa: E402
 
 OR_MAX_GROUPS = 64
 OR_MAX_K = 16
@@ -36,12 +36,22 @@ class OrState(C.Structure):
 
 
 _lib = None
+_timing = False
+
+
+def use_timing_build():
+    """Load the oracle built with the reference's fast release flags from now
+    on in this process: for the timed CPU baseline only, never as the checker."""
+    global _lib, _timing
+    if not _timing:
+        _timing = True
+        _lib = None
 
 
 def lib():
     global _lib
     if _lib is None:
-        L = C.CDLL(str(build_oracle()))
+        L = C.CDLL(str(build_oracle_timing() if _timing else build_oracle()))
         u8, i8, i32, i64, f64, u32 = (C.POINTER(C.c_uint8), C.POINTER(C.c_int8), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_uint32))
         L.or_philox4x32_10.argtypes = [u32, u32, u32]
