@@ -72,6 +72,17 @@ BINDIR = PKG / "bin"
 CLI = BINDIR / "brr"
 
 
+def zlib_flags(cxx: str) -> list:
+    """-DBRR_WITH_ZLIB -lz when a program using zlib compiles and links here,
+    else nothing: `brr` then reads only uncompressed preprocessed files and
+    says so when it meets a compressed record."""
+    BUILD.mkdir(exist_ok=True)
+    probe = BUILD / "zlib_probe.cpp"
+    probe.write_text("#include <zlib.h>\nint main() { return zlibVersion() == nullptr; }\n")
+    r = subprocess.run([cxx, str(probe), "-o", str(BUILD / "zlib_probe"), "-lz"], capture_output=True, text=True)
+    return ["-DBRR_WITH_ZLIB", "-lz"] if r.returncode == 0 else []
+
+
 def build_cli(verbose: bool = False) -> Path:
     """Compile the `brr` command-line host (C++17) against libbrr_gpu.so."""
     lib = build_gpu(verbose)
@@ -82,8 +93,9 @@ def build_cli(verbose: bool = False) -> Path:
         cxx = shutil.which("g++") or shutil.which("c++")
         if not cxx:
             raise RuntimeError("no C++ compiler for the brr host")
-        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", "-o", str(CLI), *map(str, srcs),
-               f"-L{LIBDIR}", "-lbrr_gpu", "-Wl,-rpath,$ORIGIN/../lib"]
+        z = zlib_flags(cxx)
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", *z[:1], "-o", str(CLI), *map(str, srcs),
+               f"-L{LIBDIR}", "-lbrr_gpu", *z[1:], "-Wl,-rpath,$ORIGIN/../lib"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -9,6 +9,10 @@
 #include <sstream>
 #include <unordered_set>
 
+#if defined(BRR_WITH_ZLIB)
+#include <zlib.h>
+#endif
+
 namespace brr {
 
 void Data::readFamFile(const std::string &famFile)
@@ -237,12 +241,67 @@ std::ifstream openPreprocessed(const std::string &ppFile)
     return in;
 }
 
-void checkUncompressed(const IndexEntry &e, int64_t j)
+// Inflates a zlib stream (the format deflateInit writes) into exactly
+// plain.size() bytes; false when the bytes are not such a stream or this build
+// has no zlib.
+bool inflateRecord(const std::vector<char> &packed, std::vector<char> &plain)
 {
-    if (e.compressedSize != e.originalSize)
-        throw std::string("Error: marker " + std::to_string(j) +
-                          " of the preprocessed file is compressed; write it without --compress");
+#if defined(BRR_WITH_ZLIB)
+    uLongf got = (uLongf)plain.size();
+    const int rc = uncompress(reinterpret_cast<Bytef *>(plain.data()), &got,
+                              reinterpret_cast<const Bytef *>(packed.data()), (uLong)packed.size());
+    return rc == Z_OK && got == (uLongf)plain.size();
+#else
+    (void)packed;
+    (void)plain;
+    return false;
+#endif
 }
+
+// Positions a stream at a marker's record: the file itself for uncompressed
+// files, or an in-memory copy of the inflated record for compressed ones
+// (Marker::decompress then read, src/marker.cpp:36-55).
+class RecordReader {
+public:
+    RecordReader(const std::string &ppFile, bool compressed) : file_(openPreprocessed(ppFile)), compressed_(compressed) {}
+
+    std::istream &open(const IndexEntry &e, int64_t j)
+    {
+        const std::string which = " of marker " + std::to_string(j);
+        if (!compressed_) {
+            if (e.compressedSize != e.originalSize)
+                throw std::string("Error: the record" + which +
+                                  " of the preprocessed file is compressed; read it with --compress");
+            file_.clear();
+            file_.seekg((std::streamoff)e.pos);
+            return file_;
+        }
+        packed_.resize((size_t)e.compressedSize);
+        file_.clear();
+        file_.seekg((std::streamoff)e.pos);
+        file_.read(packed_.data(), (std::streamsize)packed_.size());
+        if (!file_)
+            throw std::string("Error: the preprocessed bed file ends before the record" + which);
+        plain_.resize((size_t)e.originalSize);
+        if (!inflateRecord(packed_, plain_)) {
+            if (e.compressedSize != e.originalSize)
+                throw std::string(canReadCompressed()
+                                      ? "Error: the compressed record" + which + " does not inflate to its size"
+                                      : "Error: the record" + which +
+                                            " is compressed and this build of brr has no zlib to read it");
+            plain_ = packed_;   // stored without compression
+        }
+        mem_.str(std::string(plain_.data(), plain_.size()));
+        mem_.clear();
+        return mem_;
+    }
+
+private:
+    std::ifstream file_;
+    bool compressed_;
+    std::vector<char> packed_, plain_;
+    std::istringstream mem_;
+};
 
 // Standardised value per 2-bit code (0: genotype 2, 1: missing, 2: genotype 1,
 // 3: genotype 0) of a dense column with the given class counts: missing values
@@ -271,17 +330,16 @@ bool standardisedValues(int64_t N, const int64_t n[4], double v[4])
 }  // namespace
 
 std::vector<uint8_t> readRaggedPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
-                                                 int64_t M)
+                                                 int64_t M, bool compressed)
 {
     const std::vector<IndexEntry> index = readIndex(indexFile, M);
-    std::ifstream in = openPreprocessed(ppFile);
+    RecordReader records(ppFile, compressed);
     std::vector<uint8_t> bed = allHomozygousMajor(N, M);
     const int64_t cb = (N + 3) / 4;
     const unsigned listCode[3] = {2u, 0u, 1u};   // Zones: genotype 1, Ztwos: genotype 2, Zmissing
     std::vector<int32_t> ids;
     for (int64_t j = 0; j < M; ++j) {
-        checkUncompressed(index[(size_t)j], j);
-        in.seekg((std::streamoff)index[(size_t)j].pos);
+        std::istream &in = records.open(index[(size_t)j], j);
         double stats[4];
         in.read(reinterpret_cast<char *>(stats), sizeof stats);
         uint64_t used = sizeof stats;
@@ -309,10 +367,10 @@ std::vector<uint8_t> readRaggedPreprocessedAsBed(const std::string &ppFile, cons
 }
 
 std::vector<uint8_t> readEigenPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
-                                                int64_t M)
+                                                int64_t M, bool compressed)
 {
     const std::vector<IndexEntry> index = readIndex(indexFile, M);
-    std::ifstream in = openPreprocessed(ppFile);
+    RecordReader records(ppFile, compressed);
     std::vector<uint8_t> bed = allHomozygousMajor(N, M);
     const int64_t cb = (N + 3) / 4;
     std::vector<double> values;
@@ -320,8 +378,7 @@ std::vector<uint8_t> readEigenPreprocessedAsBed(const std::string &ppFile, const
     std::vector<int64_t> ones;
     for (int64_t j = 0; j < M; ++j) {
         const std::string which = " of marker " + std::to_string(j);
-        checkUncompressed(index[(size_t)j], j);
-        in.seekg((std::streamoff)index[(size_t)j].pos);
+        std::istream &in = records.open(index[(size_t)j], j);
         double stats[4];
         int64_t count = -1;
         in.read(reinterpret_cast<char *>(stats), sizeof stats);
@@ -379,18 +436,17 @@ std::vector<uint8_t> readEigenPreprocessedAsBed(const std::string &ppFile, const
 }
 
 std::vector<uint8_t> readDensePreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
-                                                int64_t M)
+                                                int64_t M, bool compressed)
 {
     const std::vector<IndexEntry> index = readIndex(indexFile, M);
-    std::ifstream in = openPreprocessed(ppFile);
+    RecordReader records(ppFile, compressed);
     std::vector<uint8_t> bed((size_t)(M * ((N + 3) / 4)), 0);
     const int64_t cb = (N + 3) / 4;
     std::vector<double> col((size_t)N);
     for (int64_t j = 0; j < M; ++j) {
-        checkUncompressed(index[(size_t)j], j);
         if (index[(size_t)j].originalSize != (uint64_t)N * sizeof(double))
             throw std::string("Error: dense record of marker " + std::to_string(j) + " is not N doubles");
-        in.seekg((std::streamoff)index[(size_t)j].pos);
+        std::istream &in = records.open(index[(size_t)j], j);
         in.read(reinterpret_cast<char *>(col.data()), (std::streamsize)(N * sizeof(double)));
         if (!in)
             throw std::string("Error: the preprocessed bed file ends before marker " + std::to_string(j));
@@ -440,6 +496,15 @@ std::vector<uint8_t> readDensePreprocessedAsBed(const std::string &ppFile, const
             setCode(bed, cb, j, i, (unsigned)best[cls[(size_t)i]]);
     }
     return bed;
+}
+
+bool canReadCompressed()
+{
+#if defined(BRR_WITH_ZLIB)
+    return true;
+#else
+    return false;
+#endif
 }
 
 void writeBedFile(const std::string &bedFile, const std::vector<uint8_t> &payload)

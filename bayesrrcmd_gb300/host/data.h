@@ -55,16 +55,25 @@ std::vector<IndexEntry> readIndex(const std::string &indexFile, int64_t M);
 // a dense record is the standardised column, whose at most four distinct values
 // are matched to genotype classes by recomputing the dense builder's values
 // (src/densemarkerbuilder.cpp:44-59) from the class counts each assignment
-// implies.  Throws std::string on a malformed or compressed file.
+// implies.  With `compressed` (the reference's --compress, which decides how
+// its LimitSequenceGraph reads records, src/limitsequencegraph.cpp:19-23 and
+// src/analysis.cpp:21-24) every record is a zlib stream of the same bytes
+// (src/marker.cpp:10-34, src/compression.cpp:101-126) and is inflated to its
+// index entry's originalSize; a record that does not inflate but whose two
+// sizes are equal is taken as stored (files written without compression).
+// Without `compressed` a record whose sizes differ is an error.  Throws
+// std::string on a malformed file.
 std::vector<uint8_t> readRaggedPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
-                                                 int64_t M);
+                                                 int64_t M, bool compressed = false);
 std::vector<uint8_t> readDensePreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
-                                                int64_t M);
+                                                int64_t M, bool compressed = false);
 // Eigen sparse records give the codes from the entry values; when a marker's
 // mean is exactly 1 its missing entries (stored as 1.0) are told apart from
 // heterozygotes by count only, which leaves the chain unchanged.
 std::vector<uint8_t> readEigenPreprocessedAsBed(const std::string &ppFile, const std::string &indexFile, int64_t N,
-                                                int64_t M);
+                                                int64_t M, bool compressed = false);
+// Whether this build can inflate compressed records (zlib found when it was built).
+bool canReadCompressed();
 // Writes a PLINK BED file (magic + SNP-major payload).
 void writeBedFile(const std::string &bedFile, const std::vector<uint8_t> &payload);
 

@@ -89,9 +89,9 @@ std::vector<uint8_t> readPreprocessedAsBed(const Options &opt, int64_t N, int64_
     const std::string pp = ppFileForType(opt.preprocessDataType, opt.dataFile);
     const std::string ix = ppIndexFileForType(opt.preprocessDataType, opt.dataFile);
     switch (opt.preprocessDataType) {
-    case PreprocessDataType::Dense: return readDensePreprocessedAsBed(pp, ix, N, M);
-    case PreprocessDataType::SparseEigen: return readEigenPreprocessedAsBed(pp, ix, N, M);
-    case PreprocessDataType::SparseRagged: return readRaggedPreprocessedAsBed(pp, ix, N, M);
+    case PreprocessDataType::Dense: return readDensePreprocessedAsBed(pp, ix, N, M, opt.compress);
+    case PreprocessDataType::SparseEigen: return readEigenPreprocessedAsBed(pp, ix, N, M, opt.compress);
+    case PreprocessDataType::SparseRagged: return readRaggedPreprocessedAsBed(pp, ix, N, M, opt.compress);
     default: throw std::string("Error: unsupported --sparse-data type (dense, eigen or ragged)");
     }
 }
@@ -425,7 +425,9 @@ void printOptions(const Options &o)
               << o.chainLength << ", \"burnin\": " << o.burnin << ", \"thin\": " << o.thin << ", \"seed\": " << o.seed
               << ", \"samples\": \"" << o.mcmcSampleFile << "\", \"sparse\": " << (int)o.preprocessDataType
               << ", \"form\": \"" << o.form << "\", \"colLog\": \"" << (o.colLog ? o.colLogFile : "")
-              << "\", \"fixed\": " << o.fixedEffectNumber << ", \"failure\": \"" << o.failureFile << "\", \"S\": [";
+              << "\", \"fixed\": " << o.fixedEffectNumber << ", \"failure\": \"" << o.failureFile
+              << "\", \"compress\": " << (o.compress ? "true" : "false")
+              << ", \"zlib\": " << (canReadCompressed() ? "true" : "false") << ", \"S\": [";
     for (std::size_t g = 0; g < o.S.size(); ++g) {
         std::cout << (g ? ", " : "") << "[";
         for (std::size_t k = 0; k < o.S[g].size(); ++k)

@@ -12,6 +12,7 @@ payload bit for bit from ragged and Eigen files, and from dense files codes that
 standardise to the same columns (identical codes where all three genotype
 classes occur), including markers where genotype classes are absent.
 """
+import json
 import subprocess
 
 import numpy as np
@@ -224,3 +225,83 @@ def test_eigen_value_that_is_not_a_genotype_is_an_error(brr, tmp_path):
     open(str(prefix) + ".eigen.sparsebed", "wb").write(bytes(raw))
     r = export(brr, prefix, tmp_path / "back.bed", "--sparse-data", "eigen")
     assert r.returncode == 1 and "marker 0" in r.stderr
+
+
+# Compressed files: the reference's --preprocess --compress writes each record
+# as a zlib stream at the default level (deflateInit(-1), src/compression.cpp:5-11,
+# src/marker.cpp:10-34) and the index holds {pos, compressedSize, originalSize};
+# its ppbayes inflates every record when --compress is given
+# (src/limitsequencegraph.cpp:19-23).
+PP_FILES = {None: (".ppbed", ".ppbedindex"), "ragged": (".ragged.sparsebed", ".ragged.sparsebedindex"),
+            "eigen": (".eigen.sparsebed", ".eigen.sparsebedindex")}
+
+
+def needs_zlib(brr):
+    r = subprocess.run([brr, "--print-options"], capture_output=True, text=True)
+    if not json.loads(r.stdout.strip().splitlines()[-1])["zlib"]:
+        pytest.skip("brr was built without zlib")
+
+
+def write_kind(prefix, payload, N, sparse):
+    {None: write_dense, "ragged": write_ragged, "eigen": write_eigen}[sparse](prefix, payload, N)
+
+
+def compress_files(prefix, sparse, M):
+    import zlib
+    pp, ix = (str(prefix) + s for s in PP_FILES[sparse])
+    idx = np.fromfile(ix, np.uint64).reshape(M, 3)
+    raw = open(pp, "rb").read()
+    out, entries, pos = [], [], 0
+    for j in range(M):
+        rec = raw[int(idx[j, 0]):int(idx[j, 0]) + int(idx[j, 2])]
+        z = zlib.compress(rec)
+        out.append(z)
+        entries.append((pos, len(z), len(rec)))
+        pos += len(z)
+    open(pp, "wb").write(b"".join(out))
+    np.array(entries, np.uint64).tofile(ix)
+    return np.array(entries, np.uint64)
+
+
+def sparse_args(sparse):
+    return [] if sparse is None else ["--sparse-data", sparse]
+
+
+@pytest.mark.parametrize("sparse", [None, "ragged", "eigen"])
+def test_compressed_files_are_read_with_compress(brr, tmp_path, sparse):
+    needs_zlib(brr)
+    prefix, payload, N, M = dataset(tmp_path, missing=0.02)
+    write_kind(prefix, payload, N, sparse)
+    r = export(brr, prefix, tmp_path / "plain.bed", *sparse_args(sparse))
+    assert r.returncode == 0, r.stderr
+    entries = compress_files(prefix, sparse, M)
+    assert (entries[:, 1] != entries[:, 2]).all()
+    r = export(brr, prefix, tmp_path / "no_flag.bed", *sparse_args(sparse))
+    assert r.returncode == 1 and "--compress" in r.stderr
+    r = export(brr, prefix, tmp_path / "inflated.bed", "--compress", *sparse_args(sparse))
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(read_payload(tmp_path / "inflated.bed", N, M),
+                                  read_payload(tmp_path / "plain.bed", N, M))
+
+
+def test_uncompressed_files_are_read_as_stored_with_compress(brr, tmp_path):
+    needs_zlib(brr)
+    prefix, payload, N, M = dataset(tmp_path, missing=0.02)
+    write_ragged(prefix, payload, N)
+    r = export(brr, prefix, tmp_path / "back.bed", "--compress", "--sparse-data", "ragged")
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(read_payload(tmp_path / "back.bed", N, M), payload)
+
+
+def test_corrupt_compressed_record_is_an_error(brr, tmp_path):
+    needs_zlib(brr)
+    prefix, payload, N, M = dataset(tmp_path, missing=0.0)
+    write_ragged(prefix, payload, N)
+    entries = compress_files(prefix, "ragged", M)
+    pp = str(prefix) + ".ragged.sparsebed"
+    data = bytearray(open(pp, "rb").read())
+    at = int(entries[3, 0] + entries[3, 1] // 2)
+    data[at] ^= 0x5A
+    open(pp, "wb").write(bytes(data))
+    r = export(brr, prefix, tmp_path / "back.bed", "--compress", "--sparse-data", "ragged")
+    assert r.returncode == 1 and "marker 3" in r.stderr and "inflate" in r.stderr
