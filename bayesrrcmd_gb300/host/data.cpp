@@ -2,6 +2,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <iostream>
@@ -496,6 +497,56 @@ std::vector<uint8_t> readDensePreprocessedAsBed(const std::string &ppFile, const
             setCode(bed, cb, j, i, (unsigned)best[cls[(size_t)i]]);
     }
     return bed;
+}
+
+void compressPreprocessed(const std::string &ppFile, const std::string &indexFile, int64_t M)
+{
+#if defined(BRR_WITH_ZLIB)
+    const std::vector<IndexEntry> index = readIndex(indexFile, M);
+    const std::string tmpFile = ppFile + ".compressing";
+    {
+        std::ifstream in = openPreprocessed(ppFile);
+        std::ofstream out(tmpFile, std::ios::binary | std::ios::trunc);
+        if (!out)
+            throw std::string("Error: Unable to open [" + tmpFile + "] for writing");
+        std::ofstream idx(indexFile + ".compressing", std::ios::binary | std::ios::trunc);
+        if (!idx)
+            throw std::string("Error: Unable to open [" + indexFile + ".compressing] for writing");
+        std::vector<char> plain;
+        std::vector<Bytef> packed;
+        uint64_t pos = 0;
+        for (int64_t j = 0; j < M; ++j) {
+            const IndexEntry &e = index[(size_t)j];
+            if (e.compressedSize != e.originalSize)
+                throw std::string("Error: marker " + std::to_string(j) + " is compressed already");
+            plain.resize((size_t)e.originalSize);
+            in.clear();
+            in.seekg((std::streamoff)e.pos);
+            in.read(plain.data(), (std::streamsize)plain.size());
+            if (!in)
+                throw std::string("Error: the preprocessed bed file ends before marker " + std::to_string(j));
+            uLongf size = compressBound((uLong)plain.size());
+            packed.resize((size_t)size);
+            if (compress2(packed.data(), &size, reinterpret_cast<const Bytef *>(plain.data()), (uLong)plain.size(),
+                          Z_DEFAULT_COMPRESSION) != Z_OK)
+                throw std::string("Error: compressing marker " + std::to_string(j) + " failed");
+            out.write(reinterpret_cast<const char *>(packed.data()), (std::streamsize)size);
+            const IndexEntry ne{pos, (uint64_t)size, e.originalSize};
+            idx.write(reinterpret_cast<const char *>(&ne), sizeof ne);
+            pos += size;
+        }
+        if (!out || !idx)
+            throw std::string("Error: writing the compressed preprocessed files failed");
+    }
+    if (std::rename(tmpFile.c_str(), ppFile.c_str()) != 0 ||
+        std::rename((indexFile + ".compressing").c_str(), indexFile.c_str()) != 0)
+        throw std::string("Error: replacing the preprocessed files with their compressed form failed");
+#else
+    (void)ppFile;
+    (void)indexFile;
+    (void)M;
+    throw std::string("Error: --compress needs zlib, which this build of brr does not have");
+#endif
 }
 
 bool canReadCompressed()

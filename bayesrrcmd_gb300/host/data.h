@@ -74,6 +74,12 @@ std::vector<uint8_t> readEigenPreprocessedAsBed(const std::string &ppFile, const
                                                 int64_t M, bool compressed = false);
 // Whether this build can inflate compressed records (zlib found when it was built).
 bool canReadCompressed();
+// Rewrites an uncompressed preprocessed file and its index in the layout of
+// the reference's --compress (src/preprocessgraph.cpp:63-67, :104-122): each
+// record deflated at the default level into one zlib stream, the index
+// holding {pos, compressedSize, originalSize}.  Throws std::string on error or
+// when this build has no zlib.
+void compressPreprocessed(const std::string &ppFile, const std::string &indexFile, int64_t M);
 // Writes a PLINK BED file (magic + SNP-major payload).
 void writeBedFile(const std::string &bedFile, const std::vector<uint8_t> &payload);
 

@@ -120,8 +120,8 @@ bool preprocess(const Options &opt)
 {
     if (opt.preprocessDataType == PreprocessDataType::None)
         throw std::string("Error: unsupported --sparse-data type (dense, eigen or ragged)");
-    if (opt.compress)
-        std::cout << "Note: --compress is not applied; preprocessed files are written uncompressed" << std::endl;
+    if (opt.compress && !canReadCompressed())
+        throw std::string("Error: --compress needs zlib, which this build of brr does not have");
     const auto t0 = std::chrono::steady_clock::now();
     Data data;
     readMetaData(data, opt);
@@ -160,6 +160,10 @@ bool preprocess(const Options &opt)
         else
             writeRaggedPreprocessed(pp, ix, M, table.data(), offs, idxs);
     }
+    // --compress: every record deflated, as the reference's PreprocessGraph
+    // writes them (src/preprocessgraph.cpp:63-67, :110-122)
+    if (opt.compress)
+        compressPreprocessed(pp, ix, M);
     const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::printf("Finished preprocessing the bed file in %.3f sec.\n\n", s);
     return true;

@@ -305,3 +305,66 @@ def test_corrupt_compressed_record_is_an_error(brr, tmp_path):
     open(pp, "wb").write(bytes(data))
     r = export(brr, prefix, tmp_path / "back.bed", "--compress", "--sparse-data", "ragged")
     assert r.returncode == 1 and "marker 3" in r.stderr and "inflate" in r.stderr
+
+
+COMPRESS_DRIVER = r"""
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include "data.h"
+int main(int argc, char **argv)
+{
+    try {
+        brr::compressPreprocessed(argv[1], argv[2], std::atoll(argv[3]));
+    } catch (const std::string &e) {
+        std::fprintf(stderr, "%s\n", e.c_str());
+        return 1;
+    }
+    return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def compressor(brr, tmp_path_factory):
+    """compressPreprocessed (the writer side of --preprocess --compress) built
+    from the brr sources with zlib, as a small driver."""
+    import shutil
+    needs_zlib(brr)
+    from bayesrrcmd_gb300.build import HOST
+    d = tmp_path_factory.mktemp("compress")
+    (d / "driver.cpp").write_text(COMPRESS_DRIVER)
+    cxx = shutil.which("g++") or shutil.which("c++")
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-DBRR_WITH_ZLIB", f"-I{HOST}", str(d / "driver.cpp"),
+                        str(HOST / "data.cpp"), "-o", str(d / "compress"), "-lz"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return str(d / "compress")
+
+
+@pytest.mark.parametrize("sparse", [None, "ragged", "eigen"])
+def test_written_compressed_files_round_trip(brr, compressor, tmp_path, sparse):
+    import zlib
+    prefix, payload, N, M = dataset(tmp_path, missing=0.02)
+    write_kind(prefix, payload, N, sparse)
+    pp, ix = (str(prefix) + s for s in PP_FILES[sparse])
+    before = np.fromfile(ix, np.uint64).reshape(M, 3)
+    raw = open(pp, "rb").read()
+    records = [raw[int(e[0]):int(e[0]) + int(e[2])] for e in before]
+    r = export(brr, prefix, tmp_path / "plain.bed", *sparse_args(sparse))
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([compressor, pp, ix, str(M)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    after = np.fromfile(ix, np.uint64).reshape(M, 3)
+    np.testing.assert_array_equal(after[:, 2], before[:, 2])
+    np.testing.assert_array_equal(after[1:, 0], np.cumsum(after[:-1, 1]))
+    packed = open(pp, "rb").read()
+    assert len(packed) == int(after[-1, 0] + after[-1, 1])
+    for j, e in enumerate(after):
+        assert zlib.decompress(packed[int(e[0]):int(e[0] + e[1])]) == records[j]
+    r = export(brr, prefix, tmp_path / "back.bed", "--compress", *sparse_args(sparse))
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(read_payload(tmp_path / "back.bed", N, M),
+                                  read_payload(tmp_path / "plain.bed", N, M))
+    # a second pass refuses records that are compressed already
+    r = subprocess.run([compressor, pp, ix, str(M)], capture_output=True, text=True)
+    assert r.returncode == 1 and "compressed already" in r.stderr
