@@ -473,6 +473,14 @@ int main(int argc, const char *argv[])
                 return 1;
             }
             return ppbayes(opt) ? 0 : 1;
+        case AnalysisType::AsyncPpBayes:
+        case AnalysisType::Gauss:
+        case AnalysisType::AsyncGauss:
+            // the asynchronous graph and the BayesW (Gauss) analyses of the
+            // reference (src/analysisrunner.cpp:219-268) are not on this path
+            std::cerr << "Error: this GPU sampler runs --analysis-type ppbayes (and preprocess); "
+                         "asyncppbayes, gauss and asyncgauss are not supported" << std::endl;
+            return 1;
         default:
             std::cerr << "unknown analysis type" << std::endl;
             return 1;

@@ -93,6 +93,12 @@ static AnalysisType parseAnalysisType(const std::string &t)
         return AnalysisType::Preprocess;
     if (t == "ppbayes")
         return AnalysisType::PpBayes;
+    if (t == "asyncppbayes")
+        return AnalysisType::AsyncPpBayes;
+    if (t == "gauss")
+        return AnalysisType::Gauss;
+    if (t == "asyncgauss")
+        return AnalysisType::AsyncGauss;
     return AnalysisType::Unknown;
 }
 

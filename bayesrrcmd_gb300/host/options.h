@@ -8,7 +8,7 @@
 
 namespace brr {
 
-enum class AnalysisType { Unknown = 0, Preprocess, PpBayes };   // src/common.h:8-15 (path subset)
+enum class AnalysisType { Unknown = 0, Preprocess, PpBayes, AsyncPpBayes, Gauss, AsyncGauss };   // src/common.h:8-15
 enum class InputType { Unknown = 0, BED, CSV };                  // src/common.h:19-23
 enum class PreprocessDataType { None = 0, Dense, SparseEigen, SparseRagged };  // src/common.h:27-32
 

@@ -60,7 +60,20 @@ def test_analysis_type(brr):
     assert opts(brr, "--preprocess")["analysis"] == 1
     assert opts(brr, "--analysis-type", "preprocess")["analysis"] == 1
     assert opts(brr, "--analysis-type", "ppbayes")["analysis"] == 2
-    assert opts(brr, "--analysis-type", "gauss")["analysis"] == 0
+    # test/optionstest.cpp:133-154: the reference's other analysis types parse to
+    # their own values (src/common.h:8-15) ...
+    assert opts(brr, "--analysis-type", "asyncppbayes")["analysis"] == 3
+    assert opts(brr, "--analysis-type", "gauss")["analysis"] == 4
+    assert opts(brr, "--analysis-type", "asyncgauss")["analysis"] == 5
+    assert opts(brr, "--analysis-type", "other")["analysis"] == 0
+    assert opts(brr)["analysis"] == 0
+
+
+@pytest.mark.parametrize("kind", ["asyncppbayes", "gauss", "asyncgauss"])
+def test_analyses_off_this_path_are_refused(brr, kind):
+    """... and are refused with a message naming what runs here."""
+    r = subprocess.run([brr, "--analysis-type", kind, "--S", "0.01"], capture_output=True, text=True)
+    assert r.returncode == 1 and "ppbayes" in r.stderr and "not supported" in r.stderr
 
 
 def test_sparse_data_and_chain_flags(brr):
