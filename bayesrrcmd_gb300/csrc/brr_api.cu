@@ -1306,7 +1306,8 @@ int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, dou
 
 // Allocation-free variant of brr_xbeta for callers that cannot allocate
 // device memory; the term list goes through the static array of
-// brr_noalloc.cu and the result into the caller's device buffer.
+// brr_noalloc.cu and the result into the caller's device buffer, which is
+// checked first (device memory of this context's GPU, N doubles long).
 int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, double *d_out)
 {
     if (!ctx || !ctx->packed || !d_out || n < 0 || (n > 0 && (!idx || !b)))
@@ -1319,8 +1320,10 @@ int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_
             return fail(BRR_ERR_ARG, "marker index out of range");
     BRR_CUDA(cudaSetDevice(ctx->dev));
     std::string why;
-    if (noalloc_xbeta(ctx->dev, ctx->st, ctx->kind, ctx->cfg.N, ctx->d_codes, ctx->col_stride, ctx->d_table, idx, b,
-                      n, d_out, why) != cudaSuccess)
+    if (!noalloc_check_output(ctx->dev, d_out, sizeof(double) * (size_t)ctx->cfg.N, why))
+        return fail(BRR_ERR_ARG, why);
+    if (noalloc_xbeta(ctx->st, ctx->kind, ctx->cfg.N, ctx->d_codes, ctx->col_stride, ctx->d_table, idx, b, n, d_out,
+                      why) != cudaSuccess)
         return fail(BRR_ERR_CUDA, why);
     return BRR_OK;
 }

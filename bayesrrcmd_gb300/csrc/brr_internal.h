@@ -218,9 +218,10 @@ cudaError_t launch_synth_bed(uint8_t *out, int64_t N, int64_t M, uint32_t seed, 
                              double miss, cudaStream_t st, double beta_a = 0.0, double beta_b = 0.0);
 cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st);
 size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a);
-cudaError_t noalloc_xbeta(int dev, cudaStream_t st, int kind, int64_t N, const uint8_t *codes, int64_t col_stride,
+cudaError_t noalloc_xbeta(cudaStream_t st, int kind, int64_t N, const uint8_t *codes, int64_t col_stride,
                           const double *table, const uint32_t *idx, const double *b, int64_t n, double *d_out,
                           std::string &why);
+bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string &why);
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem);
 size_t sweep_block_smem_bytes(const SweepArgs &a);
 cudaError_t launch_gather_block(const uint32_t *order, int64_t M, int64_t N, const double *table,

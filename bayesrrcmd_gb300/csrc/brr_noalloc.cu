@@ -12,12 +12,22 @@
 // The array holds at most BRR_NOALLOC_MAX_TERMS terms (12 bytes each,
 // 768 KiB); every GPU that loads the library keeps it until the process exits.
 // Host code never uses the array's name as an address: at set-up, once per
-// device and with that device current, cudaGetSymbolAddress gives the device
-// address that is passed to the kernel.  The first call on a device performs
-// that set-up, so it should come before any stream capture.  All calls share
-// the one array; the kernel reads only the n entries the same call wrote, so
-// nothing has to start at zero, and calls that overlap on the GPU (two
-// streams, two host threads, two contexts on one device) race on it.
+// device context and with that device current, cudaGetSymbolAddress gives the
+// device address that is passed to the kernel.  The address is cached per
+// CUDA context, keyed by the context's process-unique id (cuCtxGetId: the
+// primary context of a device, or any other context the caller made
+// current), so a context created again after cudaDeviceReset looks the
+// address up again even when the driver reuses the old context's handle.  The first call on a device (or in a new
+// context) performs that set-up, so it should come before any stream capture.
+// All calls share the one array; the kernel reads only the n entries the same
+// call wrote, so nothing has to start at zero, and calls that overlap on the
+// GPU (two streams, two host threads, two contexts on one device) race on it.
+// Every call is synchronous: it returns once the output is written.
+//
+// The output buffer is checked before the launch, without allocating: it must
+// be device (or managed) memory of the context's device, with at least N
+// doubles from d_out to the end of its allocation.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -81,42 +91,138 @@ __global__ void __launch_bounds__(kThreads) k_xbeta_static(int kind, int64_t N, 
 
 namespace {
 
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 std::mutex g_setup_mutex;
-NoallocTerms *g_terms_addr[kMaxDevices] = {};
 
-// Device address of the static term array on the current device, looked up
-// once per device.
-cudaError_t terms_address(int dev, NoallocTerms **out)
+// Device address of the static term array, per CUDA context: the module (and
+// with it the array) is loaded once per context, so a context made anew gets
+// a fresh lookup.  Contexts are told apart by their id, which the driver never
+// reuses within a process (a destroyed context's handle may be reused).
+struct TermsAddr {
+    unsigned long long ctx_id;
+    NoallocTerms *addr;
+};
+TermsAddr g_terms_addr[kMaxContexts] = {};
+int g_n_terms_addr = 0;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+typedef CUresult (*MemGetAddressRangeFn)(CUdeviceptr *, size_t *, CUdeviceptr);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+MemGetAddressRangeFn g_mem_get_address_range = nullptr;
+
+// Driver entry points of the three queries, through the runtime (the library
+// does not link libcuda directly).  Called with g_setup_mutex held.
+cudaError_t driver_entry_points(std::string &why)
+{
+    if (g_ctx_get_current && g_ctx_get_id && g_mem_get_address_range)
+        return cudaSuccess;
+    const char *names[3] = {"cuCtxGetCurrent", "cuCtxGetId", "cuMemGetAddressRange"};
+    void *f[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < 3; ++k) {
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        const cudaError_t e = cudaGetDriverEntryPointByVersion(names[k], &f[k], 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !f[k]) {
+            why = std::string("the driver entry point ") + names[k] + " is unavailable";
+            return e != cudaSuccess ? e : cudaErrorNotSupported;
+        }
+    }
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f[0]);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f[1]);
+    g_mem_get_address_range = reinterpret_cast<MemGetAddressRangeFn>(f[2]);
+    return cudaSuccess;
+}
+
+// Device address of the static term array in the current context.
+cudaError_t terms_address(NoallocTerms **out, std::string &why)
 {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_terms_addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_terms);
-        if (e != cudaSuccess)
-            return e;
-        g_terms_addr[dev] = static_cast<NoallocTerms *>(p);
+    cudaError_t e = driver_entry_points(why);
+    if (e != cudaSuccess)
+        return e;
+    CUcontext cur = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&cur) != CUDA_SUCCESS || !cur || g_ctx_get_id(cur, &id) != CUDA_SUCCESS) {
+        why = "no current CUDA context";
+        return cudaErrorInvalidDevice;
     }
-    *out = g_terms_addr[dev];
+    for (int k = 0; k < g_n_terms_addr; ++k)
+        if (g_terms_addr[k].ctx_id == id) {
+            *out = g_terms_addr[k].addr;
+            return cudaSuccess;
+        }
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_terms);
+    if (e != cudaSuccess) {
+        why = std::string("cudaGetSymbolAddress of the static term array failed: ") + cudaGetErrorString(e);
+        return e;
+    }
+    // the table is small: past kMaxContexts contexts the oldest entry makes room
+    if (g_n_terms_addr == kMaxContexts) {
+        for (int k = 1; k < kMaxContexts; ++k)
+            g_terms_addr[k - 1] = g_terms_addr[k];
+        --g_n_terms_addr;
+    }
+    g_terms_addr[g_n_terms_addr++] = {id, static_cast<NoallocTerms *>(p)};
+    *out = static_cast<NoallocTerms *>(p);
     return cudaSuccess;
 }
 
 }  // namespace
 
-cudaError_t noalloc_xbeta(int dev, cudaStream_t st, int kind, int64_t N, const uint8_t *codes, int64_t col_stride,
+// Whether d_out is device (or managed) memory of device `dev` with at least
+// `bytes` bytes from d_out to the end of its allocation.  Allocates nothing.
+bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string &why)
+{
+    if ((uintptr_t)d_out % alignof(double) != 0) {
+        why = "d_out must be aligned to 8 bytes";
+        return false;
+    }
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, d_out);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        why = std::string("d_out is not a CUDA pointer: ") + cudaGetErrorString(e);
+        return false;
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) {
+        why = "d_out must be device or managed memory (got host or unregistered memory)";
+        return false;
+    }
+    if (a.device != dev) {
+        why = "d_out belongs to device " + std::to_string(a.device) + ", the context runs on device " +
+              std::to_string(dev);
+        return false;
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_setup_mutex);
+        if (driver_entry_points(why) != cudaSuccess)
+            return false;
+    }
+    CUdeviceptr base = 0;
+    size_t size = 0;
+    if (g_mem_get_address_range(&base, &size, (CUdeviceptr)d_out) != CUDA_SUCCESS) {
+        why = "the allocation holding d_out could not be found";
+        return false;
+    }
+    const size_t left = (size_t)(base + size - (CUdeviceptr)d_out);
+    if (left < bytes) {
+        why = "d_out has " + std::to_string(left) + " bytes to the end of its allocation; " + std::to_string(bytes) +
+              " (N doubles) are needed";
+        return false;
+    }
+    return true;
+}
+
+cudaError_t noalloc_xbeta(cudaStream_t st, int kind, int64_t N, const uint8_t *codes, int64_t col_stride,
                           const double *table, const uint32_t *idx, const double *b, int64_t n, double *d_out,
                           std::string &why)
 {
-    if (dev < 0 || dev >= kMaxDevices) {
-        why = "device ordinal beyond the set-up table";
-        return cudaErrorInvalidDevice;
-    }
     NoallocTerms *terms = nullptr;
-    cudaError_t e = terms_address(dev, &terms);
-    if (e != cudaSuccess) {
-        why = std::string("cudaGetSymbolAddress of the static term array failed: ") + cudaGetErrorString(e);
+    cudaError_t e = terms_address(&terms, why);
+    if (e != cudaSuccess)
         return e;
-    }
     if (n > 0) {
         e = cudaMemcpyAsync(terms->idx, idx, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess)

@@ -207,9 +207,14 @@ int brr_synth_bed_device_beta(uint8_t *d_bed, int64_t N, int64_t M, uint32_t see
  * x[i, idx[q]] as brr_xbeta, but into a caller-owned device buffer of N
  * doubles, with idx/b (host arrays) staged in a fixed static device array
  * of BRR_NOALLOC_MAX_TERMS terms; n above that limit is rejected with
- * BRR_ERR_ARG.  Calls no cudaMalloc/cudaFree.  The first call on a device
- * looks up the array's device address, so make it before any stream
- * capture; calls that overlap on the GPU share the array and race. */
+ * BRR_ERR_ARG.  Calls no cudaMalloc/cudaFree.  d_out is checked before any
+ * launch, without allocating: it must be device or managed memory of the
+ * context's GPU, 8-byte aligned, with N doubles to the end of its allocation;
+ * otherwise BRR_ERR_ARG.  The first call on a device (and in each new CUDA
+ * context) looks up the array's device address, so make it before any stream
+ * capture.  Every call is synchronous on the context's stream: it returns
+ * once d_out is written.  Calls that overlap on the GPU share the array and
+ * race. */
 #define BRR_NOALLOC_MAX_TERMS 65536
 int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, double *d_out);
 
