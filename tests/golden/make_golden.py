@@ -26,6 +26,7 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
 import oracle_lib as O  # noqa: E402
+from refdir import reference_dir  # noqa: E402
 from bayesrrcmd_gb300 import plink  # noqa: E402
 
 S2 = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
@@ -66,7 +67,7 @@ def make_synth(kind: int, iters: int = 5):
 
 
 def main():
-    z = Path("/root/reference/test.zip")
+    z = reference_dir() / "test.zip"
     if z.exists():
         raw = np.frombuffer(zipfile.ZipFile(z).read("test/data/uk10k_chr1_1mb.bed"), np.uint8)
         N, M = 3642, 6717

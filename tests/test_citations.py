@@ -10,9 +10,10 @@ import re
 from pathlib import Path
 
 import pytest
+from refdir import reference_dir
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path("/root/reference")
+REF = reference_dir()
 
 QUALIFIED = re.compile(r"\b((?:src|test|test\.groups)/[\w./-]+\.(?:cpp|h|hpp|txt|R|cva))((?::\d+(?:-\d+)?)"
                        r"(?:,\s*:\d+(?:-\d+)?)*)")

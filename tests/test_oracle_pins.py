@@ -15,9 +15,10 @@ import numpy as np
 import pytest
 
 import oracle_lib as O
+from refdir import reference_dir
 from bayesrrcmd_gb300 import plink
 
-REF = Path("/root/reference")
+REF = reference_dir()
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 

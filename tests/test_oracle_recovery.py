@@ -23,8 +23,9 @@ import numpy as np
 import pytest
 
 import oracle_lib as O
+from refdir import reference_dir
 
-REF = Path("/root/reference")
+REF = reference_dir()
 GROUPS = REF / "test.groups"
 
 
