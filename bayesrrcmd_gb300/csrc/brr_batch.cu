@@ -424,7 +424,8 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
             bool ok = true;
             const long long tw = prof ? clock64() : 0;
             if (lane == 0)
-                ok = counter_wait(cnt1, (unsigned long long)a.G * (unsigned long long)(b + 1), a.err, a.timeout_ns);
+                ok = counter_wait(cnt1, (unsigned long long)(a.G + a.phantom) * (unsigned long long)(b + 1), a.err,
+                                  a.timeout_ns);
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
             __syncwarp();   // orders lane 0's acquire before the other lanes' loads
             if (!ok) {

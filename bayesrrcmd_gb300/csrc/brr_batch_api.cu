@@ -50,6 +50,7 @@ struct brr_batch {
     cudaStream_t st = nullptr;
     cudaEvent_t ev[4] = {};
     uint64_t wait_limit_ns = 2000000000ull;
+    int phantom = 0;
 
     uint8_t *d_codes = nullptr;
     int64_t *d_counts = nullptr;
@@ -577,6 +578,7 @@ int brr_batch_iterate(brr_batch *b, int32_t n_iter)
         a.part = b->d_part;
         a.err = b->d_err;
         a.timeout_ns = b->wait_limit_ns;
+        a.phantom = b->phantom;
         a.prof = b->profile ? b->d_prof : nullptr;
         BATCH_CUDA(cudaEventRecord(b->ev[0], b->st));
         BATCH_CUDA(launch_sweep_batch(a, kmax, b->st));
@@ -707,11 +709,12 @@ int brr_batch_set_profiling(brr_batch *b, int32_t on)
     return BRR_OK;
 }
 
-int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns)
+int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns, int32_t phantom_arrivals)
 {
-    if (!b || timeout_ns == 0)
-        return api_fail(BRR_ERR_ARG, "null batch or zero limit");
+    if (!b || timeout_ns == 0 || phantom_arrivals < 0)
+        return api_fail(BRR_ERR_ARG, "null batch, zero limit or negative phantom arrivals");
     b->wait_limit_ns = timeout_ns;
+    b->phantom = phantom_arrivals;
     return BRR_OK;
 }
 

@@ -157,6 +157,7 @@ struct BatchArgs {
     double *part;                    // [G][C][2] per slice: sum(E) (bits of an int64) and sum(eps^2)
     int *err;
     uint64_t timeout_ns;
+    int phantom;                     // extra arrivals the dot barrier waits for (tests of the timeout path)
     long long *prof;                 // optional [8] cycle counters of CTA 0
 };
 

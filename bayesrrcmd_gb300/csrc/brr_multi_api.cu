@@ -477,6 +477,22 @@ int brr_multi_get_state(brr_multi *m, int32_t i, brr_state *st)
     return brr_get_state(m->inst[i], st);
 }
 
+// Wait limit and phantom barrier arrivals of instance i (every instance when
+// i < 0): the instance's own context settings, read when its sweep arguments
+// are built.
+int brr_multi_set_wait_limit(brr_multi *m, int32_t i, uint64_t timeout_ns, int32_t phantom_arrivals)
+{
+    if (!m || i >= m->n)
+        return api_fail(BRR_ERR_ARG, "instance out of range");
+    for (int k = 0; k < m->n; ++k)
+        if (i < 0 || k == i) {
+            const int rc = brr_set_wait_limit(m->inst[k], timeout_ns, phantom_arrivals);
+            if (rc)
+                return rc;
+        }
+    return BRR_OK;
+}
+
 // Device time of the iteration graphs (all instances' draws, records, the one
 // sweep launch and the statistics) and wall time of the last brr_multi_iterate
 // call; per instance (optional, n values each): CTAs, round width and the last

@@ -69,7 +69,7 @@ EXPORTS = [
     "brr_batch_get_geometry",
     "brr_multi_create", "brr_multi_destroy", "brr_multi_pack_bed", "brr_multi_pack_bed_device",
     "brr_multi_set_groups", "brr_multi_set_phenotype", "brr_multi_init", "brr_multi_tune", "brr_multi_iterate",
-    "brr_multi_get_state", "brr_multi_get_timing", "brr_synth_bed_device_beta",
+    "brr_multi_get_state", "brr_multi_get_timing", "brr_synth_bed_device_beta", "brr_multi_set_wait_limit",
 ]
 
 
@@ -120,7 +120,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_batch_iterate.argtypes = [P, C.c_int32]
     lib.brr_batch_get_chain_state.argtypes = [P, C.c_int32, C.POINTER(BrrState)]
     lib.brr_batch_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
-    lib.brr_batch_set_wait_limit.argtypes = [P, C.c_uint64]
+    lib.brr_batch_set_wait_limit.argtypes = [P, C.c_uint64, C.c_int32]
     lib.brr_batch_set_profiling.argtypes = [P, C.c_int32]
     lib.brr_batch_get_geometry.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
     lib.brr_multi_create.argtypes = [C.POINTER(BrrConfig), C.c_int32, C.POINTER(P)]
@@ -133,6 +133,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_multi_tune.argtypes = [P, C.c_int32]
     lib.brr_multi_iterate.argtypes = [P, C.c_int32]
     lib.brr_multi_get_state.argtypes = [P, C.c_int32, C.POINTER(BrrState)]
+    lib.brr_multi_set_wait_limit.argtypes = [P, C.c_int32, C.c_uint64, C.c_int32]
     lib.brr_multi_get_timing.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     for name in EXPORTS:
@@ -433,8 +434,8 @@ class Batch:
         self._check(self.lib.brr_batch_get_timing(self.h, C.byref(sw), C.byref(tot), _ptr(cyc, C.c_int64)))
         return sw.value, tot.value, cyc
 
-    def set_wait_limit(self, timeout_ns: int):
-        self._check(self.lib.brr_batch_set_wait_limit(self.h, int(timeout_ns)))
+    def set_wait_limit(self, timeout_ns: int, phantom_arrivals: int = 0):
+        self._check(self.lib.brr_batch_set_wait_limit(self.h, int(timeout_ns), int(phantom_arrivals)))
 
     def set_profiling(self, on: bool):
         """Phase counters (timing()'s cycles) on or off; timed runs keep them off."""
@@ -505,6 +506,9 @@ class Multi:
 
     def iterate(self, n: int = 1):
         self._check(self.lib.brr_multi_iterate(self.h, int(n)))
+
+    def set_wait_limit(self, timeout_ns: int, phantom_arrivals: int = 0, instance: int = -1):
+        self._check(self.lib.brr_multi_set_wait_limit(self.h, int(instance), int(timeout_ns), int(phantom_arrivals)))
 
     def state(self, i: int) -> dict:
         cfg = self.cfgs[i]

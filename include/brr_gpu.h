@@ -260,7 +260,12 @@ int brr_batch_get_timing(brr_batch *b, double *sweep_ms, double *total_ms, int64
 /* Phase counters on (1) or off (0, the default; the cycles then read zero):
  * the counting runs a variant of the sweep kernel with clock reads. */
 int brr_batch_set_profiling(brr_batch *b, int32_t on);
-int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns);
+/* Limit of every device-side wait of the batched sweep (default 2 s);
+ * phantom_arrivals > 0 makes the barrier before the resolve wait for that many
+ * CTAs more than exist (tests of the timeout path).  A wait that runs out
+ * makes brr_batch_iterate return BRR_ERR_TIMEOUT; brr_batch_init then starts
+ * the chains again. */
+int brr_batch_set_wait_limit(brr_batch *b, uint64_t timeout_ns, int32_t phantom_arrivals);
 /* CTAs of the sweep, individuals per slice and shared memory per CTA. */
 int brr_batch_get_geometry(brr_batch *b, int32_t *ctas, int32_t *slice, int64_t *smem_bytes);
 
@@ -283,6 +288,12 @@ int brr_multi_init(brr_multi *m);
 int brr_multi_tune(brr_multi *m, int32_t rounds);
 int brr_multi_iterate(brr_multi *m, int32_t n_iter);
 int brr_multi_get_state(brr_multi *m, int32_t i, brr_state *st);
+/* Limit of every device-side wait of instance i's sweep (i < 0: every
+ * instance; default 2 s); phantom_arrivals > 0 makes its grid barrier wait for
+ * that many CTAs more than it has (tests of the timeout path).  A wait that
+ * runs out makes brr_multi_iterate return BRR_ERR_TIMEOUT; brr_multi_init then
+ * starts every instance again. */
+int brr_multi_set_wait_limit(brr_multi *m, int32_t i, uint64_t timeout_ns, int32_t phantom_arrivals);
 /* Device time of the iteration graphs and wall time of the last
  * brr_multi_iterate call (ms); per instance (optional, n values each): CTAs,
  * round width and the last sweep's time (ms). */

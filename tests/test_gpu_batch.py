@@ -132,3 +132,27 @@ def test_batch_phase_counting_variant_changes_no_result(gpu_lib):
     assert (counted.timing()[2] > 0).any()
     plain.close()
     counted.close()
+
+
+def test_batch_wait_limit_returns_timeout_and_batch_recovers(gpu_lib):
+    """The barrier before the resolve waits for a phantom CTA: every wait runs
+    out after its short limit (the CTAs leave and free their TMEM), the call
+    returns BRR_ERR_TIMEOUT, and the batch, re-initialised, follows the
+    oracle's chains."""
+    N, M, C = 1000, 96, 32
+    bed, ys = problem(N, M, C, seed=12)
+    b = make_batch(bed, N, ys, S1, C, seed=4, chain0=3)
+    b.set_wait_limit(50_000_000, 1)
+    for _ in range(2):
+        with pytest.raises(gpu.BrrError) as e:
+            b.iterate(1)
+        assert e.value.code == -4
+    b.set_wait_limit(2_000_000_000, 0)
+    b.init()
+    b.iterate(2)
+    for c in (0, 31):
+        oc = O.OracleChain(bed, N, ys[c], S1, seed=4, chain=3 + c, perm_chain=3)
+        oc.iterate(0)
+        oc.iterate(1)
+        compare(b.state(c), oc.state(), f"chain {c}")
+    b.close()

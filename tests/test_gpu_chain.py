@@ -221,6 +221,34 @@ def test_wait_limit_returns_timeout_status_and_context_recovers(gpu_lib):
     assert_close(ch.state(), oc.state())
 
 
+@pytest.mark.parametrize("miss", [0.0, 0.02])
+def test_blocked_sweep_wait_limit_returns_timeout_and_context_recovers(gpu_lib, miss):
+    """The Gram-blocked FP32C sweep: its grid barrier waits for a phantom CTA;
+    the barrier wait and the role signals run out after the short limit, the
+    bulk Gram copies in flight are waited for, the call returns BRR_ERR_TIMEOUT
+    and the same context, re-initialised, follows the oracle's chain."""
+    N, M = 1500, 300
+    bed, y = problem(N, M, seed=3, miss=miss)
+    ch = make_gpu(bed, N, y, S1, 0, form=gpu.FORM_FP32C, seed=2, gram=1, refresh_every=3)
+    assert ch.gram_info()["blocked"]
+    ch.set_wait_limit(50_000_000, 1)
+    for _ in range(2):
+        with pytest.raises(gpu.BrrError) as e:
+            ch.iterate(1)
+        assert e.value.code == -4
+    ch.set_wait_limit(2_000_000_000, 0)
+    ch.init()
+    ch.iterate(2)
+    oc = O.OracleChain(bed, N, y, S1, kind=0, seed=2)
+    oc.iterate(0)
+    oc.iterate(1)
+    s, o = ch.state(), oc.state()
+    np.testing.assert_array_equal(s["comp"], o["comp"])
+    nz = o["beta"] != 0
+    np.testing.assert_allclose(s["beta"][nz], o["beta"][nz], rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(s["eps"], o["eps"], rtol=0, atol=1e-10)
+
+
 def test_call_order_errors(gpu_lib):
     ch = gpu.Chain(gpu.ChainConfig(N=100, M=3))
     with pytest.raises(gpu.BrrError):

@@ -128,3 +128,29 @@ def test_multi_single_instance_equals_single_chain(gpu_lib):
     np.testing.assert_array_equal(a["eps"], b["eps"])
     m.close()
     ch.close()
+
+
+def test_multi_wait_limit_returns_timeout_and_instances_recover(gpu_lib):
+    """One instance's grid barrier waits for a phantom CTA: its waits run out
+    after the short limit, the iteration returns BRR_ERR_TIMEOUT while the
+    other instances finish, and after brr_multi_init every instance follows
+    its oracle chain again."""
+    probs = problems(SHAPES[:3], 80)
+    m = make(probs, gpu.FORM_FP64, S1)
+    m.set_wait_limit(50_000_000, 1, instance=1)
+    with pytest.raises(gpu.BrrError) as e:
+        m.iterate(1)
+    assert e.value.code == -4
+    m.set_wait_limit(2_000_000_000, 0)
+    m.init()
+    m.iterate(2)
+    ocs = oracles(probs, S1)
+    for k, oc in enumerate(ocs):
+        oc.iterate(0)
+        oc.iterate(1)
+        s, o = m.state(k), oc.state()
+        np.testing.assert_array_equal(s["comp"], o["comp"], err_msg=f"instance {k}")
+        nz = o["beta"] != 0
+        np.testing.assert_allclose(s["beta"][nz], o["beta"][nz], rtol=1e-10, err_msg=f"instance {k}")
+        np.testing.assert_allclose(s["eps"], o["eps"], rtol=0, atol=1e-11, err_msg=f"instance {k}")
+    m.close()
