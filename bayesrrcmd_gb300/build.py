@@ -104,8 +104,32 @@ def build_cli(verbose: bool = False) -> Path:
     return CLI
 
 
+ADAPTER = PKG / "adapter"
+ADAPTER_LIB = LIBDIR / "libbrr_adapter.so"
+
+
+def build_adapter(verbose: bool = False) -> Path:
+    """Compile the reference-interface adapter (GpuMarkerBuilder,
+    GpuSweepGraph; C++17) into libbrr_adapter.so against libbrr_gpu.so."""
+    lib = build_gpu(verbose)
+    srcs = sorted(ADAPTER.glob("*.cpp"))
+    deps = srcs + sorted(ADAPTER.glob("*.h")) + [PKG.parent / "include" / "brr_gpu.h", lib]
+    if _stale(ADAPTER_LIB, deps):
+        cxx = shutil.which("g++") or shutil.which("c++")
+        if not cxx:
+            raise RuntimeError("no C++ compiler for the adapter")
+        cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-o", str(ADAPTER_LIB), *map(str, srcs),
+               f"-L{LIBDIR}", "-lbrr_gpu", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of libbrr_adapter.so failed:\n{r.stdout}\n{r.stderr}")
+    return ADAPTER_LIB
+
+
 def build_all(verbose: bool = False):
-    return build_gpu(verbose), build_cli(verbose)
+    return build_gpu(verbose), build_cli(verbose), build_adapter(verbose)
 
 
 if __name__ == "__main__":

@@ -371,6 +371,214 @@ def run_uneven(lib, gpu, torch, device, steps, tune_rounds, scale=1.0):
                 N=N.tolist(), M=M.tolist())
 
 
+# Ragged sparse markers (the C2 configuration): N = 20,000 x M = 50,000, 70 % of
+# the markers rare (p ~ U(0.001, 0.05)), the rest p ~ U(0.05, 0.5), 1 % missing
+# genotypes, 500 causal markers with beta ~ N(0, 0.5/500), h2 = 0.5; the plain
+# FP64 form against the FP32C form with the FP64 refresh every 50 sweeps.
+R_N, R_M, R_RARE = 20_000, 50_000, 35_000
+R_WORKLOAD = ("ragged sparse BayesR, N=20,000 x M=50,000, 70% rare p~U(0.001,0.05), rest p~U(0.05,0.5), 1% missing, "
+              "500 causal, h2=0.5, S=0.01,0.001,0.0001")
+# The plain dense configuration C1 (CPU-runnable): N = 2,000 x M = 5,000,
+# p ~ U(0.05, 0.5), 100 causal, h2 = 0.5.
+C1_N, C1_M = 2_000, 5_000
+S1 = [[0.01, 0.001, 0.0001]]
+
+
+def synth_parts(torch, gpu, lib, device, N, parts, seed, missing):
+    """Concatenated device BED payloads, one per (markers, p_lo, p_hi) part."""
+    cb = (N + 3) // 4
+    out = []
+    for k, (m, lo, hi) in enumerate(parts):
+        d = torch.empty(m * cb, dtype=torch.uint8, device=device)
+        gpu.synth_bed_device(d.data_ptr(), N, m, seed + k, lo, hi, missing, lib=lib)
+        out.append(d)
+    return torch.cat(out) if len(out) > 1 else out[0]
+
+
+def synth_phenotype(gpu, lib, device, d_bed, N, M, n_causal, h2, seed):
+    """Phenotype from n_causal standardised columns (effects N(0, h2/n_causal))
+    plus N(0, 1-h2) noise, and the markers' genotype counts."""
+    rng = np.random.default_rng(seed)
+    probe = gpu.Chain(gpu.ChainConfig(N=N, M=M, S=S1, device=device), lib=lib)
+    probe.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+    causal = np.sort(rng.choice(M, n_causal, replace=False)).astype(np.uint32)
+    b = rng.normal(0.0, np.sqrt(h2 / n_causal), n_causal)
+    y = (probe.xbeta(causal, b) + rng.normal(0.0, np.sqrt(1.0 - h2), N)).astype(np.float32)
+    _, counts = probe.marker_table()
+    probe.close()
+    return y, counts
+
+
+def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed):
+    """W warm-up and K timed iterations of one chain; the library's CUDA-event
+    time of the timed ones."""
+    ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S1, seed=seed,
+                                   refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device), lib=lib)
+    ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+    ch.set_phenotype(y)
+    ch.init()
+    ch.iterate(warmup)
+    ch.iterate(steps)
+    sweep_ms, total_ms, rounds = ch.timing()
+    st = ch.state()
+    ch.close()
+    return dict(rate=M * steps / (total_ms / 1e3), ms_per_step=total_ms / steps, sweep_ms=sweep_ms / steps,
+                rounds=rounds / steps, beta=st["beta"], comp=st["comp"], sigmaE=st["sigmaE"])
+
+
+def cpu_rate(bed, N, y, kind, iters):
+    """Rate of the FP64 restatement (fast-flags build, one core) over all
+    markers of a small configuration, after one untimed iteration."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as O
+    O.use_timing_build()
+    oc = O.OracleChain(np.ascontiguousarray(bed), N, y, S1, kind=kind, seed=SEED)
+    oc.iterate(0)
+    t0 = time.perf_counter()
+    for it in range(1, 1 + iters):
+        oc.iterate(it)
+    dt = time.perf_counter() - t0
+    return {"value": bed.shape[0] * iters / dt, "unit": "marker-updates/s", "cores": 1, "kind": "port",
+            "sample": f"all {bed.shape[0]} markers x N={N}, {iters} Gibbs iterations after one untimed ({dt:.1f} s), "
+                      f"FP64 restatement built -O3 -ffast-math -funroll-loops"}
+
+
+def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
+    """C2: the FP64 and FP32C ragged chains, their rates and the roofline on
+    the index bytes; C1: the plain FP64 dense chain; the CPU restatement's
+    rate on both beside them."""
+    d_bed = synth_parts(torch, gpu, lib, device, R_N, [(R_RARE, 0.001, 0.05), (R_M - R_RARE, 0.05, 0.5)], SEED + 21,
+                        0.01)
+    y, counts = synth_phenotype(gpu, lib, device, d_bed, R_N, R_M, 500, 0.5, SEED + 21)
+    f64 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP64, steps, warmup, SEED)
+    f32 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED)
+    # algorithmic bytes of a sweep: 4 bytes per listed genotype (ones, twos, missing)
+    idx_bytes = 4.0 * float(counts[:, 1:4].sum())
+    hbm, _ = peaks()
+    achieved = idx_bytes / (f32["sweep_ms"] / 1e3) / 1e9
+    host_bed = d_bed.cpu().numpy().reshape(R_M, -1)
+    del d_bed
+    c1_bed = synth_parts(torch, gpu, lib, device, C1_N, [(C1_M, 0.05, 0.5)], SEED + 31, 0.0)
+    c1_y, _ = synth_phenotype(gpu, lib, device, c1_bed, C1_N, C1_M, 100, 0.5, SEED + 31)
+    c1 = time_chain(gpu, lib, device, c1_bed, C1_N, C1_M, c1_y, gpu.KIND_DENSE, gpu.FORM_FP64, 10, 3, SEED)
+    c1_host = c1_bed.cpu().numpy().reshape(C1_M, -1)
+    del c1_bed
+    torch.cuda.empty_cache()
+    out = {
+        "workload": R_WORKLOAD, "value": f32["rate"], "unit": "marker-updates/s", "form": "fp32c (refresh 50)",
+        "steps": steps, "ms_per_step": f32["ms_per_step"], "sweep_ms": f32["sweep_ms"],
+        "plain_fp64": {"value": f64["rate"], "ms_per_step": f64["ms_per_step"], "rounds_per_step": f64["rounds"]},
+        "speedup_fp32c_vs_plain": f32["rate"] / f64["rate"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "k_sweep (ragged, FP32C)",
+                     "algorithmic_bytes_per_launch": idx_bytes,
+                     "note": "4 bytes per listed genotype (ones, twos, missing) per sweep"},
+        "matched_error": {"beta_max_abs_diff_vs_plain": float(np.abs(f32["beta"] - f64["beta"]).max()),
+                          "component_mismatches_vs_plain": int(np.count_nonzero(f32["comp"] != f64["comp"])),
+                          "sigmaE_rel_diff_vs_plain": abs(f32["sigmaE"] / f64["sigmaE"] - 1),
+                          "compared": "final state after the warm-up and timed iterations (same draws)"},
+        "c1_dense_fp64": {"workload": "plain dense BayesR, N=2,000 x M=5,000, p~U(0.05,0.5), 100 causal, h2=0.5",
+                          "value": c1["rate"], "ms_per_step": c1["ms_per_step"], "unit": "marker-updates/s"},
+    }
+    if cpu:
+        out["cpu_baseline"] = cpu_rate(host_bed, R_N, y, 1, 3)
+        out["c1_dense_fp64"]["cpu_baseline"] = cpu_rate(c1_host, C1_N, c1_y, 0, 10)
+    return out
+
+
+def posterior_pair(a, b, n_iter, burn, thin, G, kmax):
+    """Two chains on the same draws, iterated in lockstep: posterior means of
+    beta, sigmaG and sigmaE and per-marker component frequencies over the kept
+    iterations (after `burn`, every `thin`-th), and the iterations whose
+    components differ between the two chains."""
+    sums = [None, None]
+    n_kept = 0
+    mismatch_iters, mismatches, first = 0, 0, None
+    t = [0.0, 0.0]
+    for it in range(n_iter):
+        for k, ch in enumerate((a, b)):
+            t0 = time.perf_counter()
+            ch.iterate(1)
+            t[k] += time.perf_counter() - t0
+        sa, sb = a.state(), b.state()
+        d = int(np.count_nonzero(sa["comp"] != sb["comp"]))
+        if d:
+            mismatch_iters += 1
+            mismatches += d
+            first = it if first is None else first
+        if it >= burn and (it - burn) % thin == 0:
+            n_kept += 1
+            for k, s in enumerate((sa, sb)):
+                freq = np.zeros((s["comp"].size, kmax))
+                freq[np.arange(s["comp"].size), s["comp"]] = 1.0
+                cur = dict(beta=s["beta"], sigmaG=np.asarray(s["sigmaG"], float), sigmaE=s["sigmaE"], freq=freq)
+                if sums[k] is None:
+                    sums[k] = {kk: np.array(v, dtype=float, copy=True) for kk, v in cur.items()}
+                else:
+                    for kk, v in cur.items():
+                        sums[k][kk] += v
+    ma = {k: v / n_kept for k, v in sums[0].items()}
+    mb = {k: v / n_kept for k, v in sums[1].items()}
+    nz = mb["beta"] != 0
+    floor = 1e-6 * float(np.abs(mb["beta"]).max())
+    rel_beta = np.abs(ma["beta"] - mb["beta"])[nz] / np.maximum(np.abs(mb["beta"][nz]), floor)
+    return {
+        "iterations": n_iter, "burn_in": burn, "thin": thin, "kept": n_kept,
+        "posterior_mean_beta_max_rel_diff": float(rel_beta.max()) if rel_beta.size else 0.0,
+        "posterior_mean_beta_rel_floor": floor,
+        "posterior_mean_beta_max_abs_diff": float(np.abs(ma["beta"] - mb["beta"]).max()),
+        "posterior_mean_sigmaG_max_rel_diff": float(np.max(np.abs(ma["sigmaG"] / mb["sigmaG"] - 1))),
+        "posterior_mean_sigmaE_rel_diff": float(abs(ma["sigmaE"] / mb["sigmaE"] - 1)),
+        "component_frequency_max_abs_diff": float(np.abs(ma["freq"] - mb["freq"]).max()),
+        "iterations_with_component_mismatch": mismatch_iters, "component_mismatches": mismatches,
+        "first_mismatch_iteration": first,
+        "markers_with_nonzero_posterior_mean_beta": int(nz.sum()),
+        "posterior_mean_sigmaG_plain": mb["sigmaG"].tolist(), "posterior_mean_sigmaE_plain": float(mb["sigmaE"]),
+        "wall_s_chosen": t[0], "wall_s_plain": t[1],
+    }
+
+
+def run_matched_chains(lib, gpu, torch, device, c3_iters, c2_iters):
+    """The chosen forms against the plain FP64 chain (itself within 1e-10 of
+    the FP64 oracle per iteration) over whole chains on the same draws: C3
+    (1,000 iterations, burn-in 200) and C2 (2,000 iterations, burn-in 500,
+    thin 5)."""
+    out = {}
+    d_bed, y, group = make_problem(lib, gpu, torch, device, 0)
+    mk = []
+    for form in (gpu.FORM_FP32C, gpu.FORM_FP64):
+        cfg = gpu.ChainConfig(N=N_IND, M=M_SNP, S=S_GROUPS, form=form, seed=SEED, chain=0,
+                              refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device)
+        ch = gpu.Chain(cfg, lib=lib)
+        ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+        ch.set_groups(group)
+        ch.set_phenotype(y)
+        ch.init()
+        mk.append(ch)
+    out["c3"] = {"workload": WORKLOAD, "chosen": "fp32c gram-blocked" if mk[0].gram_info()["blocked"] else "fp32c",
+                 **posterior_pair(mk[0], mk[1], c3_iters, min(200, c3_iters // 5), 1, 2, 4)}
+    for ch in mk:
+        ch.close()
+    del d_bed
+    torch.cuda.empty_cache()
+    d_bed = synth_parts(torch, gpu, lib, device, R_N, [(R_RARE, 0.001, 0.05), (R_M - R_RARE, 0.05, 0.5)], SEED + 21,
+                        0.01)
+    y, _ = synth_phenotype(gpu, lib, device, d_bed, R_N, R_M, 500, 0.5, SEED + 21)
+    mk = []
+    for form in (gpu.FORM_FP32C, gpu.FORM_FP64):
+        ch = gpu.Chain(gpu.ChainConfig(N=R_N, M=R_M, kind=gpu.KIND_RAGGED, form=form, S=S1, seed=SEED,
+                                       refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device), lib=lib)
+        ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+        ch.set_phenotype(y)
+        ch.init()
+        mk.append(ch)
+    out["c2"] = {"workload": R_WORKLOAD, "chosen": "fp32c (refresh 50)",
+                 **posterior_pair(mk[0], mk[1], c2_iters, min(500, c2_iters // 4), 5, 1, 4)}
+    for ch in mk:
+        ch.close()
+    return out
+
+
 def numpy_sample(m_sample, seed):
     """A CPU-generated sample of the workload: N individuals, m_sample markers."""
     from bayesrrcmd_gb300 import plink
@@ -429,6 +637,10 @@ def main():
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (32 regressions) measurement")
     ap.add_argument("--uneven-only", action="store_true", help="only the uneven-batch leg; --uneven-scale shrinks it")
     ap.add_argument("--uneven-scale", type=float, default=1.0)
+    ap.add_argument("--no-ragged", action="store_true", help="skip the ragged (C2) and C1 measurements")
+    ap.add_argument("--matched-chains", action="store_true",
+                    help="only the whole-chain comparisons of the chosen forms with the plain FP64 chain (C3: "
+                         "1,000 iterations, burn-in 200; C2: 2,000 iterations, burn-in 500, thin 5)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: N=100,000 x M=8,192 (200 MB of codes, above L2), same settings")
     args = ap.parse_args()
@@ -467,6 +679,12 @@ def main():
     lib = gpu.load_library()
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
+    if args.matched_chains:
+        mc = run_matched_chains(lib, gpu, torch, device, int(os.environ.get("BRR_C3_ITERS", "1000")),
+                                int(os.environ.get("BRR_C2_ITERS", "2000")))
+        if rank == 0:
+            print(json.dumps({"matched_chains": mc}))
+        return
     if args.uneven_only:
         uu = run_uneven(lib, gpu, torch, device, args.steps, 2, args.uneven_scale)
         if rank == 0:
@@ -548,6 +766,12 @@ def main():
                                 "instance_sweep_ms": uu["inst_ms"],
                                 "slowest_over_mean": uu["balance_max_over_mean"]},
                   "sizes": {"N": uu["N"], "M": uu["M"]}}
+    ragged = None
+    if not args.no_ragged and not args.small:
+        ragged = run_ragged(lib, gpu, torch, device, int(os.environ.get("BRR_RAGGED_STEPS", "10")), 3,
+                            cpu=not args.no_cpu and rank == 0)
+        ragged["value"] = replica_rate(world, R_M, ragged["steps"],
+                                       max_over_ranks(ragged["ms_per_step"] * ragged["steps"] / 1e3, dist, device))
     if rank != 0:
         return
     cpu = None
@@ -578,17 +802,6 @@ def main():
         "config": {"workload": WORKLOAD, "form": "fp32c" + (" gram-blocked" if fp32c["gram"]["blocked"] else ""),
                    "refresh_every": REFRESH,
                    "l2": f"inputs larger than L2 ({M_SNP * N_IND / 4 / 1e9:.2g} GB of codes per sweep)", "parallelism": "replicas" if world > 1 else "1 chain"},
-        "plain_fp64": {"value": plain_rate, "unit": "marker-updates/s", "ms_per_step": fp64["total_ms"] / args.steps,
-                       "speedup_chosen_vs_plain": value / world / plain_rate,
-                       "rounds_per_step": fp64["rounds"] / args.steps},
-        "matched_error": {"beta_max_abs_diff_vs_plain": float(np.abs(fp32c["beta"] - fp64["beta"]).max()),
-                          "sigmaE_rel_diff_vs_plain": abs(fp32c["sigmaE"] / fp64["sigmaE"] - 1),
-                          "sigmaG_max_rel_diff_vs_plain": float(np.max(np.abs(np.asarray(fp32c["sigmaG"]) /
-                                                                               np.asarray(fp64["sigmaG"]) - 1))),
-                          "component_mismatches_vs_plain": int(np.count_nonzero(fp32c["comp"] != fp64["comp"])),
-                          "component_counts_plain": np.bincount(fp64["comp"], minlength=4).tolist(),
-                          "compared": "final state after the warm-up and timed iterations (same draws)",
-                          "nonzero_beta_plain": int(nzb.sum())},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
                      "kernel": "k_sweep_block (FP32C dense, Gram-blocked)",
@@ -612,6 +825,18 @@ def main():
         "e2e": e2e,
         "batched": batched,
         "uneven": uneven,
+        "ragged": ragged,
+        "plain_fp64": {"value": plain_rate, "unit": "marker-updates/s", "ms_per_step": fp64["total_ms"] / args.steps,
+                       "speedup_chosen_vs_plain": value / world / plain_rate,
+                       "rounds_per_step": fp64["rounds"] / args.steps},
+        "matched_error": {"beta_max_abs_diff_vs_plain": float(np.abs(fp32c["beta"] - fp64["beta"]).max()),
+                          "sigmaE_rel_diff_vs_plain": abs(fp32c["sigmaE"] / fp64["sigmaE"] - 1),
+                          "sigmaG_max_rel_diff_vs_plain": float(np.max(np.abs(np.asarray(fp32c["sigmaG"]) /
+                                                                               np.asarray(fp64["sigmaG"]) - 1))),
+                          "component_mismatches_vs_plain": int(np.count_nonzero(fp32c["comp"] != fp64["comp"])),
+                          "component_counts_plain": np.bincount(fp64["comp"], minlength=4).tolist(),
+                          "compared": "final state after the warm-up and timed iterations (same draws)",
+                          "nonzero_beta_plain": int(nzb.sum())},
     }
     print(json.dumps(line))
 

@@ -335,7 +335,9 @@ int or_ragged_lists(const uint8_t *bed, int64_t N, int64_t M,
 struct or_markers {
     int kind;
     int64_t N, M;
-    double *x;          /* dense: M x N standardized columns */
+    double *x;          /* dense: M x N standardized columns (dense_lut == 0) */
+    double *lut;        /* dense: M x 4 standardized value per 2-bit code (dense_lut != 0) */
+    const uint8_t *bed; /* dense_lut != 0: the problem's BED payload */
     double *stats;      /* ragged: M x {mean, sd, sqrdZ, Zsum} */
     int64_t *off[3];    /* ragged: ones, twos, missing offsets (M+1 each) */
     int32_t *idx[3];
@@ -346,6 +348,7 @@ void or_markers_destroy(or_markers *m)
     if (!m)
         return;
     free(m->x);
+    free(m->lut);
     free(m->stats);
     for (int k = 0; k < 3; ++k) {
         free(m->off[k]);
@@ -365,7 +368,11 @@ int or_markers_create(const or_problem *p, or_markers **out)
     m->N = p->N;
     m->M = p->M;
     int rc = OR_OK;
-    if (p->kind == OR_KIND_DENSE) {
+    if (p->kind == OR_KIND_DENSE && p->dense_lut) {
+        m->lut = (double *)malloc(sizeof(double) * 4 * (size_t)p->M);
+        m->bed = p->bed;
+        rc = m->lut ? or_dense_lut(p->bed, p->N, p->M, m->lut) : OR_ERR_ARG;
+    } else if (p->kind == OR_KIND_DENSE) {
         m->x = (double *)malloc(sizeof(double) * (size_t)p->N * (size_t)p->M);
         rc = m->x ? or_dense_columns(p->bed, p->N, p->M, m->x) : OR_ERR_ARG;
     } else if (p->kind == OR_KIND_RAGGED || p->kind == OR_KIND_EIGEN) {
@@ -478,7 +485,15 @@ static void process_column(const or_problem *p, const or_markers *mk, or_state *
         denom[k - 1] = NM1 + sigmaEOverSigmaG * cVaI[k];
 
     double num;
-    if (mk->kind == OR_KIND_DENSE) {
+    if (mk->kind == OR_KIND_DENSE && mk->lut) {
+        /* the same column values as below, read through the code table */
+        const double *lut = mk->lut + 4 * (size_t)j;
+        const uint8_t *col = mk->bed + (size_t)j * (size_t)col_bytes(N);
+        double dot = 0.0;
+        for (int64_t i = 0; i < N; ++i)
+            dot += lut[code_at(col, i)] * s->eps[i];
+        num = dot + beta_old * (double)(N - 1);
+    } else if (mk->kind == OR_KIND_DENSE) {
         const double *x = mk->x + (size_t)j * (size_t)N;
         double dot = 0.0;
         for (int64_t i = 0; i < N; ++i)
@@ -575,7 +590,12 @@ static void process_column(const or_problem *p, const or_markers *mk, or_state *
     if (beta_old == 0.0 && beta_new == 0.0)
         return;                                   /* (:372) */
     const double dBeta = beta_old - beta_new;
-    if (mk->kind == OR_KIND_DENSE) {
+    if (mk->kind == OR_KIND_DENSE && mk->lut) {
+        const double *lut = mk->lut + 4 * (size_t)j;
+        const uint8_t *col = mk->bed + (size_t)j * (size_t)col_bytes(N);
+        for (int64_t i = 0; i < N; ++i)
+            s->eps[i] = s->eps[i] + dBeta * lut[code_at(col, i)];
+    } else if (mk->kind == OR_KIND_DENSE) {
         const double *x = mk->x + (size_t)j * (size_t)N;
         for (int64_t i = 0; i < N; ++i)
             s->eps[i] = s->eps[i] + dBeta * x[i];

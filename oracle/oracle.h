@@ -101,6 +101,12 @@ typedef struct {
      * iteration is the permutation of chain perm_chain's stream */
     int32_t shared_perm;
     uint32_t perm_chain;
+    /* dense markers: 0 stores the standardized columns (M x N doubles, as the
+     * reference's DenseMarker does); 1 keeps the four standardized values per
+     * marker and reads the codes from `bed` (which must outlive the markers),
+     * for problems whose columns do not fit in host memory.  Both read the
+     * same value for every genotype, in the same order: identical results. */
+    int32_t dense_lut;
 } or_problem;
 
 typedef struct {

@@ -40,3 +40,20 @@ def test_oracle_reproduces_golden(kind):
         assert s["sigmaE"] == d["trace_sigmaE"][it]
         np.testing.assert_array_equal(s["sigmaG"], d["trace_sigmaG"][it])
         assert s["mu"] == d["trace_mu"][it]
+
+
+def test_dense_lut_storage_equals_column_storage():
+    """The compact dense storage (four values per marker, codes read from the
+    BED payload) gives the same chain bit for bit as the stored columns."""
+    d = dict(np.load(GOLDEN / "synth_dense.npz"))
+    N = int(d["N"])
+    S = [[0.01, 0.001, 0.0001], [0.1, 0.01]]
+    a = O.OracleChain(d["bed"], N, d["y"], S, kind=0, group=d["group"], seed=int(d["seed"]))
+    b = O.OracleChain(d["bed"], N, d["y"], S, kind=0, group=d["group"], seed=int(d["seed"]), dense_lut=True)
+    for it in range(4):
+        a.iterate(it)
+        b.iterate(it)
+        sa, sb = a.state(), b.state()
+        for k in ("beta", "comp", "eps", "acum", "sigmaG"):
+            np.testing.assert_array_equal(sa[k], sb[k])
+        assert sa["sigmaE"] == sb["sigmaE"] and sa["mu"] == sb["mu"]
