@@ -461,6 +461,7 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
     c1_bed = synth_parts(torch, gpu, lib, device, C1_N, [(C1_M, 0.05, 0.5)], SEED + 31, 0.0)
     c1_y, _ = synth_phenotype(gpu, lib, device, c1_bed, C1_N, C1_M, 100, 0.5, SEED + 31)
     c1 = time_chain(gpu, lib, device, c1_bed, C1_N, C1_M, c1_y, gpu.KIND_DENSE, gpu.FORM_FP64, 10, 3, SEED)
+    c1c = time_chain(gpu, lib, device, c1_bed, C1_N, C1_M, c1_y, gpu.KIND_DENSE, gpu.FORM_FP32C, 10, 3, SEED)
     c1_host = c1_bed.cpu().numpy().reshape(C1_M, -1)
     del c1_bed
     torch.cuda.empty_cache()
@@ -478,7 +479,8 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
                           "sigmaE_rel_diff_vs_plain": abs(f32["sigmaE"] / f64["sigmaE"] - 1),
                           "compared": "final state after the warm-up and timed iterations (same draws)"},
         "c1_dense_fp64": {"workload": "plain dense BayesR, N=2,000 x M=5,000, p~U(0.05,0.5), 100 causal, h2=0.5",
-                          "value": c1["rate"], "ms_per_step": c1["ms_per_step"], "unit": "marker-updates/s"},
+                          "value": c1["rate"], "ms_per_step": c1["ms_per_step"], "unit": "marker-updates/s",
+                          "fp32c_gram_blocked": {"value": c1c["rate"], "ms_per_step": c1c["ms_per_step"]}},
     }
     if cpu:
         out["cpu_baseline"] = cpu_rate(host_bed, R_N, y, 1, 3)
@@ -579,6 +581,52 @@ def run_matched_chains(lib, gpu, torch, device, c3_iters, c2_iters):
     return out
 
 
+def run_sample_writer(lib, gpu, torch, device, iters):
+    """brr ppbayes on the benchmark workload (N = M = 100,000, two groups,
+    FP32C form) from PLINK files: the mean iteration time with no sample
+    rows, with a row every 5th iteration (thin 5, the C3 chain's setting) and
+    with a row every iteration; a row holds 3M + N + 4 numbers."""
+    import re
+    import tempfile
+    from bayesrrcmd_gb300 import plink
+    from bayesrrcmd_gb300.build import build_cli
+    cli = build_cli()
+    d_bed, y, group = make_problem(lib, gpu, torch, device, 0)
+    payload = d_bed.cpu().numpy().reshape(M_SNP, -1)
+    del d_bed
+    torch.cuda.empty_cache()
+    out = {"workload": WORKLOAD + ", brr --form fp32c from PLINK files", "iterations": iters}
+    with tempfile.TemporaryDirectory(dir=os.environ.get("BRR_SCRATCH")) as td:
+        prefix = Path(td) / "c3"
+        plink.write_plink(prefix, payload, N_IND)
+        plink.write_phen(Path(td) / "c3.phen", y)
+        plink.write_groups(Path(td) / "c3.group", group)
+        del payload
+        for name, burn, thin in (("no_rows", iters, 1), ("thin5", 0, 5), ("thin1", 0, 1)):
+            samples = Path(td) / f"{name}.csv"
+            cmd = [str(cli), "--analysis-type", "ppbayes", "--bfile", str(prefix), "--pheno", str(Path(td) / "c3.phen"),
+                   "--group", str(Path(td) / "c3.group"), "--S", "0.01,0.001,0.0001;0.1,0.01", "--form", "fp32c",
+                   "--chain-length", str(iters), "--burn-in", str(burn), "--thin", str(thin),
+                   "--mcmc-samples", str(samples), "--seed", str(SEED)]
+            t0 = time.perf_counter()
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            wall = time.perf_counter() - t0
+            if r.returncode != 0:
+                raise RuntimeError(f"brr failed: {r.stderr[-2000:]}")
+            it_s = float(re.search(r"mean iteration duration: ([0-9.eE+-]+)s", r.stdout).group(1))
+            sw_s = float(re.search(r"mean flowgraph duration: ([0-9.eE+-]+)s", r.stdout).group(1))
+            rows = max(0, sum(1 for _ in open(samples)) - 1) if samples.exists() else 0
+            out[name] = {"mean_iteration_ms": 1e3 * it_s, "mean_sweep_ms": 1e3 * sw_s, "rows": rows,
+                         "sample_file_bytes": samples.stat().st_size if samples.exists() else 0,
+                         "wall_s": wall}
+            if samples.exists():
+                samples.unlink()
+    base = out["no_rows"]["mean_iteration_ms"]
+    for name in ("thin5", "thin1"):
+        out[name]["overhead_ms_per_iteration"] = out[name]["mean_iteration_ms"] - base
+    return out
+
+
 def numpy_sample(m_sample, seed):
     """A CPU-generated sample of the workload: N individuals, m_sample markers."""
     from bayesrrcmd_gb300 import plink
@@ -638,6 +686,8 @@ def main():
     ap.add_argument("--uneven-only", action="store_true", help="only the uneven-batch leg; --uneven-scale shrinks it")
     ap.add_argument("--uneven-scale", type=float, default=1.0)
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged (C2) and C1 measurements")
+    ap.add_argument("--sample-writer", action="store_true",
+                    help="only the sample-file measurement: brr at the benchmark workload with and without rows")
     ap.add_argument("--matched-chains", action="store_true",
                     help="only the whole-chain comparisons of the chosen forms with the plain FP64 chain (C3: "
                          "1,000 iterations, burn-in 200; C2: 2,000 iterations, burn-in 500, thin 5)")
@@ -679,6 +729,11 @@ def main():
     lib = gpu.load_library()
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
+    if args.sample_writer:
+        sw = run_sample_writer(lib, gpu, torch, device, int(os.environ.get("BRR_SW_ITERS", "60")))
+        if rank == 0:
+            print(json.dumps({"sample_writer": sw}))
+        return
     if args.matched_chains:
         mc = run_matched_chains(lib, gpu, torch, device, int(os.environ.get("BRR_C3_ITERS", "1000")),
                                 int(os.environ.get("BRR_C2_ITERS", "2000")))

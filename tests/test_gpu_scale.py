@@ -12,7 +12,9 @@ absolute, sigmaG 1e-9).
 C4 size: 64 batched chains on N = 50,000 x M = 200,000 shared genotypes,
 p ~ U(0.01, 0.5), each chain its own phenotype (h2 ~ U(0.1, 0.7), 1,000 causal
 markers); chains 0, 31 and 63 against their oracle chains for two
-iterations, at the batched form's bars (those of test_gpu_batch.py).
+iterations, at the batched form's bars for this size (c4_compare: the
+fixed-point rounding of 40,000 updates per sweep gives betas an absolute
+error of a few 1e-13).
 
 The oracle keeps dense markers as four standardised values per marker and
 reads the codes from the BED payload (the columns would take 8 GB and 80 GB);
@@ -101,9 +103,38 @@ def test_c3_size_plain_and_blocked_chains_match_oracle(gpu_lib):
     blocked.close()
 
 
+def c4_compare(s, o, what):
+    """Bars of the batched form at C4 size.  The residual is fixed point
+    eps * 2^40 and every update coefficient is rounded to that grid, so each
+    update leaves an error of up to 2^-41 per individual, coherent over the
+    changed marker's genotype pattern; over the ~40,000 updates of a sweep at
+    M = 200,000 the dot products move by up to ~2e-8, so betas carry an
+    absolute error of a few 1e-13 (relative 1e-7 on the smallest non-zero
+    betas, within the 1e-6 posterior-mean target).  Components identical,
+    beta within 1e-9 relative or 1e-12 absolute, residual within 1e-9
+    absolute, sigmaE and sigmaG within 1e-9 relative, acum within 2e-6
+    relative (FP32 exponentials), mu within 1e-10 absolute."""
+    np.testing.assert_array_equal(s["comp"], o["comp"], err_msg=what)
+    nz = o["beta"] != 0
+    np.testing.assert_array_equal(s["beta"] != 0, nz, err_msg=what)
+    d = {
+        "beta": np.abs(s["beta"][nz] - o["beta"][nz]) - 1e-9 * np.abs(o["beta"][nz]) - 1e-12,
+        "eps": np.abs(s["eps"] - o["eps"]) - 1e-9,
+        "sigmaE": np.abs(s["sigmaE"] / o["sigmaE"] - 1) - 1e-9,
+        "sigmaG": np.abs(np.asarray(s["sigmaG"]) / np.asarray(o["sigmaG"]) - 1) - 1e-9,
+        "acum": np.abs(s["acum"] - o["acum"]) - 2e-6 * np.abs(o["acum"]) - 1e-12,
+        "mu": np.abs(s["mu"] - o["mu"]) - 1e-10,
+    }
+    seen = {"beta_abs": float(np.abs(s["beta"][nz] - o["beta"][nz]).max()),
+            "eps_abs": float(np.abs(s["eps"] - o["eps"]).max()),
+            "sigmaE_rel": float(abs(s["sigmaE"] / o["sigmaE"] - 1)),
+            "acum_abs": float(np.abs(s["acum"] - o["acum"]).max()), "mu_abs": float(abs(s["mu"] - o["mu"]))}
+    bad = [k for k, v in d.items() if np.max(v) > 0]
+    assert not bad, f"{what}: {bad} beyond the bars; observed {seen}"
+
+
 def test_c4_size_batched_chains_match_oracle(gpu_lib):
     import torch
-    from test_gpu_batch import compare
     N, M, C = 50_000, 200_000, 64
     seed = 404
     d_bed = device_bed(torch, N, M, seed, 0.01, 0.5)
@@ -126,5 +157,5 @@ def test_c4_size_batched_chains_match_oracle(gpu_lib):
             for c, oc in ocs.items():
                 o = oc.state()
                 assert (o["beta"] != 0).sum() > 100
-                compare(bt.state(c), o, f"iteration {it} chain {c}")
+                c4_compare(bt.state(c), o, f"iteration {it} chain {c}")
     bt.close()
