@@ -171,6 +171,7 @@ void free_all(brr_ctx *c)
     cudaFree(c->d_err);
     cudaFree(c->d_rounds);
     cudaFree(c->d_prof);
+    cudaFree(c->d_tline);
     cudaFree(c->d_nzj);
     cudaFree(c->d_nzb);
     cudaFree(c->d_gram);
@@ -440,6 +441,7 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     a.err = c->d_err;
     a.rounds_out = c->d_rounds;
     a.prof = c->profile ? c->d_prof : nullptr;
+    a.tline = c->profile && c->timeline ? c->d_tline : nullptr;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
     a.gram = c->d_gram;
@@ -1352,9 +1354,39 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
 
 int brr_set_profiling(brr_ctx *ctx, int32_t on)
 {
-    if (!ctx || (on != 0 && on != 1))
-        return fail(BRR_ERR_ARG, "profiling is 0 or 1");
+    if (!ctx || on < 0 || on > 2)
+        return fail(BRR_ERR_ARG, "profiling is 0, 1 or 2");
+    if (on == 2 && !ctx->d_tline) {
+        BRR_CUDA(cudaSetDevice(ctx->dev));
+        const size_t n = (size_t)kTimelineIters * (size_t)ctx->sms * kTimelineEvents;
+        if (cudaMalloc((void **)&ctx->d_tline, sizeof(unsigned long long) * n) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->d_tline = nullptr;
+            return fail(BRR_ERR_OOM, "device allocation failed");
+        }
+        BRR_CUDA(cudaMemset(ctx->d_tline, 0, sizeof(unsigned long long) * n));
+    }
     ctx->profile = on != 0;
+    ctx->timeline = on == 2;
+    return BRR_OK;
+}
+
+int brr_get_sweep_timeline(brr_ctx *ctx, uint64_t *events, int64_t capacity, int32_t *iterations, int32_t *ctas)
+{
+    if (!ctx || !events || !iterations || !ctas)
+        return fail(BRR_ERR_ARG, "null argument");
+    if (!ctx->d_tline)
+        return fail(BRR_ERR_ARG, "the timeline is recorded with brr_set_profiling(ctx, 2)");
+    const int64_t n = (int64_t)kTimelineIters * ctx->G * kTimelineEvents;
+    if (capacity < n)
+        return fail(BRR_ERR_ARG, "the timeline needs " + std::to_string(n) + " values");
+    if (ctx->G > ctx->sms)
+        return fail(BRR_ERR_ARG, "more CTAs than the timeline holds");
+    BRR_CUDA(cudaSetDevice(ctx->dev));
+    BRR_CUDA(cudaStreamSynchronize(ctx->st));
+    BRR_CUDA(cudaMemcpy(events, ctx->d_tline, sizeof(uint64_t) * (size_t)n, cudaMemcpyDeviceToHost));
+    *iterations = kTimelineIters;
+    *ctas = ctx->G;
     return BRR_OK;
 }
 

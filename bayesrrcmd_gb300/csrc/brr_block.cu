@@ -913,6 +913,13 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     unsigned long long *fb_counter = PROF ? reinterpret_cast<unsigned long long *>(a.prof + 8) : nullptr;
     long long steps = 0;
     const bool prof_h = PROF && sidx == 0 && tid == kInputWarp * 32;
+    // event timeline (counting variant): kTimelineIters iterations around the
+    // middle of the sweep, every CTA
+    const int tl_r0 = nblk / 2 > kTimelineIters / 2 ? nblk / 2 - kTimelineIters / 2 : 0;
+    auto stamp = [&](int r, int e) {
+        if (PROF && a.tline && r >= tl_r0 && r < tl_r0 + kTimelineIters)
+            a.tline[((size_t)(r - tl_r0) * (size_t)a.G + (size_t)sidx) * kTimelineEvents + e] = global_timer_ns();
+    };
     int cp_issued = -1, cp_waited = -1;   // resolve warp: Gram copies issued / waited for
 
     // ---- rank-U residual update of block q (dot warps, run at the start of the
@@ -1037,6 +1044,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         if (!ok && lane == 0)
             s_abort = 1;
         __syncwarp();
+        if (lane == 0)
+            stamp(q - 1, 2);
         const long long t1 = prof ? clk() : 0;
         if (!ok)
             return;
@@ -1168,6 +1177,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             const bool ok = role_wait(&s_mb[r & 1], (unsigned)((r >> 1) & 1));
             if (__any_sync(0xffffffffu, !ok || *(volatile int *)&s_abort != 0))
                 break;
+            if (lane == 0)
+                stamp(r, 6);
             if (prof_e)
                 t_it = clk();
             const unsigned q0 = (unsigned)r * Bu;
@@ -1364,12 +1375,17 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                     }
                     if (lane == 0)
                         s_nupd[par] = nupd;
-                    // the block's decisions for the CTA that writes them out
-                    if (sidx == r % a.G) {
+                    // the decisions of the markers whose outputs this CTA writes
+                    // (sweep position p by CTA p mod G)
+                    {
                         BlockOut &o = s_out[r & 1];
 #pragma unroll
                         for (int h = 0; h < 2; ++h) {
                             const int m = lane + 32 * h;
+                            if ((q0 + (unsigned)m) % (unsigned)a.G != (unsigned)sidx) {
+                                o.code[m] = -2;
+                                continue;
+                            }
                             float xh = nh[h], xl = nl[h];
                             df_add(xh, xl, ch[h], cl[h]);
                             o.x[m] = make_float2(xh, xl);
@@ -1391,6 +1407,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             if (prof_e)
                 t_end += clk() - t_it;
             __syncwarp();
+            if (lane == 0)
+                stamp(r, 7);
             mbar_arrive(&s_mb[2 + (r & 1)]);   // RESOLVED(r)
         }
     } else {
@@ -1402,6 +1420,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             const bool ok = r == 0 || role_wait(&s_mb[2 + ((r - 1) & 1)], (unsigned)(((r - 1) >> 1) & 1));
             if (others_any(!ok || *(volatile int *)&s_abort != 0))
                 break;
+            if (tid == 0)
+                stamp(r, 0);
             if (prof_e)
                 t_it = clk();
             mark(prof_d, 0);
@@ -1434,20 +1454,28 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 }
                 if (r + 3 < nblk)
                     gather_store(r + 3);
-                if (sidx == 0 && r + 4 < nblk)
-                    for (int i = lane; i < kAccBufWords; i += 32)
+                // block r+4's accumulators, zeroed in shares of 32 words by the
+                // first CTAs
+                if (r + 4 < nblk)
+                    for (int i = sidx * 32 + lane; i < kAccBufWords; i += 32 * a.G)
                         a.acc[(size_t)((r + 4) % kAccBufs) * kAccBufWords + i] = 0ull;
                 __syncwarp();
                 chore_signal();
+                if (lane == 0)
+                    stamp(r, 4);
                 if (r + 4 < nblk)
                     gather_load(r + 4);
-                if (r >= 1 && sidx == (r - 1) % a.G)
+                if (r >= 1)
                     write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
+                if (lane == 0)
+                    stamp(r, 5);
                 mbar_arrive(&s_mb[(r + 1) & 1]);   // GO(r+1): block r-1's outputs read
             } else if (warp == kInputWarp) {
                 // ---- input warp: block r+1's inputs
                 if (r + 1 < nblk)
                     prepare_inputs(r + 1, prof_h);
+                if (lane == 0)
+                    stamp(r, 3);
                 mbar_arrive(&s_mb[(r + 1) & 1]);   // GO(r+1): block r+1's inputs
             } else if (dw >= 0) {
                 // ---- dot side: update of block r-1, the code slices of block r+3
@@ -1465,6 +1493,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 arrive_sync();
                 if (tid == 0 && r + 2 < nblk)
                     arrive(r + 2);
+                if (tid == 0)
+                    stamp(r, 1);
                 mark(prof_d, 1);
             }
             if (prof_e)
@@ -1478,7 +1508,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     if (!s_abort && r == nblk) {
         if (dw >= 0)
             apply_update(nblk - 1);
-        else if (warp == kChoreWarp && sidx == (nblk - 1) % a.G)
+        else if (warp == kChoreWarp)
             write_block_outputs<KM>(a, s_out[(nblk - 1) & 1], gcf, s_gk, gbf, lane);
     }
     if (prof_d) {

@@ -88,6 +88,8 @@ struct brr_ctx {
     int64_t last_rounds = 0;
     long long phase[16] = {};   // summed over the sweeps of the last call
     bool profile = false;       // phase counters on (brr_set_profiling)
+    bool timeline = false;      // and the per-CTA event timeline of the blocked sweep
+    unsigned long long *d_tline = nullptr;
     uint64_t wait_limit_ns = 2000000000ull;
     int phantom = 0;
 

@@ -93,7 +93,16 @@ struct SweepArgs {
     int eigen;                   // ragged sweep: Eigen sparse markers (missing genotypes enter
                                  // the dot product at the marker's mean)
     unsigned long long *t_out;   // optional [2]: global timer (ns) at the start and end of the sweep (CTA 0)
+    unsigned long long *tline;   // blocked sweep, counting variant, optional: per-CTA event timeline
+                                 // [kTimelineIters][G][kTimelineEvents] of global-timer stamps (ns)
 };
+// Event timeline of the counting variant of the blocked sweep: iterations
+// nblk/2 - 32 .. nblk/2 + 31 (or all, fewer blocks), per CTA: 0 the others'
+// iteration start, 1 the dot warps' grid-barrier arrival, 2 the input warp
+// past the barrier, 3 the input warp's GO signal, 4 the chore warp's signal to
+// the dot warps, 5 the chore warp's GO signal, 6 the resolve's start, 7 its end.
+constexpr int kTimelineIters = 64;
+constexpr int kTimelineEvents = 8;
 
 // ---------------------------------------------------------------------------
 // Batched chains on shared genotypes (brr_batch.cu).

@@ -70,6 +70,7 @@ EXPORTS = [
     "brr_multi_create", "brr_multi_destroy", "brr_multi_pack_bed", "brr_multi_pack_bed_device",
     "brr_multi_set_groups", "brr_multi_set_phenotype", "brr_multi_init", "brr_multi_tune", "brr_multi_iterate",
     "brr_multi_get_state", "brr_multi_get_timing", "brr_synth_bed_device_beta", "brr_multi_set_wait_limit",
+    "brr_get_sweep_timeline",
 ]
 
 
@@ -104,6 +105,8 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_get_phase_cycles.argtypes = [P, C.POINTER(C.c_int64)]
     lib.brr_set_wait_limit.argtypes = [P, C.c_uint64, C.c_int32]
     lib.brr_set_profiling.argtypes = [P, C.c_int32]
+    lib.brr_get_sweep_timeline.argtypes = [P, C.POINTER(C.c_uint64), C.c_int64, C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_int32)]
     lib.brr_get_gram_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
@@ -335,9 +338,19 @@ class Chain:
     def set_wait_limit(self, timeout_ns: int, phantom_arrivals: int = 0):
         self._check(self.lib.brr_set_wait_limit(self.h, int(timeout_ns), int(phantom_arrivals)))
 
-    def set_profiling(self, on: bool):
-        """Phase counters (phase_cycles) on or off; timed runs keep them off."""
-        self._check(self.lib.brr_set_profiling(self.h, 1 if on else 0))
+    def set_profiling(self, on):
+        """Phase counters (phase_cycles) on or off; 2 adds the blocked sweep's
+        per-CTA event timeline (timeline()); timed runs keep them off."""
+        self._check(self.lib.brr_set_profiling(self.h, int(on) if not isinstance(on, bool) else (1 if on else 0)))
+
+    def timeline(self) -> np.ndarray:
+        """Events [iteration, cta, event] (global timer, ns) of the last sweep
+        run with profiling 2."""
+        n = 64 * 152 * 8 * 2
+        buf = np.zeros(n, np.uint64)
+        it, ctas = C.c_int32(), C.c_int32()
+        self._check(self.lib.brr_get_sweep_timeline(self.h, _ptr(buf, C.c_uint64), n, C.byref(it), C.byref(ctas)))
+        return buf[:it.value * ctas.value * 8].reshape(it.value, ctas.value, 8).copy()
 
     def gram_info(self):
         b, ms, n = C.c_int32(), C.c_double(), C.c_int64()

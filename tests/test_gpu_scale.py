@@ -113,7 +113,9 @@ def c4_compare(s, o, what):
     betas, within the 1e-6 posterior-mean target).  Components identical,
     beta within 1e-9 relative or 1e-12 absolute, residual within 1e-9
     absolute, sigmaE and sigmaG within 1e-9 relative, acum within 2e-6
-    relative (FP32 exponentials), mu within 1e-10 absolute."""
+    relative (FP32 exponentials), mu within 1e-9 absolute (the constant part
+    of every update is rounded once and moves the residual mean coherently by
+    up to 2^-41: about 1e-10 after the sweeps' 40,000 updates)."""
     np.testing.assert_array_equal(s["comp"], o["comp"], err_msg=what)
     nz = o["beta"] != 0
     np.testing.assert_array_equal(s["beta"] != 0, nz, err_msg=what)
@@ -123,7 +125,7 @@ def c4_compare(s, o, what):
         "sigmaE": np.abs(s["sigmaE"] / o["sigmaE"] - 1) - 1e-9,
         "sigmaG": np.abs(np.asarray(s["sigmaG"]) / np.asarray(o["sigmaG"]) - 1) - 1e-9,
         "acum": np.abs(s["acum"] - o["acum"]) - 2e-6 * np.abs(o["acum"]) - 1e-12,
-        "mu": np.abs(s["mu"] - o["mu"]) - 1e-10,
+        "mu": np.abs(s["mu"] - o["mu"]) - 1e-9,
     }
     seen = {"beta_abs": float(np.abs(s["beta"][nz] - o["beta"][nz]).max()),
             "eps_abs": float(np.abs(s["eps"] - o["eps"]).max()),
