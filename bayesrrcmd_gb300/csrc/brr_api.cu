@@ -441,7 +441,8 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     a.err = c->d_err;
     a.rounds_out = c->d_rounds;
     a.prof = c->profile ? c->d_prof : nullptr;
-    a.tline = c->profile && c->timeline ? c->d_tline : nullptr;
+    // the timeline holds one row per SM: a sweep on more CTAs records none
+    a.tline = c->profile && c->timeline && c->G <= c->sms ? c->d_tline : nullptr;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
     a.gram = c->d_gram;

@@ -1018,6 +1018,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 }
             }
         }
+        if (lane == 0)
+            stamp(q - 1, 10);
         const long long t0 = prof ? clk() : 0;
         bool ok = true;
         if (lane < kCounters) {
@@ -1261,10 +1263,16 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                             const float delta = fabsf(sx[h] - sref[h]) * 1.000001f + 4e-7f * (sx[h] + sref[h]);
                             need[h] = own[h] && lane + 32 * h >= next && !(hg[h] * delta <= wmar[h]);
                         }
-                        if (__any_sync(0xffffffffu, need[0] || need[1])) {
+                        const unsigned need_halves = (__ballot_sync(0xffffffffu, need[0]) ? 1u : 0u) |
+                                                     (__ballot_sync(0xffffffffu, need[1]) ? 2u : 0u);
+                        if (need_halves) {
                             bool slow[2];
 #pragma unroll
                             for (int h = 0; h < 2; ++h) {
+                                slow[h] = false;
+                                // a half none of whose markers needs a new decision is skipped
+                                if (!(need_halves & (1u << h)))
+                                    continue;
                                 int c;
                                 float w;
                                 const bool okm =
@@ -1465,6 +1473,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                     stamp(r, 4);
                 if (r + 4 < nblk)
                     gather_load(r + 4);
+                if (lane == 0)
+                    stamp(r, 11);
                 if (r >= 1)
                     write_block_outputs<KM>(a, s_out[(r - 1) & 1], gcf, s_gk, gbf, lane);
                 if (lane == 0)
@@ -1485,11 +1495,15 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 if (r >= 1)
                     apply_update(r - 1);
                 mbar_arrive(&s_mb[(r + 1) & 1]);   // GO(r+1): block r-1's decisions applied
+                if (tid == 0)
+                    stamp(r, 8);
                 mark(prof_d, 4);
                 issue_block_codes(r + 3, false);
                 cp_async_commit();
                 if (r + 2 < nblk)
                     dot_block(r + 2);
+                if (tid == 0)
+                    stamp(r, 9);
                 arrive_sync();
                 if (tid == 0 && r + 2 < nblk)
                     arrive(r + 2);

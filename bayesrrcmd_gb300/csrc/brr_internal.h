@@ -100,9 +100,11 @@ struct SweepArgs {
 // nblk/2 - 32 .. nblk/2 + 31 (or all, fewer blocks), per CTA: 0 the others'
 // iteration start, 1 the dot warps' grid-barrier arrival, 2 the input warp
 // past the barrier, 3 the input warp's GO signal, 4 the chore warp's signal to
-// the dot warps, 5 the chore warp's GO signal, 6 the resolve's start, 7 its end.
+// the dot warps, 5 the chore warp's GO signal, 6 the resolve's start, 7 its end,
+// 8 the dot warps' residual update done, 9 their dot products done, 10 the
+// input warp's far corrections done, 11 the chore warp's Gram loads issued.
 constexpr int kTimelineIters = 64;
-constexpr int kTimelineEvents = 8;
+constexpr int kTimelineEvents = 12;
 
 // ---------------------------------------------------------------------------
 // Batched chains on shared genotypes (brr_batch.cu).

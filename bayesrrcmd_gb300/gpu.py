@@ -346,11 +346,12 @@ class Chain:
     def timeline(self) -> np.ndarray:
         """Events [iteration, cta, event] (global timer, ns) of the last sweep
         run with profiling 2."""
-        n = 64 * 152 * 8 * 2
+        ev = 12
+        n = 64 * 152 * ev * 2
         buf = np.zeros(n, np.uint64)
         it, ctas = C.c_int32(), C.c_int32()
         self._check(self.lib.brr_get_sweep_timeline(self.h, _ptr(buf, C.c_uint64), n, C.byref(it), C.byref(ctas)))
-        return buf[:it.value * ctas.value * 8].reshape(it.value, ctas.value, 8).copy()
+        return buf[:it.value * ctas.value * ev].reshape(it.value, ctas.value, ev).copy()
 
     def gram_info(self):
         b, ms, n = C.c_int32(), C.c_double(), C.c_int64()
