@@ -449,6 +449,7 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     a.gstage = c->d_gstage;
     a.has_missing = c->has_missing ? 1 : 0;
     a.brec = c->d_brec;
+    a.order = c->d_order;
     a.beta_df = c->d_bdf;
     a.acum_df = c->d_bdf ? c->d_bdf + cf.M : nullptr;
     smem = c->blocked ? sweep_block_smem_bytes(a) : sweep_smem_bytes(cf.form, c->kind, a);

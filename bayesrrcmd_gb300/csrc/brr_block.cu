@@ -94,6 +94,7 @@
 #include "brr_internal.h"
 #include "brr_pick.cuh"
 
+
 namespace brr {
 
 namespace {
@@ -119,6 +120,7 @@ constexpr int kAccBufWords = kAccCopies * kMaxSpec * 4;
 constexpr int kCounters = 8;
 constexpr int kCounterStride = 16;
 constexpr int kStageSlots = 8;
+constexpr int kIdSlots = 8;
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
@@ -564,6 +566,10 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     __shared__ uint32_t s_glut[256];         // code byte -> 4 genotype bytes (code 0: 2, 2: 1, 1 and 3: 0)
     __shared__ uint32_t s_mlut[256];         // code byte -> 4 missing-indicator bytes (code 1)
     __shared__ long long s_D[kMaxSpec][4];   // residual change per update and code, fixed point
+    // marker ids of blocks q (slot q % kIdSlots), copied from the sweep order
+    // one iteration before they are read: blocks r+1 .. r+4 are resident in
+    // iteration r while block r+5's ids are in flight
+    __shared__ __align__(16) uint32_t s_ids[kIdSlots][kMaxSpec];
     __shared__ int s_abort;
     __shared__ int s_cp_issued;
     // resolve warp <-> other warps: GO(q) on s_mb[q & 1] (320 arrivals: the dot
@@ -696,42 +702,36 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
         rec_issued = upto;
     };
     // Code slices of a block, copied by the dot warps: thread t copies chunk
-    // my_c of the block's markers my_q, my_q + per_pass, ...  In the steady
-    // state the marker ids come from the records in global memory, loaded at
-    // the top of the iteration (the block's records are still in flight).
+    // my_c of the block's markers my_q, my_q + per_pass, ...; the marker ids come
+    // from the id ring in shared memory.
     const unsigned chunks = (unsigned)nbytes / 16u;
     const unsigned per_pass = chunks ? (unsigned)(kDotWarps * 32) / chunks : 0u;
     const unsigned my_q = chunks ? (unsigned)dtid / chunks : 0u;
     const unsigned my_c = chunks ? (unsigned)dtid - my_q * chunks : 0u;
-    constexpr int kCodePasses = 4;
-    uint32_t jpre[kCodePasses] = {0u, 0u, 0u, 0u};
-    auto prefetch_code_ids = [&](int q) {
-        if (q >= nblk || dw < 0 || my_q >= per_pass)
+    // ids of block q into its ring slot (threads idx, idx + stride, ...): 16-byte
+    // copies of four ids, 4-byte copies for a partial last group
+    auto issue_ids = [&](int q, int idx, int stride) {
+        if (q >= nblk)
             return;
         const unsigned qb = (unsigned)q * Bu, nbq = (unsigned)nb_of(q);
-#pragma unroll
-        for (int k = 0; k < kCodePasses; ++k) {
-            const unsigned m = my_q + (unsigned)k * per_pass;
-            if (m < nbq)
-                jpre[k] = __ldg(&a.brec[qb + m].j);
+        uint32_t *dst = s_ids[q % kIdSlots];
+        for (unsigned g = (unsigned)idx; 4u * g < nbq; g += (unsigned)stride) {
+            if (4u * g + 4u <= nbq) {
+                cp_async16(dst + 4u * g, a.order + qb + 4u * g);
+            } else {
+                for (unsigned m = 4u * g; m < nbq; ++m)
+                    cp_async4(dst + m, a.order + qb + m);
+            }
         }
     };
-    auto issue_block_codes = [&](int q, bool from_ring) {
+    auto issue_block_codes = [&](int q) {
         if (q >= nblk || dw < 0 || my_q >= per_pass)
             return;
         const unsigned qb = (unsigned)q * Bu, nbq = (unsigned)nb_of(q);
-        auto copy = [&](unsigned m, uint32_t j) {
+        const uint32_t *ids = s_ids[q % kIdSlots];
+        for (unsigned m = my_q; m < nbq; m += per_pass)
             cp_async16(ring_codes + ((qb + m) & Rm) * a.slot_bytes + 16 * my_c,
-                       a.codes + (int64_t)j * a.col_stride + byte_lo + 16 * my_c);
-        };
-#pragma unroll
-        for (int k = 0; k < kCodePasses; ++k) {
-            const unsigned m = my_q + (unsigned)k * per_pass;
-            if (m < nbq)
-                copy(m, from_ring ? ring_rec[(qb + m) & Rm].j : jpre[k]);
-        }
-        for (unsigned m = my_q + kCodePasses * per_pass; m < nbq; m += per_pass)
-            copy(m, from_ring ? ring_rec[(qb + m) & Rm].j : __ldg(&a.brec[qb + m].j));
+                       a.codes + (int64_t)ids[m] * a.col_stride + byte_lo + 16 * my_c);
     };
 
     // ---- Gram entries of block q (chore warp): CTA s gathers entries
@@ -766,7 +766,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 return false;
             qa = q0 - back * Bu + pa;
         }
-        const int64_t ja = __ldg(&a.brec[qa].j), jb = __ldg(&a.brec[q0 + pb].j);
+        const int64_t ja = s_ids[(qa / Bu) % kIdSlots][qa % Bu], jb = s_ids[q % kIdSlots][pb];
         const int64_t hi = ja > jb ? ja : jb, lw = ja > jb ? jb : ja;
         *out = __ldg(&a.gram[hi * (hi - 1) / 2 + lw]);
         return true;
@@ -1106,11 +1106,13 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     // of blocks 0..2 staged and blocks 0 and 1's dot products published before
     // the arrivals at barriers 0 and 1; block 0's inputs assembled
     issue_recs(4u * Bu, tid, kBlockThreads);
+    for (int q = 0; q < 5; ++q)
+        issue_ids(q, tid, kBlockThreads);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
     for (int q = 0; q < 3; ++q)
-        issue_block_codes(q, true);
+        issue_block_codes(q);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
@@ -1434,6 +1436,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 t_it = clk();
             mark(prof_d, 0);
             issue_recs((unsigned)(r + 4) * Bu, otid, kOtherThreads);
+            issue_ids(r + 5, otid, kOtherThreads);
             cp_async_commit();
 
             if (warp == kChoreWarp) {
@@ -1491,14 +1494,13 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 // ---- dot side: update of block r-1, the code slices of block r+3
                 // into the slot block r-1 held, dots of block r+2 and their
                 // publication
-                prefetch_code_ids(r + 3);
                 if (r >= 1)
                     apply_update(r - 1);
                 mbar_arrive(&s_mb[(r + 1) & 1]);   // GO(r+1): block r-1's decisions applied
                 if (tid == 0)
                     stamp(r, 8);
                 mark(prof_d, 4);
-                issue_block_codes(r + 3, false);
+                issue_block_codes(r + 3);
                 cp_async_commit();
                 if (r + 2 < nblk)
                     dot_block(r + 2);

@@ -88,6 +88,7 @@ struct SweepArgs {
     double *gstage;              // blocked FP32C sweep: staged Gram entries (sweep_block_stage_bytes)
     int has_missing;             // any missing genotype in the packed markers
     const BlockRec *brec;        // blocked FP32C sweep: M records in sweep order
+    const uint32_t *order;       // blocked FP32C sweep: the M marker ids in sweep order
     float2 *beta_df;             // blocked FP32C sweep: new beta per marker (hi, lo)
     float2 *acum_df;             // blocked FP32C sweep: acum per marker (hi, lo)
     int eigen;                   // ragged sweep: Eigen sparse markers (missing genotypes enter
