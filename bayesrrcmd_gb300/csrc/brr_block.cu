@@ -943,7 +943,11 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 atomicCAS(a.err, kDevOk, kDevRange);
             s_D[u][code] = D;
         }
+        if (tid == 0)
+            stamp(q + 1, 12);
         dot_warps_sync();
+        if (tid == 0)
+            stamp(q + 1, 13);
         // The sum of the residual is left as it was at the sweep start: the
         // standardised columns sum to zero, so a dense update moves it only
         // by rounding (dBeta times a column sum of order 1e-11).
@@ -971,7 +975,11 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             reinterpret_cast<longlong2 *>(fix)[2 * b + 1] = make_longlong2(E[2], E[3]);
             store_fix4(planes, b, E);
         }
+        if (tid == 0)
+            stamp(q + 1, 14);
         dot_warps_sync();
+        if (tid == 0)
+            stamp(q + 1, 15);
     };
 
     constexpr int kCopyThread = kChoreWarp * 32; // issues the Gram bulk copies

@@ -103,9 +103,11 @@ struct SweepArgs {
 // past the barrier, 3 the input warp's GO signal, 4 the chore warp's signal to
 // the dot warps, 5 the chore warp's GO signal, 6 the resolve's start, 7 its end,
 // 8 the dot warps' residual update done, 9 their dot products done, 10 the
-// input warp's far corrections done, 11 the chore warp's Gram loads issued.
+// input warp's far corrections done, 11 the chore warp's Gram loads issued,
+// 12-15 inside the residual update: the update terms computed, the dot warps
+// synchronised, the residual slice updated, synchronised again.
 constexpr int kTimelineIters = 64;
-constexpr int kTimelineEvents = 12;
+constexpr int kTimelineEvents = 16;
 
 // ---------------------------------------------------------------------------
 // Batched chains on shared genotypes (brr_batch.cu).

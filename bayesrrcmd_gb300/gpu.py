@@ -346,7 +346,7 @@ class Chain:
     def timeline(self) -> np.ndarray:
         """Events [iteration, cta, event] (global timer, ns) of the last sweep
         run with profiling 2."""
-        ev = 12
+        ev = 16
         n = 64 * 152 * ev * 2
         buf = np.zeros(n, np.uint64)
         it, ctas = C.c_int32(), C.c_int32()

@@ -324,14 +324,15 @@ int brr_get_phase_cycles(brr_ctx *ctx, int64_t *cycles);
 int brr_set_profiling(brr_ctx *ctx, int32_t on);
 /* on = 2: the counters of on = 1 and, in the Gram-blocked sweep, a per-CTA
  * event timeline of 64 iterations around the sweep's middle (global timer,
- * ns): events[(it * ctas + cta) * 12 + e] for e = 0 the iteration's start on
+ * ns): events[(it * ctas + cta) * 16 + e] for e = 0 the iteration's start on
  * the warps other than the sampling warp, 1 the grid-barrier arrival of the
  * dot products, 2 the input warp past the barrier, 3 the next block's inputs
  * ready, 4 the Gram warp's staging done, 5 the Gram warp's work done, 6 and 7
  * the start and end of the block's sampling, 8 the residual update done, 9 the
- * dot products done, 10 the far corrections done, 11 the Gram loads issued.
- * capacity: values available (64 x ctas x 12).  Diagnostics of the pipeline's
- * critical path. */
+ * dot products done, 10 the far corrections done, 11 the Gram loads issued,
+ * 12-15 the residual update's terms computed, first barrier, slice updated,
+ * second barrier.  capacity: values available (64 x ctas x 16).  Diagnostics
+ * of the pipeline's critical path. */
 int brr_get_sweep_timeline(brr_ctx *ctx, uint64_t *events, int64_t capacity, int32_t *iterations, int32_t *ctas);
 
 #ifdef __cplusplus
