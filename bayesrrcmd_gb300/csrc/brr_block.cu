@@ -95,6 +95,7 @@
 #include "brr_pick.cuh"
 
 
+
 namespace brr {
 
 namespace {
@@ -1456,21 +1457,23 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 // the zeroed accumulators of block r+4, signalled to the dot warps
                 // before their arrival at barrier r+2; then the Gram loads of
                 // block r+4 and the outputs of block r-1
-                if (lane == 0) {
-                    fence_proxy_async();
-                    if (r == 0) {
-                        mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
-                        bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
-                        cp_issued = 0;
-                    }
-                    if (r + 1 < nblk) {
+                auto issue_bulk_next = [&]() {
+                    if (lane == 0 && r + 1 < nblk) {
                         const int q = r + 1;
+                        fence_proxy_async();
                         mbar_expect_tx(&mbar[q & 1], (unsigned)(gent * sizeof(float2)));
                         bulk_copy_g2s(gbuf + (size_t)(q & 1) * gent, gstage + (size_t)(q % kStageSlots) * gst,
                                       (unsigned)(gent * sizeof(float2)), &mbar[q & 1]);
                         cp_issued = q;
                     }
+                };
+                if (lane == 0 && r == 0) {
+                    fence_proxy_async();
+                    mbar_expect_tx(&mbar[0], (unsigned)(gent * sizeof(float2)));
+                    bulk_copy_g2s(gbuf, gstage, (unsigned)(gent * sizeof(float2)), &mbar[0]);
+                    cp_issued = 0;
                 }
+                issue_bulk_next();
                 if (r + 3 < nblk)
                     gather_store(r + 3);
                 // block r+4's accumulators, zeroed in shares of 32 words by the
