@@ -326,16 +326,13 @@ def run_uneven(lib, gpu, torch, device, steps, tune_rounds, scale=1.0):
     S = [[0.01, 0.001, 0.0001]]
     seed = SEED + 11
     N, M, h2 = uneven_instances(seed, scale)
-    # dense or ragged by storage: ragged index lists take 4 bytes per non-zero
-    # genotype, dense columns N/4 bytes; with p ~ Beta(0.5, 2) clipped to
-    # [0.001, 0.5] the expected non-zero fraction E[1 - (1 - p)^2] decides
-    ps = np.clip(np.random.default_rng(seed + 1).beta(0.5, 2.0, 200_000), 0.001, 0.5)
-    nz = float(np.mean(1.0 - (1.0 - ps) ** 2))
-    kinds = [gpu.KIND_RAGGED if 4.0 * nz < 0.25 else gpu.KIND_DENSE for _ in range(len(N))]
-    cfgs = [gpu.ChainConfig(N=int(N[i]), M=int(M[i]), kind=kinds[i], form=gpu.FORM_FP32C, S=S, seed=seed,
-                            chain=i, refresh_every=REFRESH, device=device) for i in range(len(N))]
-    mm = gpu.Multi(cfgs, lib=lib)
+    # each instance's genotypes and phenotype; its kind, dense or ragged, from
+    # its own packed genotype counts: the ragged sweep reads 2 bytes (a
+    # slice-local index) per listed genotype (ones, twos, missing), the dense
+    # sweep N/4 bytes per marker, so ragged storage is chosen when fewer than one
+    # genotype in eight is listed
     rng = np.random.default_rng(seed + 2)
+    beds, ys, kinds, listed = [], [], [], []
     for i in range(len(N)):
         n_i, m_i = int(N[i]), int(M[i])
         d_bed = torch.empty(m_i * ((n_i + 3) // 4), dtype=torch.uint8, device=device)
@@ -345,11 +342,20 @@ def run_uneven(lib, gpu, torch, device, steps, tune_rounds, scale=1.0):
         n_c = max(1, int(0.005 * m_i))
         causal = np.sort(rng.choice(m_i, n_c, replace=False)).astype(np.uint32)
         b = rng.normal(0.0, np.sqrt(h2[i] / n_c), n_c)
-        y = (probe.xbeta(causal, b) + rng.normal(0.0, np.sqrt(1.0 - h2[i]), n_i)).astype(np.float32)
+        ys.append((probe.xbeta(causal, b) + rng.normal(0.0, np.sqrt(1.0 - h2[i]), n_i)).astype(np.float32))
+        _, counts = probe.marker_table()
         probe.close()
-        mm.pack_bed_device(i, d_bed.data_ptr(), d_bed.numel())
-        mm.set_phenotype(i, y)
-        del d_bed
+        frac = float(counts[:, 1:4].sum()) / (float(n_i) * float(m_i))
+        listed.append(frac)
+        kinds.append(gpu.KIND_RAGGED if 2.0 * frac < 0.25 else gpu.KIND_DENSE)
+        beds.append(d_bed)
+    cfgs = [gpu.ChainConfig(N=int(N[i]), M=int(M[i]), kind=kinds[i], form=gpu.FORM_FP32C, S=S, seed=seed,
+                            chain=i, refresh_every=REFRESH, device=device) for i in range(len(N))]
+    mm = gpu.Multi(cfgs, lib=lib)
+    for i in range(len(N)):
+        mm.pack_bed_device(i, beds[i].data_ptr(), beds[i].numel())
+        mm.set_phenotype(i, ys[i])
+    del beds
     torch.cuda.empty_cache()
     mm.init()
     t0 = mm.timing()
@@ -364,7 +370,10 @@ def run_uneven(lib, gpu, torch, device, steps, tune_rounds, scale=1.0):
                 ms_per_step=t["total_ms"] / steps,
                 sweep_ms=t["sweep_ms"] / steps, instances=len(N), total_markers=total_m,
                 total_genotypes=float((N.astype(float) * M.astype(float)).sum()),
-                kinds={"dense": kinds.count(gpu.KIND_DENSE), "ragged": kinds.count(gpu.KIND_RAGGED)},
+                kinds={"dense": kinds.count(gpu.KIND_DENSE), "ragged": kinds.count(gpu.KIND_RAGGED),
+                       "rule": "ragged when fewer than 1 in 8 genotypes are listed (2-byte indices vs N/4 "
+                               "bytes per marker), from each instance's packed counts",
+                       "listed_fraction_min_max": [round(min(listed), 4), round(max(listed), 4)]},
                 ctas_first=t0["ctas"].tolist(), ctas=t["ctas"].tolist(), widths=t["width"].tolist(),
                 inst_ms=[round(x, 3) for x in inst.tolist()],
                 balance_max_over_mean=float(inst.max() / max(inst.mean(), 1e-9)),
