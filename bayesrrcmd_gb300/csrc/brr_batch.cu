@@ -485,17 +485,57 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
             int fcomp = -1;
             long long Wl = 0, Csum = 0;
             const float two40 = (float)(1ll << kBatchFrac);
-            for (;; ++steps) {
-                int comp = -1;
-                float a032 = 0.f;
-                const bool cert = pick_f32<KM>(nh, nl, uf, gcf, K, comp, a032);
-                double fb_beta = bold, fb_acum = 0.0;
-                if (!cert) {
-                    const Pick pk = pick_marker<false, KM>((double)nh + (double)nl, u, z, bold, gc, K);
-                    comp = pk.comp;
-                    fb_acum = pk.acum0;
-                    fb_beta = pk.beta;
+            // certified stability margin of the current decision: while num^2
+            // moves by Delta with H * Delta <= wmar (H: the spread of the
+            // group's h_k, h_0 = 0 included) no cumulative probability crosses
+            // u, so a marker is evaluated again only when a correction moves it
+            // beyond its margin (the decisions are those of an evaluation at the
+            // current num)
+            float H = 0.f;
+            {
+                float hmax = 0.f, hmin = 0.f;
+                for (int k = 1; k < K; ++k) {
+                    hmax = fmaxf(hmax, gcf[2 * k + 1]);
+                    hmin = fminf(hmin, gcf[2 * k + 1]);
                 }
+                H = (hmax - hmin) * 1.000001f;
+            }
+            float sref = 0.f, wmar = -1.f;
+            int comp = -1;
+            bool fbd = false;   // the decision came from the FP64 sampler
+            double fb_beta = bold, fb_acum = 0.0;
+            for (;; ++steps) {
+                const float sx = __fmaf_rn(nh, nh, 2.f * nh * nl);
+                const float delta = fabsf(sx - sref) * 1.000001f + 4e-7f * (sx + sref);
+                const bool need = !done && !(H * delta <= wmar);
+                if (__any_sync(0xffffffffu, need)) {
+                    int cm;
+                    float w;
+                    const bool okm = pick_margin<KM>(sx, uf, gcf, K, cm, w);
+                    if (need) {
+                        comp = cm;
+                        fbd = false;
+                        sref = sx;
+                        wmar = okm ? w : -1.f;
+                    }
+                    const bool slow = need && !okm;
+                    if (__any_sync(0xffffffffu, slow) && slow) {
+                        // 700 guards possibly active or u near a boundary: the
+                        // guarded FP32 sampler, then FP64
+                        int c2;
+                        float a0;
+                        if (pick_f32<KM>(nh, nl, uf, gcf, K, c2, a0)) {
+                            comp = c2;
+                        } else {
+                            const Pick pk = pick_marker<false, KM>((double)nh + (double)nl, u, z, bold, gc, K);
+                            comp = pk.comp;
+                            fb_acum = pk.acum0;
+                            fb_beta = pk.beta;
+                            fbd = true;
+                        }
+                    }
+                }
+                const bool cert = !fbd;
                 const bool chg = !done && (bold != 0.0 || comp > 0);
                 const unsigned mask = __ballot_sync(0xffffffffu, chg);
                 const int p = mask ? __ffs(mask) - 1 : 32;
@@ -518,7 +558,6 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                         }
                     }
                     acum_is_d = !cert;
-                    acum_f = a032;
                     acum_d = fb_acum;
                     done = true;
                 }
@@ -558,6 +597,14 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                     df_add(nh, nl, xh, xl);
                 }
                 sumE += Wp * (long long)Sp - (long long)a.N * Cp;
+            }
+            // acum of an FP32 decision: P(component 0) of the FP32 sampler at
+            // the marker's final num
+            {
+                int c2;
+                float a0;
+                pick_f32<KM>(nh, nl, uf, gcf, K, c2, a0);
+                acum_f = a0;
             }
             if (q < a.M) {
                 const size_t cj = (size_t)c * a.M + rc.j;

@@ -392,69 +392,6 @@ __global__ void k_block_finish(int64_t M, const uint8_t *__restrict__ chosen, co
     }
 }
 
-// Branch-free certified FP32 decision with a stability margin.  With
-// D_k = dc_k + h_k * s (s = num^2, D_0 = 0) the component is the first k with
-// u * sum(e) <= c_k (e_k = exp(D_k - max D), c_k the running sums).  Returns
-// false when the 700 guards of the log-likelihood differences could matter
-// (any difference beyond 600) or when u lies within the certified error tol of
-// a boundary; the caller then takes the guarded or the FP64 path.
-// On success *w is a margin in log-probability: while the true s moves by Delta
-// with H * Delta <= w (H: largest h_k - smallest, h_0 = 0 included), every
-// cumulative probability changes by a factor within exp(+-H * Delta), which
-// cannot carry a boundary across u, so the decision stays the same.
-template <int KM>
-__device__ __forceinline__ bool pick_margin(float s, float uf, const float *__restrict__ gcf, int K, int &comp,
-                                            float &w)
-{
-    float D[KM];
-    float maxerr = 0.f;
-    D[0] = 0.f;
-#pragma unroll
-    for (int k = 1; k < KM; ++k) {
-        const float dc = gcf[2 * k], h = gcf[2 * k + 1];
-        D[k] = k < K ? __fmaf_rn(h, s, dc) : -INFINITY;
-        maxerr = k < K ? fmaxf(maxerr, 3.0e-7f * (fabsf(dc) + fabsf(h * s))) : maxerr;
-    }
-    float dmax = 0.f, dmax1 = D[1], dmin1 = D[1];
-#pragma unroll
-    for (int k = 1; k < KM; ++k) {
-        dmax = fmaxf(dmax, D[k]);
-        dmax1 = fmaxf(dmax1, D[k]);
-        dmin1 = k < K ? fminf(dmin1, D[k]) : dmin1;
-    }
-    const bool far = (dmax1 - dmin1) < 600.f && dmax1 < 600.f && dmin1 > -600.f;
-    float c[KM];
-    float run = 0.f;
-#pragma unroll
-    for (int k = 0; k < KM; ++k) {
-        run = __fadd_rn(run, __expf(D[k] - dmax));   // exp(-inf) = 0 beyond K
-        c[k] = run;
-    }
-    const float es = run;
-    const float target = uf * es;
-    const float tol = (4e-5f + 4.f * maxerr) * es;
-    int chosen = 0;
-    bool close = false;
-    float up = es, lo = 0.f;
-#pragma unroll
-    for (int k = 0; k < KM; ++k) {
-        if (k < K) {
-            const bool below = c[k] < target;
-            chosen += below ? 1 : 0;
-            close = close || fabsf(c[k] - target) < tol;
-            lo = below ? c[k] : lo;
-        }
-    }
-#pragma unroll
-    for (int k = KM - 1; k >= 0; --k)
-        up = (k < K && c[k] >= target) ? c[k] : up;
-    comp = chosen < K ? chosen : -1;
-    const float w1 = __logf(up - tol) - __logf(target);
-    const float w2 = chosen > 0 ? __logf(target) - __logf(lo + tol) : 50.f;
-    w = fminf(fminf(w1, w2) - 1e-5f, 50.f);
-    return far && !close && chosen < K && w > 0.f;
-}
-
 // One halving exchange of a warp's reduce-scatter over double-float sums:
 // lanes of the lower half (upper false) keep entries [0, H), the others
 // [H, 2H), each adding the partner's copy; the kept sums move to [0, H).
