@@ -402,6 +402,37 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
         if (prof)
             ph[1] += clock64() - t0, t0 = clock64();
 
+        // ---- the block's integer Gram (lower triangle), summed over its copies
+        // once per CTA into shared memory for all the CTA's chains (the
+        // genotypes are shared): row t holds P[t][p] for p < t, 33 words apart.
+        // A CTA that resolves chains first waits for every CTA's dot products.
+        const int *sP = s_pbuf;
+        if (s < C) {
+            const long long tw = prof ? clock64() : 0;
+            if (tid == 0 && !counter_wait(cnt1, (unsigned long long)(a.G + a.phantom) * (unsigned long long)(b + 1),
+                                          a.err, a.timeout_ns)) {
+                atomicCAS(a.err, kDevOk, kDevTimeout);
+                s_abort = 1;
+            }
+            __syncthreads();   // orders tid 0's acquire before the loads below
+            if (prof)
+                ph[4] += clock64() - tw;
+            if (!s_abort) {
+                const unsigned *pk_base = a.pacc + (size_t)(b & 1) * kBatchPCopies * (kBatchBlock * kBatchBlock);
+                for (int e = tid; e < kBatchBlock * kBatchBlock; e += kBT) {
+                    const int t = e >> 5, pp = e & 31;
+                    if (pp < t) {
+                        unsigned v = 0;
+#pragma unroll
+                        for (int cp = 0; cp < kBatchPCopies; ++cp)
+                            v += __ldcg(pk_base + (size_t)cp * (kBatchBlock * kBatchBlock) + e);
+                        s_pbuf[t * 33 + pp] = (int)v;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
         // ---- resolve: one warp per chain
         for (int k = warp;; k += kBW) {
             const int c = s + a.G * k;
@@ -421,23 +452,7 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
             const double *gc = a.gconst + ((size_t)c * a.n_groups + grp) * kMaxK * 4;
             const float *gcf = a.gcf + ((size_t)c * a.n_groups + grp) * kMaxK * 2;
             const int K = a.gK[grp];
-            bool ok = true;
-            const long long tw = prof ? clock64() : 0;
-            if (lane == 0)
-                ok = counter_wait(cnt1, (unsigned long long)(a.G + a.phantom) * (unsigned long long)(b + 1), a.err,
-                                  a.timeout_ns);
-            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-            __syncwarp();   // orders lane 0's acquire before the other lanes' loads
-            if (!ok) {
-                if (lane == 0) {
-                    atomicCAS(a.err, kDevOk, kDevTimeout);
-                    s_abort = 1;
-                }
-                break;
-            }
             const long long tl = prof ? clock64() : 0;
-            if (prof && k == 0)
-                ph[4] += tl - tw;
             int steps = 0;
             long long dot = 0;
 #pragma unroll
@@ -446,24 +461,6 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                 dot += (long long)ld_relaxed_u64(p);
                 *p = 0ull;
             }
-            // the block's integer Gram (lower triangle) into this warp's rows:
-            // row t holds P[t][p] for p < t, 33 words apart
-            int *sP = s_pbuf + (warp % pl.nres) * (kBatchBlock * 33);
-            {
-                const unsigned *pk_base = a.pacc + (size_t)(b & 1) * kBatchPCopies * (kBatchBlock * kBatchBlock);
-#pragma unroll 8
-                for (int e = lane; e < kBatchBlock * kBatchBlock; e += 32) {
-                    const int t = e >> 5, pp = e & 31;
-                    if (pp < t) {
-                        unsigned v = 0;
-#pragma unroll
-                        for (int cp = 0; cp < kBatchPCopies; ++cp)
-                            v += __ldcg(pk_base + (size_t)cp * (kBatchBlock * kBatchBlock) + e);
-                        sP[t * 33 + pp] = (int)v;
-                    }
-                }
-            }
-            __syncwarp();
             long long sumE = a.sumE[c];
             // num_t from the exact integer dot and residual total, once per
             // block in FP64; then carried as a double-float pair through the
