@@ -443,6 +443,7 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     a.prof = c->profile ? c->d_prof : nullptr;
     // the timeline holds one row per SM: a sweep on more CTAs records none
     a.tline = c->profile && c->timeline && c->G <= c->sms ? c->d_tline : nullptr;
+    a.async_batch = cf.async_batch;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
     a.gram = c->d_gram;
@@ -801,6 +802,13 @@ int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
     int spec = c.spec_width ? c.spec_width : (c.form == BRR_FORM_FP64 ? 16 : 32);
     if (spec != 8 && spec != 16 && spec != 32 && spec != 64)
         return fail(BRR_ERR_ARG, "spec_width must be 8, 16, 32 or 64");
+    if (c.async_batch < 0 || c.async_batch > kMaxSpec)
+        return fail(BRR_ERR_ARG, "async_batch must be in 0..64");
+    if (c.async_batch > 0 && c.form != BRR_FORM_FP64)
+        return fail(BRR_ERR_ARG, "the asynchronous schedule runs the FP64 form");
+    // an asynchronous batch is one round: the round width covers it
+    while (spec < c.async_batch)
+        spec *= 2;
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)

@@ -94,6 +94,7 @@ struct SweepArgs {
     int eigen;                   // ragged sweep: Eigen sparse markers (missing genotypes enter
                                  // the dot product at the marker's mean)
     unsigned long long *t_out;   // optional [2]: global timer (ns) at the start and end of the sweep (CTA 0)
+    int async_batch;             // restart sweep: 0 synchronous; T > 0 asynchronous batches of T markers
     unsigned long long *tline;   // blocked sweep, counting variant, optional: per-CTA event timeline
                                  // [kTimelineIters][G][kTimelineEvents] of global-timer stamps (ns)
 };

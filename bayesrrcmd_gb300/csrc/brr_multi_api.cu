@@ -258,6 +258,8 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
             return api_fail(BRR_ERR_ARG, "all instances of a multi-instance run share the sweep form and the device");
         if (cfgs[i].kind != BRR_KIND_DENSE && cfgs[i].kind != BRR_KIND_RAGGED && cfgs[i].kind != BRR_KIND_EIGEN)
             return api_fail(BRR_ERR_ARG, "unknown marker kind");
+        if (cfgs[i].async_batch != 0)
+            return api_fail(BRR_ERR_ARG, "the multi-instance sweep runs the synchronous schedule");
     }
     brr_multi *m = new brr_multi();
     m->n = n;

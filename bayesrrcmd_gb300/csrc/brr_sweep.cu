@@ -449,7 +449,10 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         issue_codes(start + 2u * B);
         issue_recs(start + 3u * B);
         cp_async_commit();
-        const int nb = (int)min((unsigned)B, M32 - start);
+        // a synchronous round resolves up to B markers and ends at the first
+        // that changes the residual; an asynchronous batch takes T markers
+        // that all read the same residual, and applies every change
+        const int nb = (int)min((unsigned)(a.async_batch > 0 ? a.async_batch : B), M32 - start);
         if (tid == 0)
             s_first = kMaxSpec;
         mark(0);
@@ -662,7 +665,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         __syncthreads();
         mark(3);
 
-        const int first = s_first;
+        const int first = a.async_batch > 0 ? nb : s_first;
         const int last = first < nb ? first : nb - 1;
         if (sidx == 0) {
             // outputs of the resolved markers, only from CTA 0
@@ -670,7 +673,8 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                 const SweepRec &rc = ring_rec[(start + tid) & Rm];
                 const int c = s_comp[tid];
                 a.beta[rc.j] = s_beta[tid];
-                a.acum[rc.j] = s_acum[tid];
+                if (a.async_batch == 0)   // processColumnAsync leaves acum as it was
+                    a.acum[rc.j] = s_acum[tid];
                 a.chosen[rc.j] = c >= 0 ? 1 : 0;
                 if (c >= 0)
                     a.comp[rc.j] = c;
@@ -683,11 +687,15 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             for (int i = tid; i < kMaxSpec * 4; i += kThreads)
                 s_acc[i] = 0ull;
 
-        // ---- apply the residual update of the first changing marker
-        if (first < nb) {
-            const unsigned slot = (start + first) & Rm;
+        // ---- apply the residual update of marker u of the round (the first
+        // changing marker of a synchronous round; every changing marker of an
+        // asynchronous batch, in order).  The decision of whether to apply is
+        // the same in every thread (shared memory), so the barriers inside are
+        // reached by all.
+        auto apply_one = [&](const int u) {
+            const unsigned slot = (start + u) & Rm;
             const SweepRec &rc = ring_rec[slot];
-            const double dBeta = rc.beta_old - s_beta[first];
+            const double dBeta = rc.beta_old - s_beta[u];
             if (KIND == kKindDense) {
                 const uint8_t *cb = ring_codes + slot * a.slot_bytes;
                 if (FORM == kFormFP64) {
@@ -753,6 +761,16 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                     }
                 }
             }
+        };
+        if (a.async_batch > 0) {
+            for (int u = 0; u < nb; ++u) {
+                if (ring_rec[(start + u) & Rm].beta_old != 0.0 || s_beta[u] != 0.0) {
+                    apply_one(u);
+                    __syncthreads();
+                }
+            }
+        } else if (first < nb) {
+            apply_one(first);
         }
         __syncthreads();
         mark(4);

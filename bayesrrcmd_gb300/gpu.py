@@ -35,7 +35,7 @@ class BrrConfig(C.Structure):
         ("seed", C.c_uint32), ("chain", C.c_uint32),
         ("v0E", C.c_double), ("s02E", C.c_double), ("v0G", C.c_double), ("s02G", C.c_double),
         ("refresh_every", C.c_int32), ("spec_width", C.c_int32), ("grid", C.c_int32), ("device", C.c_int32),
-        ("gram", C.c_int32),
+        ("gram", C.c_int32), ("async_batch", C.c_int32),
     ]
 
 
@@ -194,6 +194,7 @@ class ChainConfig:
     grid: int = 0
     device: int = 0
     gram: int = 0
+    async_batch: int = 0
 
     def to_c(self) -> BrrConfig:
         c = BrrConfig()
@@ -207,6 +208,7 @@ class ChainConfig:
         c.v0E, c.s02E, c.v0G, c.s02G = self.v0E, self.s02E, self.v0G, self.s02G
         c.refresh_every, c.spec_width, c.grid, c.device = self.refresh_every, self.spec_width, self.grid, self.device
         c.gram = self.gram
+        c.async_batch = self.async_batch
         return c
 
 

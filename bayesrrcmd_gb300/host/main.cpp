@@ -74,6 +74,15 @@ brr_config makeConfig(const Options &opt, const Data &data)
     c.refresh_every = opt.refreshEvery;
     c.spec_width = opt.specWidth;
     c.device = opt.device;
+    if (opt.analysisType == AnalysisType::AsyncPpBayes) {
+        // the reference's ParallelGraph with --analysis-tokens markers in flight
+        // (src/analysisrunner.cpp:259-268, src/parallelgraph.cpp:51-150)
+        if (opt.analysisTokens < 1 || opt.analysisTokens > 64)
+            throw std::string("Error: --analysis-tokens must be in 1..64 for the GPU asyncppbayes sweep");
+        if (c.form != BRR_FORM_FP64)
+            throw std::string("Error: asyncppbayes runs the FP64 form (--form fp64)");
+        c.async_batch = opt.analysisTokens;
+    }
     return c;
 }
 
@@ -459,7 +468,7 @@ void printOptions(const Options &o)
               << o.chainLength << ", \"burnin\": " << o.burnin << ", \"thin\": " << o.thin << ", \"seed\": " << o.seed
               << ", \"samples\": \"" << o.mcmcSampleFile << "\", \"sparse\": " << (int)o.preprocessDataType
               << ", \"form\": \"" << o.form << "\", \"colLog\": \"" << (o.colLog ? o.colLogFile : "")
-              << "\", \"fixed\": " << o.fixedEffectNumber << ", \"failure\": \"" << o.failureFile
+              << "\", \"tokens\": " << o.analysisTokens << ", \"fixed\": " << o.fixedEffectNumber << ", \"failure\": \"" << o.failureFile
               << "\", \"compress\": " << (o.compress ? "true" : "false")
               << ", \"zlib\": " << (canReadCompressed() ? "true" : "false") << ", \"S\": [";
     for (std::size_t g = 0; g < o.S.size(); ++g) {
@@ -504,12 +513,17 @@ int main(int argc, const char *argv[])
             }
             return ppbayes(opt) ? 0 : 1;
         case AnalysisType::AsyncPpBayes:
+            if (opt.S.empty()) {
+                std::cerr << "Variance components `--S` are missing or could not be parsed!" << std::endl;
+                return 1;
+            }
+            return ppbayes(opt) ? 0 : 1;
         case AnalysisType::Gauss:
         case AnalysisType::AsyncGauss:
-            // the asynchronous graph and the BayesW (Gauss) analyses of the
-            // reference (src/analysisrunner.cpp:219-268) are not on this path
-            std::cerr << "Error: this GPU sampler runs --analysis-type ppbayes (and preprocess); "
-                         "asyncppbayes, gauss and asyncgauss are not supported" << std::endl;
+            // the BayesW (Gauss) analyses of the reference
+            // (src/analysisrunner.cpp:219-268) are not on this path
+            std::cerr << "Error: this GPU sampler runs --analysis-type ppbayes and asyncppbayes (and preprocess); "
+                         "gauss and asyncgauss are not supported" << std::endl;
             return 1;
         default:
             std::cerr << "unknown analysis type" << std::endl;

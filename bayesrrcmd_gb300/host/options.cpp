@@ -218,9 +218,13 @@ void Options::inputOptions(int argc, const char *argv[])
             v0G = std::atof(need(i));
         } else if (!std::strcmp(a, "--s02G")) {
             s02G = std::atof(need(i));
+        } else if (!std::strcmp(a, "--analysis-tokens")) {
+            // asyncppbayes: the markers the reference's ParallelGraph keeps in
+            // flight (src/options.cpp:216-219), the GPU sweep's batch
+            analysisTokens = std::atoi(need(i));
         } else if (!std::strcmp(a, "--thread-spawned") || !std::strcmp(a, "--decompression-concurrency") ||
                    !std::strcmp(a, "--decompression-tokens") || !std::strcmp(a, "--analysis-concurrency") ||
-                   !std::strcmp(a, "--analysis-tokens") || !std::strcmp(a, "--preprocess-chunks")) {
+                   !std::strcmp(a, "--preprocess-chunks")) {
             need(i);   // host-thread tuning of the reference's TBB graphs: accepted, no effect on the GPU path
         } else if (!std::strcmp(a, "--form")) {
             form = need(i);

@@ -52,6 +52,7 @@ struct Options {
     // GB300 additions
     std::string form = "fp64";             // fp64 (drop-in) | fp32c
     int refreshEvery = 50;
+    int analysisTokens = 20;    // asyncppbayes: markers in flight (src/options.hpp:33)
     int specWidth = 0;
     int device = 0;
     bool printOptions = false;

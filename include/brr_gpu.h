@@ -110,6 +110,11 @@ typedef struct brr_config {
     int32_t device;            /* CUDA device ordinal */
     int32_t gram;              /* FP32C dense: 0 blocked sweep with a precomputed marker Gram when it fits
                                   in device memory, -1 never, 1 required */
+    int32_t async_batch;       /* 0: the synchronous sweep (ppbayes); T in 1..64: the asyncppbayes
+                                  schedule of the reference's ParallelGraph with T analysis tokens
+                                  (src/parallelgraph.cpp:51-150): the T markers of a batch all read
+                                  the residual before any of them updates it, acum is not written
+                                  (src/BayesRBase.cpp:394-524); FP64 form only */
 } brr_config;
 
 /* Chain state; arrays are caller-owned, sized M (beta, comp, acum) and N (eps).

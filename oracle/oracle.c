@@ -462,8 +462,13 @@ int or_init(const or_problem *p, or_state *s)
  * kernel (src/densebayesrkernel.cpp:10-20) or the ragged kernel
  * (src/sparsebayesrkernel.cpp:10-34, src/raggedbayesrkernel.cpp:10-35,
  * src/SparseBayesRRG.cpp:76-92). */
-static void process_column(const or_problem *p, const or_markers *mk, or_state *s,
-                           uint32_t j, double p_u, double z)
+/* The sampling half of processColumn (src/BayesRBase.cpp:287-366) for marker j
+ * against the current residual: the new beta, component, component counts and
+ * squared effects; acum (P(component 0)) is stored when write_acum is set, as
+ * the synchronous processColumn does (:341) and processColumnAsync does not
+ * (:394-496).  Returns the new beta; *beta_old_out gets the old one. */
+static double column_pick(const or_problem *p, const or_markers *mk, or_state *s,
+                          uint32_t j, double p_u, double z, int write_acum, double *beta_old_out)
 {
     const int64_t N = p->N;
     const double NM1 = (double)(N - 1);
@@ -555,7 +560,8 @@ static void process_column(const or_problem *p, const or_markers *mk, or_state *
             sum += exp(logL[k] - logL[0]);
         acum = 1.0 / sum;
     }
-    s->acum[j] = acum;
+    if (write_acum)
+        s->acum[j] = acum;
 
     /* inverse-CDF walk (:346-366).  The reference evaluates the guard for
      * k = K-1 against logL[K], one past the end; the resulting acum is never
@@ -586,7 +592,17 @@ static void process_column(const or_problem *p, const or_markers *mk, or_state *
         }
     }
     s->beta[j] = beta_new;
+    *beta_old_out = beta_old;
+    return beta_new;
+}
 
+/* The residual half (src/BayesRBase.cpp:368-378, the kernels' epsilon change
+ * and the running epsilon sum): nothing when the marker stays out of the
+ * model. */
+static void column_update(const or_problem *p, const or_markers *mk, or_state *s,
+                          uint32_t j, double beta_old, double beta_new)
+{
+    const int64_t N = p->N;
     if (beta_old == 0.0 && beta_new == 0.0)
         return;                                   /* (:372) */
     const double dBeta = beta_old - beta_new;
@@ -622,12 +638,42 @@ static void process_column(const or_problem *p, const or_markers *mk, or_state *
     }
 }
 
+static void process_column(const or_problem *p, const or_markers *mk, or_state *s,
+                           uint32_t j, double p_u, double z)
+{
+    double beta_old;
+    const double beta_new = column_pick(p, mk, s, j, p_u, z, 1, &beta_old);
+    column_update(p, mk, s, j, beta_old, beta_new);
+}
+
 int or_sweep(const or_problem *p, const or_markers *mk, or_state *s,
              const uint32_t *order, const double *u, const double *z)
 {
-    for (int64_t q = 0; q < p->M; ++q) {
-        const uint32_t j = order[q];
-        process_column(p, mk, s, j, u[j], z[j]);
+    if (p->async_batch <= 0) {
+        for (int64_t q = 0; q < p->M; ++q) {
+            const uint32_t j = order[q];
+            process_column(p, mk, s, j, u[j], z[j]);
+        }
+        return OR_OK;
+    }
+    /* asyncppbayes (src/parallelgraph.cpp:51-150, src/BayesRBase.cpp:394-524):
+     * the ParallelGraph keeps up to analysisTokens markers in flight and lets the
+     * next ones start when all have returned.  The schedule restated here is
+     * the one where every marker of a batch of async_batch consecutive markers
+     * reads the residual (and the running residual sum) before any of them
+     * writes: all picks of the batch first, then the updates in sweep order. */
+    const int64_t T = p->async_batch;
+    double bo[OR_MAX_ASYNC], bn[OR_MAX_ASYNC];
+    if (T > OR_MAX_ASYNC)
+        return OR_ERR_ARG;
+    for (int64_t q0 = 0; q0 < p->M; q0 += T) {
+        const int64_t q1 = q0 + T < p->M ? q0 + T : p->M;
+        for (int64_t q = q0; q < q1; ++q) {
+            const uint32_t j = order[q];
+            bn[q - q0] = column_pick(p, mk, s, j, u[j], z[j], 0, &bo[q - q0]);
+        }
+        for (int64_t q = q0; q < q1; ++q)
+            column_update(p, mk, s, order[q], bo[q - q0], bn[q - q0]);
     }
     return OR_OK;
 }

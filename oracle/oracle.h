@@ -35,6 +35,7 @@ extern "C" {
 
 #define OR_MAX_GROUPS 64
 #define OR_MAX_K 16
+#define OR_MAX_ASYNC 64     /* largest asyncppbayes batch (markers in flight) */
 
 /* Marker storage kinds (reference: src/common.h:27-32 PreprocessDataType). */
 #define OR_KIND_DENSE 0
@@ -107,6 +108,9 @@ typedef struct {
      * for problems whose columns do not fit in host memory.  Both read the
      * same value for every genotype, in the same order: identical results. */
     int32_t dense_lut;
+    /* 0: the synchronous sweep (ppbayes); T > 0: the asyncppbayes schedule with
+     * T markers in flight (at most OR_MAX_ASYNC) */
+    int32_t async_batch;
 } or_problem;
 
 typedef struct {

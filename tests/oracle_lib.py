@@ -23,6 +23,7 @@ class OrProblem(C.Structure):
         ("y", C.POINTER(C.c_float)), ("bed", C.POINTER(C.c_uint8)), ("seed", C.c_uint32), ("chain", C.c_uint32),
         ("v0E", C.c_double), ("s02E", C.c_double), ("v0G", C.c_double), ("s02G", C.c_double),
         ("shared_perm", C.c_int32), ("perm_chain", C.c_uint32), ("dense_lut", C.c_int32),
+        ("async_batch", C.c_int32),
     ]
 
 
@@ -169,7 +170,7 @@ class OracleChain:
     """Oracle chain over the same inputs as the GPU Chain."""
 
     def __init__(self, bed, N, y, S, kind=0, group=None, seed=1, chain=0, priors=(1e-4, 1e-4, 1e-4, 1e-4),
-                 perm_chain=None, dense_lut=False):
+                 perm_chain=None, dense_lut=False, async_batch=0):
         self.bed = np.ascontiguousarray(bed, np.uint8)
         self.N, self.M = N, bed.shape[0]
         self.y = np.ascontiguousarray(y, np.float32)
@@ -189,6 +190,7 @@ class OracleChain:
         if perm_chain is not None:
             pr.shared_perm, pr.perm_chain = 1, perm_chain
         pr.dense_lut = 1 if dense_lut else 0
+        pr.async_batch = int(async_batch)
         self.pr = pr
         h = C.c_void_p()
         rc = lib().or_markers_create(C.byref(pr), C.byref(h))

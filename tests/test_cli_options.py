@@ -69,11 +69,18 @@ def test_analysis_type(brr):
     assert opts(brr)["analysis"] == 0
 
 
-@pytest.mark.parametrize("kind", ["asyncppbayes", "gauss", "asyncgauss"])
+@pytest.mark.parametrize("kind", ["gauss", "asyncgauss"])
 def test_analyses_off_this_path_are_refused(brr, kind):
-    """... and are refused with a message naming what runs here."""
+    """... and the BayesW analyses are refused with a message naming what runs here."""
     r = subprocess.run([brr, "--analysis-type", kind, "--S", "0.01"], capture_output=True, text=True)
     assert r.returncode == 1 and "ppbayes" in r.stderr and "not supported" in r.stderr
+
+
+def test_asyncppbayes_takes_the_analysis_tokens(brr):
+    """asyncppbayes runs with --analysis-tokens markers in flight (the
+    reference's default 20, src/options.hpp:33); the GPU batch holds 1..64."""
+    assert opts(brr, "--analysis-type", "asyncppbayes")["tokens"] == 20
+    assert opts(brr, "--analysis-type", "asyncppbayes", "--analysis-tokens", "7")["tokens"] == 7
 
 
 def test_sparse_data_and_chain_flags(brr):

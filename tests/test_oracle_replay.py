@@ -103,7 +103,12 @@ def sweep_once(kind, N, M, miss, seed, strong=False):
     return g, group, s0, order, u, z, oc.state()
 
 
-def replay(kind, g, group, s0, order, u, z, S=S2):
+def replay(kind, g, group, s0, order, u, z, S=S2, async_batch=0):
+    """One sweep.  async_batch T > 0 replays the asyncppbayes schedule: the
+    markers of each batch of T consecutive positions all read the residual and
+    its running sum before any of them writes (processColumnAsync then
+    updateGlobal, src/BayesRBase.cpp:394-524, src/SparseBayesRRG.cpp:94-102),
+    and acum is left as it was (processColumnAsync never writes m_acum)."""
     M, N = g.shape
     beta, comp, acum = s0["beta"].copy(), s0["comp"].copy(), s0["acum"].copy()
     eps, eps_sum = s0["eps"].copy(), s0["epsSum"]
@@ -116,7 +121,8 @@ def replay(kind, g, group, s0, order, u, z, S=S2):
         ones, twos, missing = g == 1, g == 2, g < 0
     else:
         zg, mean, sd, zsum = eigen_statistics(g)
-    for j in order:
+
+    def pick(j):
         gr = group[j]
         b_old = beta[j]
         if kind == 0:
@@ -126,16 +132,21 @@ def replay(kind, g, group, s0, order, u, z, S=S2):
         else:
             num = b_old * (N - 1.0) - mean[j] * eps_sum / sd[j] + zg[j] @ eps / sd[j]
         a0, k, b_new = process_column(num, b_old, u[j], z[j], s0["sigmaE"], s0["sigmaG"][gr], s0["pi"][gr], S[gr], N)
-        acum[j] = a0
+        if async_batch <= 0:
+            acum[j] = a0
         if k is not None:
             beta[j] = b_new
             comp[j] = k
             v[gr, k] += 1.0
             if k > 0:
                 bsq[gr] += b_new * b_new
-        if b_old == 0.0 and beta[j] == 0.0:
-            continue
-        d = b_old - beta[j]
+        return b_old, beta[j]
+
+    def update(j, b_old, b_new):
+        nonlocal eps, eps_sum
+        if b_old == 0.0 and b_new == 0.0:
+            return
+        d = b_old - b_new
         if kind == 0:
             eps += d * x[j]
         elif kind == 2:
@@ -149,6 +160,16 @@ def replay(kind, g, group, s0, order, u, z, S=S2):
             delta[twos[j]] += 2.0 * d / sd[j]
             delta[missing[j]] += adj
             eps += delta
+
+    if async_batch <= 0:
+        for j in order:
+            update(j, *pick(j))
+    else:
+        for q0 in range(0, len(order), async_batch):
+            batch = order[q0:q0 + async_batch]
+            picks = [pick(j) for j in batch]
+            for j, (b_old, b_new) in zip(batch, picks):
+                update(j, b_old, b_new)
     return dict(beta=beta, comp=comp, acum=acum, eps=eps, epsSum=eps_sum, v=v, betasqnG=bsq)
 
 
@@ -179,6 +200,62 @@ def test_oracle_sweep_equals_numpy_restatement(kind, N, M, miss, seed, strong):
     if strong:
         # the guards fired: P(component 0) is exactly zero for the strong marker
         assert s1["acum"][0] == 0.0
+
+
+@pytest.mark.parametrize("kind,miss,T,seed", [
+    (0, 0.0, 20, 31), (0, 0.02, 7, 32), (1, 0.03, 20, 33), (1, 0.0, 64, 34), (2, 0.03, 13, 35),
+])
+def test_oracle_async_sweep_equals_numpy_restatement(kind, miss, T, seed):
+    """The asyncppbayes schedule (batches of T markers in flight) of the oracle
+    against the numpy restatement, over a chain that has run two asynchronous
+    iterations first."""
+    N, M = 540, 150
+    g, _ = plink.synth_genotypes(N, M, seed=seed, missing=miss)
+    bed = plink.encode_bed(g)
+    y, _, _ = plink.synth_phenotype(g, seed, M // 8, 0.6)
+    group = (np.arange(M) % 2).astype(np.int32)
+    oc = O.OracleChain(bed, N, y, S2, kind=kind, group=group, seed=seed, async_batch=T)
+    for it in range(2):
+        oc.iterate(it)
+    s0 = oc.state()
+    order = O.permutation(seed, 0, 77, M)
+    u, z = O.marker_draws(seed, 0, 77, M)
+    oc.sweep(order, u, z)
+    s1 = oc.state()
+    r = replay(kind, g, group, s0, order, u, z, async_batch=T)
+    np.testing.assert_array_equal(s1["comp"], r["comp"])
+    np.testing.assert_allclose(s1["beta"], r["beta"], rtol=1e-10, atol=1e-14)
+    np.testing.assert_array_equal(s1["acum"], s0["acum"])
+    np.testing.assert_allclose(s1["eps"], r["eps"], rtol=0, atol=1e-10)
+    np.testing.assert_array_equal(s1["v"][:, :4], r["v"])
+    np.testing.assert_allclose(s1["betasqnG"], r["betasqnG"], rtol=1e-10)
+    if kind != 0:
+        np.testing.assert_allclose(s1["epsSum"], r["epsSum"], rtol=0, atol=1e-9)
+    assert np.count_nonzero(s1["comp"] != s0["comp"]) > 0
+    # the schedule differs from the synchronous sweep
+    sync = replay(kind, g, group, s0, order, u, z)
+    assert not np.allclose(sync["eps"], r["eps"], rtol=0, atol=1e-12)
+
+
+def test_oracle_async_batch_of_one_is_the_synchronous_chain():
+    """One marker in flight is the sequential chain (acum aside, which the
+    asynchronous path never writes)."""
+    N, M = 400, 90
+    g, _ = plink.synth_genotypes(N, M, seed=5, missing=0.01)
+    bed = plink.encode_bed(g)
+    y, _, _ = plink.synth_phenotype(g, 5, 10, 0.5)
+    for kind in (0, 1, 2):
+        a = O.OracleChain(bed, N, y, S2, kind=kind, group=(np.arange(M) % 2).astype(np.int32), seed=3)
+        b = O.OracleChain(bed, N, y, S2, kind=kind, group=(np.arange(M) % 2).astype(np.int32), seed=3,
+                          async_batch=1)
+        for it in range(3):
+            a.iterate(it)
+            b.iterate(it)
+            sa, sb = a.state(), b.state()
+            for k in ("beta", "comp", "eps", "sigmaG"):
+                np.testing.assert_array_equal(sa[k], sb[k])
+            assert sa["sigmaE"] == sb["sigmaE"] and sa["mu"] == sb["mu"]
+        assert (sb["acum"] == 0).all() and (sa["acum"] != 0).any()
 
 
 # Two groups with the same number of components, as the reference's K x groups
