@@ -444,6 +444,7 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     // the timeline holds one row per SM: a sweep on more CTAs records none
     a.tline = c->profile && c->timeline && c->G <= c->sms ? c->d_tline : nullptr;
     a.async_batch = cf.async_batch;
+    a.cluster = cf.cluster > 0 && c->G > 1 ? c->G : 0;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
     a.gram = c->d_gram;
@@ -609,7 +610,7 @@ void schedule_permutation(brr_ctx *c, uint32_t it)
 int prepare_blocked(brr_ctx *c)
 {
     const brr_config &cf = c->cfg;
-    if (cf.form != BRR_FORM_FP32C || cf.kind != BRR_KIND_DENSE || cf.gram < 0 || cf.M < 2) {
+    if (cf.form != BRR_FORM_FP32C || cf.kind != BRR_KIND_DENSE || cf.gram < 0 || cf.M < 2 || cf.cluster > 0) {
         c->blocked = false;
         if (cf.gram > 0)
             return fail(BRR_ERR_ARG, "the Gram-blocked sweep needs the FP32C form, dense markers and M >= 2");
@@ -806,6 +807,10 @@ int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
         return fail(BRR_ERR_ARG, "async_batch must be in 0..64");
     if (c.async_batch > 0 && c.form != BRR_FORM_FP64)
         return fail(BRR_ERR_ARG, "the asynchronous schedule runs the FP64 form");
+    if (c.cluster < 0 || c.cluster == 1 || c.cluster > 16)
+        return fail(BRR_ERR_ARG, "cluster must be 0 or 2..16");
+    if (c.cluster > 0 && c.gram > 0)
+        return fail(BRR_ERR_ARG, "the cluster sweep is the restart sweep: gram cannot be required");
     // an asynchronous batch is one round: the round width covers it
     while (spec < c.async_batch)
         spec *= 2;
@@ -840,7 +845,7 @@ int brr_ctx_create(const brr_config *cfg, brr_ctx **out)
     // slices of individuals in 64-individual chunks (16 bytes of codes)
     x->chunks = (c.N + kChunk - 1) / kChunk;
     x->col_stride = x->chunks * 16;
-    compute_slices(x, c.grid > 0 ? c.grid : x->sms);
+    compute_slices(x, c.cluster > 0 ? c.cluster : (c.grid > 0 ? c.grid : x->sms));
     if (c.kind != BRR_KIND_DENSE && x->slice_max > 65536) {
         free_all(x);
         delete x;
@@ -972,7 +977,15 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     a.n_groups = cf.n_groups;
     a.slice_max = c.slice_max;
     a.slot_bytes = c.slot_bytes;
+    a.cluster = cf.cluster > 0 && c.G > 1 ? c.G : 0;
     const size_t smem = sweep_smem_bytes(cf.form, c.kind, a);
+    if (a.cluster > 0) {
+        if (sweep_cluster_fits(cf.form, c.kind, c.G, smem) < 1)
+            return fail(BRR_ERR_ARG, "a cluster of " + std::to_string(c.G) + " CTAs with " + std::to_string(smem) +
+                                         " bytes of shared memory each cannot be scheduled");
+        c.packed = true;
+        return BRR_OK;
+    }
     const int per_sm = sweep_max_ctas_per_sm(cf.form, c.kind, smem);
     if (per_sm < 1 || (int64_t)per_sm * c.sms < c.G)
         return fail(BRR_ERR_ARG, "the sweep kernel does not fit " + std::to_string(c.G) +

@@ -243,6 +243,8 @@ int brr_batch_create(const brr_config *cfg, int32_t chains, brr_batch **out)
         return api_fail(BRR_ERR_ARG, "the batched form runs 32 or 64 chains");
     if (c.async_batch != 0)
         return api_fail(BRR_ERR_ARG, "the batched form runs the synchronous schedule");
+    if (c.cluster != 0)
+        return api_fail(BRR_ERR_ARG, "the batched form runs on the whole GPU, not as one cluster");
     if (c.n_groups < 1 || c.n_groups > BRR_MAX_GROUPS)
         return api_fail(BRR_ERR_ARG, "n_groups must be in 1..64");
     for (int g = 0; g < c.n_groups; ++g) {

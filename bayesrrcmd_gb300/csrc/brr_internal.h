@@ -95,6 +95,8 @@ struct SweepArgs {
                                  // the dot product at the marker's mean)
     unsigned long long *t_out;   // optional [2]: global timer (ns) at the start and end of the sweep (CTA 0)
     int async_batch;             // restart sweep: 0 synchronous; T > 0 asynchronous batches of T markers
+    int cluster;                 // restart sweep: 0 grid-wide exchange; G: the G CTAs are one thread-block
+                                 // cluster exchanging through distributed shared memory
     unsigned long long *tline;   // blocked sweep, counting variant, optional: per-CTA event timeline
                                  // [kTimelineIters][G][kTimelineEvents] of global-timer stamps (ns)
 };
@@ -239,6 +241,8 @@ cudaError_t noalloc_xbeta(cudaStream_t st, int kind, int64_t N, const uint8_t *c
                           std::string &why);
 bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string &why);
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem);
+// Clusters of G CTAs of the cluster sweep that can be resident at once (0: none).
+int sweep_cluster_fits(int form, int kind, int G, size_t smem);
 size_t sweep_block_smem_bytes(const SweepArgs &a);
 cudaError_t launch_gather_block(const uint32_t *order, int64_t M, int64_t N, const double *table,
                                 const double *scale, const double *beta, const double *u, const double *z,

@@ -260,6 +260,8 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
             return api_fail(BRR_ERR_ARG, "unknown marker kind");
         if (cfgs[i].async_batch != 0)
             return api_fail(BRR_ERR_ARG, "the multi-instance sweep runs the synchronous schedule");
+        if (cfgs[i].cluster != 0)
+            return api_fail(BRR_ERR_ARG, "the multi-instance sweep exchanges through L2, not as clusters");
     }
     brr_multi *m = new brr_multi();
     m->n = n;

@@ -17,6 +17,11 @@
 // (beta_old != 0 or beta_new != 0) ends the round: its update is applied and
 // the next round starts right after it.  Every sampled marker therefore sees
 // exactly the residual of the sequential chain.
+//
+// The cluster variant runs the same sweep as one thread-block cluster of up to
+// 16 CTAs: each CTA stores its partial sums straight into every CTA's shared
+// memory (distributed shared memory, st.async completing on the receiver's
+// mbarrier), so a round needs no global atomics and no grid-wide barrier.
 #include "brr_device.cuh"
 #include "brr_internal.h"
 #include "brr_pick.cuh"
@@ -180,13 +185,14 @@ struct SmemPlan {
     size_t gk;              // n_groups ints
     size_t gcf;             // FP32C: FP32 sampler constants, n_groups x kMaxK x 2 floats
     size_t gtab;            // FP32C dense: 256 float4 + 256 bytes
+    size_t xch;             // cluster: [2][cluster][B] exchange records of 32 bytes
     size_t total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 __host__ __device__ inline SmemPlan make_plan(int form, int kind, int slice_max, int slot_bytes, int B, int n_groups,
-                                              size_t rec_bytes = sizeof(SweepRec))
+                                              int cluster = 0, size_t rec_bytes = sizeof(SweepRec))
 {
     SmemPlan p;
     const int R = 4 * B;
@@ -214,6 +220,9 @@ __host__ __device__ inline SmemPlan make_plan(int form, int kind, int slice_max,
     p.gtab = o;
     if (form != kFormFP64 && kind == kKindDense)
         o += 256 * 16 + 256;
+    o = align16(o);
+    p.xch = o;
+    o += (size_t)2 * cluster * B * 32;
     p.total = align16(o);
     return p;
 }
@@ -255,13 +264,91 @@ __device__ __forceinline__ double lut_select(unsigned c, double l0, double l1, d
     return (c & 2u) ? ((c & 1u) ? l3 : l2) : ((c & 1u) ? l1 : l0);
 }
 
+// ---- thread-block-cluster primitives (distributed shared memory)
+__device__ __forceinline__ unsigned cl_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Address of the same shared-memory location in CTA `rank` of the cluster.
+__device__ __forceinline__ unsigned cl_map(unsigned addr, unsigned rank)
+{
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+
+// 16-byte store into a CTA's shared memory that completes as 16 transaction
+// bytes on that CTA's mbarrier `rbar`.
+__device__ __forceinline__ void cl_push16(unsigned raddr, unsigned long long w0, unsigned long long w1, unsigned rbar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b64 [%0], {%1, %2}, [%3];" ::"r"(raddr),
+                 "l"(w0), "l"(w1), "r"(rbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cl_bar_init(uint64_t *m)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cl_addr(m)) : "memory");
+}
+
+// The receiver's own arrival of a round: one arrival plus the bytes it expects.
+__device__ __forceinline__ void cl_expect(uint64_t *m, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(cl_addr(m)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool cl_test(uint64_t *m, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(cl_addr(m)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `parity` of m at most timeout_ns; false on timeout.
+__device__ __forceinline__ bool cl_wait(uint64_t *m, unsigned parity, uint64_t timeout_ns)
+{
+    if (cl_test(m, parity))
+        return true;
+    const uint64_t t0 = global_timer_ns();
+    unsigned spins = 0;
+    while (!cl_test(m, parity)) {
+        if ((++spins & 63u) == 0 && global_timer_ns() - t0 > timeout_ns)
+            return false;
+    }
+    return true;
+}
+
+// All threads of all CTAs of the cluster (release / acquire at cluster scope).
+// Used once after the mbarriers are initialised and once before the CTAs
+// exit; every wait between the two is bounded, so every CTA reaches both.
+__device__ __forceinline__ void cl_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cl_rank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ __int128 u128_join(unsigned long long lo, unsigned long long hi)
+{
+    return (__int128)(((unsigned __int128)hi << 64) | (unsigned __int128)lo);
+}
+
 // --------------------------------------------------------------------------
 // The sweep of one chain over its G CTAs; sidx is this CTA's slice.  Run by
 // k_sweep (one chain per launch) and k_sweep_multi (several chains of
 // different sizes, each on its own group of CTAs, in one launch).  PROF: the
 // variant that counts phase cycles on the first CTA (the plain variant reads no
 // clock, whose reads would constrain the scheduling of every CTA's code).
-template <int FORM, int KIND, int KM, bool PROF>
+// CL: the G CTAs are one thread-block cluster and exchange the round's partial
+// sums through distributed shared memory (k_sweep_cl).
+template <int FORM, int KIND, int KM, bool PROF, bool CL = false>
 __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -276,7 +363,9 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     __shared__ double s_red[kThreads / 32][2];
     // a chain on one CTA exchanges nothing: its round's sums stay in shared memory
     __shared__ unsigned long long s_acc[kMaxSpec * 4];
-    const bool solo = a.G == 1 && a.phantom == 0;
+    // cluster: the exchange's mbarrier of each round parity
+    __shared__ __align__(8) uint64_t s_xbar[2];
+    const bool solo = !CL && a.G == 1 && a.phantom == 0;
 
     const int B = a.B;
     const int lpm = kThreads / B;
@@ -288,7 +377,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     const int ns = a.slice_lo[sidx + 1] - lo;
     const int nbytes = ((ns + kChunk - 1) / kChunk) * 16;
     const int64_t byte_lo = lo / 4;
-    const SmemPlan plan = make_plan(FORM, KIND, a.slice_max, a.slot_bytes, B, a.n_groups);
+    const SmemPlan plan = make_plan(FORM, KIND, a.slice_max, a.slot_bytes, B, a.n_groups, CL ? a.G : 0);
 
     double *eps64 = reinterpret_cast<double *>(smem + plan.eps0);
     float *eh = reinterpret_cast<float *>(smem + plan.eps0);
@@ -301,6 +390,9 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     float *gcf = reinterpret_cast<float *>(smem + plan.gcf);
     float4 *gtab = reinterpret_cast<float4 *>(smem + plan.gtab);
     uint8_t *mtab = smem + plan.gtab + 256 * 16;
+    // cluster exchange records [round parity][source CTA][marker]: the partial
+    // sum and the missing-genotype sum, each a 128-bit fixed-point integer
+    ulonglong2 *xch = reinterpret_cast<ulonglong2 *>(smem + plan.xch);
 
     // ---- prologue: residual slice, constants, tables
     float muh, mul;
@@ -351,7 +443,14 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         s_scal[0] = 0.0;          // ragged shift
         s_scal[1] = a.epsSum;     // ragged running sum
         s_scal[2] = a.eps_total;  // dense FP32C: sum of the residual
+        if (CL) {
+            cl_bar_init(&s_xbar[0]);
+            cl_bar_init(&s_xbar[1]);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
     }
+    if (CL)
+        cl_sync_all();   // every CTA's mbarriers exist before the first store into it
     __syncthreads();
 
     // ---- prefetch machinery (ring slots are positions modulo R, a power of two)
@@ -443,6 +542,31 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     unsigned start = 0;
     long long r = 0;
     int rb = 0;   // r % 3
+    // cluster: the team's lanes store marker t's two sums (those of the team's
+    // first lane) into CTAs lane, lane + lpm, ... of the cluster; the copy for
+    // this CTA is a plain shared-memory store, made visible by the CTA barrier
+    // after the round's wait
+    auto push = [&](int t, __int128 x, __int128 xm) {
+        unsigned long long w[4] = {(unsigned long long)x, (unsigned long long)(x >> 64), (unsigned long long)xm,
+                                   (unsigned long long)(xm >> 64)};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            w[k] = __shfl_sync(tm.mask, w[k], tm.base);
+        ulonglong2 *rec2 = xch + ((size_t)((r & 1) * a.G + sidx) * B + t) * 2;
+        const unsigned off = cl_addr(rec2);
+        const unsigned bar = cl_addr(&s_xbar[r & 1]);
+        for (int d = tm.lane; d < a.G; d += lpm) {
+            if (d == sidx) {
+                rec2[0] = make_ulonglong2(w[0], w[1]);
+                rec2[1] = make_ulonglong2(w[2], w[3]);
+            } else {
+                const unsigned ra = cl_map(off, (unsigned)d);
+                const unsigned rbar = cl_map(bar, (unsigned)d);
+                cl_push16(ra, w[0], w[1], rbar);
+                cl_push16(ra + 16, w[2], w[3], rbar);
+            }
+        }
+    };
     while (start < M32) {
         cp_async_wait_all();
         __syncthreads();
@@ -478,12 +602,16 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                         p = fma(lut_select((v >> 6) & 3u, l0, l1, l2, l3), e23.y, p);
                     }
                     p = team_sum_d(p, tm, lpm);
+                    __int128 x = 0;
                     if (tm.lane == 0) {
-                        __int128 x;
                         ok = fx_from_double(p, x);
-                        if (ok)
+                        if (!ok)
+                            x = 0;
+                        else if (!CL)
                             publish(acc, x);
                     }
+                    if (CL)
+                        push(team, x, 0);
                 } else {
                     // A = sum over non-missing of g*eps in double-float: the
                     // products g*hi are exact, each is added with an
@@ -513,16 +641,23 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                     df_add(Ah, Al, A1, L1);
                     team_df_sum(Ah, Al, tm, lpm);
                     team_df_sum(mh, ml, tm, lpm);
+                    __int128 xs = 0, xms = 0;
                     if (tm.lane == 0) {
                         __int128 x1, x2, m1, m2;
                         ok = fx_from_float(Ah, x1) && fx_from_float(Al, x2) && fx_from_float(mh, m1) &&
                              fx_from_float(ml, m2);
                         if (ok) {
-                            publish(acc, x1 + x2);
-                            if (mh != 0.f || ml != 0.f)
-                                publish(acc + 2, m1 + m2);
+                            xs = x1 + x2;
+                            xms = m1 + m2;
+                            if (!CL) {
+                                publish(acc, xs);
+                                if (mh != 0.f || ml != 0.f)
+                                    publish(acc + 2, xms);
+                            }
                         }
                     }
+                    if (CL)
+                        push(team, xs, xms);
                 }
             } else {
                 const int32_t *ro = ring_roff + slot * 8;
@@ -542,15 +677,22 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                             pm += eps64[a.ridx[2][e]];
                         pm = team_sum_d(pm, tm, lpm);
                     }
+                    __int128 xs = 0, xms = 0;
                     if (tm.lane == 0) {
                         __int128 x, xm;
                         ok = fx_from_double(p, x) && fx_from_double(pm, xm);
                         if (ok) {
-                            publish(acc, x);
-                            if (pm != 0.0)
-                                publish(acc + 2, xm);
+                            xs = x;
+                            xms = xm;
+                            if (!CL) {
+                                publish(acc, x);
+                                if (pm != 0.0)
+                                    publish(acc + 2, xm);
+                            }
                         }
                     }
+                    if (CL)
+                        push(team, xs, xms);
                 } else {
                     float h = 0.f, l = 0.f;
                     for (int e = ro[0] + tm.lane; e < ro[1]; e += lpm) {
@@ -570,16 +712,23 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                         }
                         team_df_sum(mh, ml, tm, lpm);
                     }
+                    __int128 xs = 0, xms = 0;
                     if (tm.lane == 0) {
                         __int128 x1, x2, m1, m2;
                         ok = fx_from_float(h, x1) && fx_from_float(l, x2) && fx_from_float(mh, m1) &&
                              fx_from_float(ml, m2);
                         if (ok) {
-                            publish(acc, x1 + x2);
-                            if (mh != 0.f || ml != 0.f)
-                                publish(acc + 2, m1 + m2);
+                            xs = x1 + x2;
+                            xms = m1 + m2;
+                            if (!CL) {
+                                publish(acc, xs);
+                                if (mh != 0.f || ml != 0.f)
+                                    publish(acc + 2, xms);
+                            }
                         }
                     }
+                    if (CL)
+                        push(team, xs, xms);
                 }
             }
             if (!ok)
@@ -590,8 +739,18 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
 
         // ---- grid barrier: one counter; release orders this CTA's
         // accumulator updates (ordered before it by bar.sync), acquire orders
-        // the reads below.  The wait is bounded.
-        if (tid == 0 && !solo) {
+        // the reads below.  The wait is bounded.  Cluster: the round's
+        // mbarrier completes when the other CTAs' records of the nb markers
+        // have landed in this CTA's shared memory (phantom records never arrive).
+        if (CL) {
+            if (tid == 0) {
+                cl_expect(&s_xbar[r & 1], (unsigned)(((a.G - 1) * nb + a.phantom) * 32));
+                if (!cl_wait(&s_xbar[r & 1], (unsigned)(r >> 1) & 1u, a.timeout_ns)) {
+                    atomicCAS(a.err, kDevOk, kDevTimeout);
+                    s_abort = 1;
+                }
+            }
+        } else if (tid == 0 && !solo) {
             red_release_add_u64(a.counter, 1ull);
             const unsigned long long target = (unsigned long long)(a.G + a.phantom) * (unsigned long long)(r + 1);
             const uint64_t t0 = global_timer_ns();
@@ -615,7 +774,25 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         if (tid < nb) {
             const SweepRec &rc = ring_rec[(start + tid) & Rm];
             const unsigned long long *acc = solo ? s_acc + tid * 4 : a.acc + (rb * kMaxSpec + tid) * 4;
-            auto ldacc = [&](int k) -> unsigned long long { return solo ? acc[k] : ld_relaxed_u64(acc + k); };
+            unsigned long long cw[4] = {0ull, 0ull, 0ull, 0ull};
+            if (CL) {
+                // the exact sums over the cluster's CTAs, in the accumulator format
+                __int128 t0 = 0, t1 = 0;
+                const ulonglong2 *xr = xch + ((size_t)(r & 1) * a.G * B + tid) * 2;
+                for (int s = 0; s < a.G; ++s) {
+                    const ulonglong2 w0 = xr[(size_t)s * B * 2], w1 = xr[(size_t)s * B * 2 + 1];
+                    t0 += u128_join(w0.x, w0.y);
+                    t1 += u128_join(w1.x, w1.y);
+                }
+                const Fx f0 = fx_split(t0), f1 = fx_split(t1);
+                cw[0] = (unsigned long long)f0.hi;
+                cw[1] = f0.lo;
+                cw[2] = (unsigned long long)f1.hi;
+                cw[3] = f1.lo;
+            }
+            auto ldacc = [&](int k) -> unsigned long long {
+                return CL ? cw[k] : (solo ? acc[k] : ld_relaxed_u64(acc + k));
+            };
             const double tot = fx_join((long long)ldacc(0), ldacc(1));
             double num;
             if (KIND == kKindDense) {
@@ -680,7 +857,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                     a.comp[rc.j] = c;
             }
             // all CTAs have read the accumulators of round r-1: recycle them
-            if (tid < 4 * kMaxSpec)
+            if (!CL && tid < 4 * kMaxSpec)
                 a.acc[((rb + 2) % 3) * kMaxSpec * 4 + tid] = 0ull;
         }
         if (solo)   // the sampling has read this round's sums (barrier above)
@@ -832,12 +1009,22 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                 a.t_out[1] = global_timer_ns();
         }
     }
+    if (CL)
+        cl_sync_all();   // no CTA exits while another may still store into its shared memory
 }
 
 template <int FORM, int KIND, int KM, bool PROF>
 __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
 {
     sweep_body<FORM, KIND, KM, PROF>(a, (int)blockIdx.x);
+}
+
+// The sweep as one thread-block cluster of G CTAs (the whole grid); the
+// slice of a CTA is its rank in the cluster.
+template <int FORM, int KIND, int KM, bool PROF>
+__global__ void __launch_bounds__(kThreads, 1) k_sweep_cl(SweepArgs a)
+{
+    sweep_body<FORM, KIND, KM, PROF, true>(a, (int)cl_rank());
 }
 
 // Several independent chains of different sizes in one cooperative launch:
@@ -948,12 +1135,53 @@ cudaError_t launch_sweep_stats(int64_t M, const int32_t *group, const int32_t *c
 
 size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a)
 {
-    return make_plan(form, kind, a.slice_max, a.slot_bytes, a.B, a.n_groups).total;
+    return make_plan(form, kind, a.slice_max, a.slot_bytes, a.B, a.n_groups, a.cluster).total;
+}
+
+// Clusters above 8 CTAs are a non-portable size, allowed per kernel.
+static cudaError_t cluster_attrs(const void *f, size_t smem)
+{
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+static cudaLaunchConfig_t cluster_config(int G, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)G);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+template <int FORM, int KIND, int KM>
+static cudaError_t launch_one_cl(const SweepArgs &a, size_t smem, cudaStream_t st)
+{
+    const void *f = a.prof ? (const void *)k_sweep_cl<FORM, KIND, KM, true> : (const void *)k_sweep_cl<FORM, KIND, KM, false>;
+    cudaError_t e = cluster_attrs(f, smem);
+    if (e != cudaSuccess)
+        return e;
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = cluster_config(a.G, smem, st, attr);
+    SweepArgs args = a;
+    void *params[] = {&args};
+    return cudaLaunchKernelExC(&cfg, f, params);
 }
 
 template <int FORM, int KIND, int KM>
 static cudaError_t launch_one(const SweepArgs &a, size_t smem, cudaStream_t st)
 {
+    if (a.cluster > 0)
+        return launch_one_cl<FORM, KIND, KM>(a, smem, st);
     const void *f = a.prof ? (const void *)k_sweep<FORM, KIND, KM, true> : (const void *)k_sweep<FORM, KIND, KM, false>;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
@@ -971,6 +1199,34 @@ static const void *sweep_fn(int form, int kind)
                                   : (const void *)k_sweep<kFormFP64, kKindRagged, KM, PROF>;
     return kind == kKindDense ? (const void *)k_sweep<kFormFP32C, kKindDense, KM, PROF>
                               : (const void *)k_sweep<kFormFP32C, kKindRagged, KM, PROF>;
+}
+
+template <int KM, bool PROF>
+static const void *sweep_cl_fn(int form, int kind)
+{
+    if (form == kFormFP64)
+        return kind == kKindDense ? (const void *)k_sweep_cl<kFormFP64, kKindDense, KM, PROF>
+                                  : (const void *)k_sweep_cl<kFormFP64, kKindRagged, KM, PROF>;
+    return kind == kKindDense ? (const void *)k_sweep_cl<kFormFP32C, kKindDense, KM, PROF>
+                              : (const void *)k_sweep_cl<kFormFP32C, kKindRagged, KM, PROF>;
+}
+
+int sweep_cluster_fits(int form, int kind, int G, size_t smem)
+{
+    int n = 1 << 30;
+    const void *fs[4] = {sweep_cl_fn<4, false>(form, kind), sweep_cl_fn<kMaxK, false>(form, kind),
+                         sweep_cl_fn<4, true>(form, kind), sweep_cl_fn<kMaxK, true>(form, kind)};
+    for (const void *f : fs) {
+        int m = 0;
+        cudaLaunchAttribute attr[1];
+        const cudaLaunchConfig_t cfg = cluster_config(G, smem, nullptr, attr);
+        if (cluster_attrs(f, smem) != cudaSuccess || cudaOccupancyMaxActiveClusters(&m, f, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        n = m < n ? m : n;
+    }
+    return n;
 }
 
 template <int KM>

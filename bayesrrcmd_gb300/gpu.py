@@ -35,7 +35,7 @@ class BrrConfig(C.Structure):
         ("seed", C.c_uint32), ("chain", C.c_uint32),
         ("v0E", C.c_double), ("s02E", C.c_double), ("v0G", C.c_double), ("s02G", C.c_double),
         ("refresh_every", C.c_int32), ("spec_width", C.c_int32), ("grid", C.c_int32), ("device", C.c_int32),
-        ("gram", C.c_int32), ("async_batch", C.c_int32),
+        ("gram", C.c_int32), ("async_batch", C.c_int32), ("cluster", C.c_int32),
     ]
 
 
@@ -195,6 +195,7 @@ class ChainConfig:
     device: int = 0
     gram: int = 0
     async_batch: int = 0
+    cluster: int = 0
 
     def to_c(self) -> BrrConfig:
         c = BrrConfig()
@@ -209,6 +210,7 @@ class ChainConfig:
         c.refresh_every, c.spec_width, c.grid, c.device = self.refresh_every, self.spec_width, self.grid, self.device
         c.gram = self.gram
         c.async_batch = self.async_batch
+        c.cluster = self.cluster
         return c
 
 

@@ -590,6 +590,66 @@ def run_matched_chains(lib, gpu, torch, device, c3_iters, c2_iters):
     return out
 
 
+def run_cluster_compare(lib, gpu, torch, device, steps, warmup):
+    """The restart sweep with its partial sums exchanged through L2 and a
+    grid-wide barrier (one CTA per 64-individual chunk up to one per SM)
+    against the same sweep as one thread-block cluster of 16, 8 or 4 CTAs
+    (exchange through distributed shared memory): C1 dense and C2 ragged, FP64
+    and FP32C forms, per-iteration time and the per-round phase cycles of
+    CTA 0 (one further iteration of the counting variant); C3 dense FP32C for
+    two iterations (grid-wide restart sweep against a cluster of 16)."""
+    def one(d_bed, N, M, y, kind, form, cluster, group=None, S=S1, n_steps=steps, n_warm=warmup, spec=0):
+        ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S, seed=SEED, device=device, gram=-1,
+                                       spec_width=spec,
+                                       refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, cluster=cluster),
+                       lib=lib)
+        ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
+        if group is not None:
+            ch.set_groups(group)
+        ch.set_phenotype(y)
+        ch.init()
+        ch.iterate(n_warm)
+        ch.iterate(n_steps)
+        _, tot, rounds = ch.timing()
+        ch.set_profiling(1)
+        ch.iterate(1)
+        ph = ch.phase_cycles()
+        ch.close()
+        r = max(int(ph[5]), 1)
+        names = ("ring", "dot_products", "exchange_wait", "sampling", "update")
+        return {"ms_per_step": tot / n_steps, "rate": M * n_steps / (tot / 1e3), "rounds_per_step": rounds / n_steps,
+                "cycles_per_round": {k: round(float(ph[i]) / r) for i, k in enumerate(names)}}
+
+    out = {}
+    c1 = synth_parts(torch, gpu, lib, device, C1_N, [(C1_M, 0.05, 0.5)], SEED + 31, 0.0)
+    c1_y, _ = synth_phenotype(gpu, lib, device, c1, C1_N, C1_M, 100, 0.5, SEED + 31)
+    for form, fname in ((gpu.FORM_FP64, "fp64"), (gpu.FORM_FP32C, "fp32c_restart")):
+        out[f"c1_dense_{fname}"] = {f"cluster_{cl}" if cl else "grid": one(c1, C1_N, C1_M, c1_y, gpu.KIND_DENSE, form, cl)
+                                    for cl in (0, 16, 8, 4)}
+    del c1
+    d_bed = synth_parts(torch, gpu, lib, device, R_N, [(R_RARE, 0.001, 0.05), (R_M - R_RARE, 0.05, 0.5)], SEED + 21,
+                        0.01)
+    y, _ = synth_phenotype(gpu, lib, device, d_bed, R_N, R_M, 500, 0.5, SEED + 21)
+    for form, fname in ((gpu.FORM_FP64, "fp64"), (gpu.FORM_FP32C, "fp32c")):
+        out[f"c2_ragged_{fname}"] = {f"cluster_{cl}" if cl else "grid": one(d_bed, R_N, R_M, y, gpu.KIND_RAGGED, form,
+                                                                             cl) for cl in (0, 16, 8, 4)}
+    del d_bed
+    torch.cuda.empty_cache()
+    d_bed, y, group = make_problem(lib, gpu, torch, device, 0)
+    # a cluster CTA holds 6,250 individuals: 16 markers per round keep its
+    # ring of code slices and its residual slice within shared memory
+    out["c3_dense_fp32c_restart"] = {f"cluster_{cl}" if cl else "grid": one(d_bed, N_IND, M_SNP, y, gpu.KIND_DENSE,
+                                                                            gpu.FORM_FP32C, cl, group=group,
+                                                                            S=S_GROUPS, n_steps=2, n_warm=1,
+                                                                            spec=16 if cl else 0)
+                                     for cl in (0, 16)}
+    del d_bed
+    torch.cuda.empty_cache()
+    out["workloads"] = {"c1": "dense, N=2,000 x M=5,000, p~U(0.05,0.5), 100 causal, h2=0.5", "c2": R_WORKLOAD,
+                        "c3": WORKLOAD}
+    return out
+
+
 def run_sample_writer(lib, gpu, torch, device, iters):
     """brr ppbayes on the benchmark workload (N = M = 100,000, two groups,
     FP32C form) from PLINK files: the mean iteration time with no sample
@@ -700,6 +760,9 @@ def main():
     ap.add_argument("--matched-chains", action="store_true",
                     help="only the whole-chain comparisons of the chosen forms with the plain FP64 chain (C3: "
                          "1,000 iterations, burn-in 200; C2: 2,000 iterations, burn-in 500, thin 5)")
+    ap.add_argument("--cluster-compare", action="store_true",
+                    help="only the comparison of the grid-wide restart sweep with its thread-block-cluster variant "
+                         "(C1, C2; C3 for two iterations)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: N=100,000 x M=8,192 (200 MB of codes, above L2), same settings")
     args = ap.parse_args()
@@ -742,6 +805,11 @@ def main():
         sw = run_sample_writer(lib, gpu, torch, device, int(os.environ.get("BRR_SW_ITERS", "60")))
         if rank == 0:
             print(json.dumps({"sample_writer": sw}))
+        return
+    if args.cluster_compare:
+        cc = run_cluster_compare(lib, gpu, torch, device, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps({"cluster_compare": cc}))
         return
     if args.matched_chains:
         mc = run_matched_chains(lib, gpu, torch, device, int(os.environ.get("BRR_C3_ITERS", "1000")),

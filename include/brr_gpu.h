@@ -115,6 +115,11 @@ typedef struct brr_config {
                                   (src/parallelgraph.cpp:51-150): the T markers of a batch all read
                                   the residual before any of them updates it, acum is not written
                                   (src/BayesRBase.cpp:394-524); FP64 form only */
+    int32_t cluster;           /* 0: the restart sweep exchanges its partial sums through L2 across `grid`
+                                  CTAs with a grid-wide barrier; C in 2..16: the restart sweep runs as
+                                  one thread-block cluster of C CTAs, each holding its slice of the
+                                  residual in shared memory and storing its partial sums into every
+                                  CTA's shared memory (no Gram-blocked form; gram must not be 1) */
 } brr_config;
 
 /* Chain state; arrays are caller-owned, sized M (beta, comp, acum) and N (eps).

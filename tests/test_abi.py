@@ -69,6 +69,11 @@ def test_invalid_config_rejected():
     assert lib.brr_ctx_create(C.byref(bad), C.byref(h)) == -1
     bad = gpu.ChainConfig(N=10, M=5, spec_width=12).to_c()
     assert lib.brr_ctx_create(C.byref(bad), C.byref(h)) == -1
+    # the cluster sweep: 2..16 CTAs, and it is the restart sweep
+    for kw in (dict(cluster=1), dict(cluster=17), dict(cluster=-2), dict(cluster=8, gram=1)):
+        bad = gpu.ChainConfig(N=10, M=5, **kw).to_c()
+        assert lib.brr_ctx_create(C.byref(bad), C.byref(h)) == -1, kw
+        assert b"cluster" in lib.brr_last_error()
 
 
 def test_batch_config_rejected_before_the_device():
