@@ -60,7 +60,7 @@ def build_gpu(verbose: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     if _stale(LIB, objs):
-        cmd = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lcublas"]
+        cmd = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lcublas", "-lcublasLt"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libbrr_gpu.so failed:\n{r.stdout}\n{r.stderr}")

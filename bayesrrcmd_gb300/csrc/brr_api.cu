@@ -1375,6 +1375,24 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
     return BRR_OK;
 }
 
+int brr_get_gram_entries(brr_ctx *ctx, const int64_t *j, const int64_t *k, int64_t n, double *out)
+{
+    if (!ctx || !j || !k || !out || n < 0)
+        return fail(BRR_ERR_ARG, "null argument");
+    if (!ctx->d_gram)
+        return fail(BRR_ERR_ARG, "the chain holds no marker Gram");
+    const int64_t M = ctx->cfg.M;
+    for (int64_t i = 0; i < n; ++i)
+        if (!(j[i] > k[i] && k[i] >= 0 && j[i] < M))
+            return fail(BRR_ERR_ARG, "Gram entries need M > j > k >= 0");
+    BRR_CUDA(cudaSetDevice(ctx->dev));
+    BRR_CUDA(cudaStreamSynchronize(ctx->st));
+    for (int64_t i = 0; i < n; ++i)
+        BRR_CUDA(cudaMemcpy(out + i, ctx->d_gram + j[i] * (j[i] - 1) / 2 + k[i], sizeof(double),
+                            cudaMemcpyDeviceToHost));
+    return BRR_OK;
+}
+
 int brr_set_profiling(brr_ctx *ctx, int32_t on)
 {
     if (!ctx || on < 0 || on > 2)

@@ -10,9 +10,13 @@
 //   P = g_j . g_k,  Q_jk = g_j . m_k,  R = m_j . m_k
 // (missing genotypes take the value (mean - colmean) * sigma, which is zero up
 // to the rounding of the two means and is left out).  P, Q, R are integer
-// sums below 2^24, computed exactly by BF16 GEMMs with FP32 accumulation
-// (cuBLAS, a plain library GEMM) on tiles of markers; the FP64 combination runs
-// in k_gram_combine.
+// sums below 2^24.  They come from FP8 (E4M3, in which 0, 1 and 2 are exact)
+// GEMMs with FP32 accumulation on tiles of 8,192 markers (cuBLASLt, a plain
+// library GEMM); every product and partial sum is an integer below 2^24, so
+// the FP32 results are exact.  Where the library offers no FP8 algorithm for
+// the shapes the build uses BF16 GEMMs instead.  The FP64 combination runs in
+// k_gram_combine, one CTA row per marker j of the tile.
+#include <cublasLt.h>
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
 
@@ -24,86 +28,217 @@
 
 namespace brr {
 
-// Rows [m0, m0+mt) of the genotype matrix as BF16 (row length npad, padding
-// zero), and optionally the non-missing indicator.
-__global__ void k_decode_bf16(const uint8_t *__restrict__ codes, int64_t col_stride, int64_t N, int64_t npad,
-                              int64_t m0, int64_t mt, __nv_bfloat16 *__restrict__ gp, __nv_bfloat16 *__restrict__ nm)
+
+// Per-marker constants of the combination: s_k, s_k c_k and, without missing
+// genotypes, w_k = s_k (q_k - c_k N) with q_k = sum of g_k; q_k itself.
+__global__ void k_gram_consts(int64_t M, int64_t N, const double *__restrict__ scale,
+                              const int64_t *__restrict__ counts, double *__restrict__ cst)
 {
-    const int64_t total = mt * (npad / 4);
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M)
+        return;
+    const double sk = scale[2 * k], ck = scale[2 * k + 1];
+    const double qk = (double)(counts[4 * k + 1] + 2 * counts[4 * k + 2]);
+    cst[4 * k] = sk;
+    cst[4 * k + 1] = sk * ck;
+    cst[4 * k + 2] = sk * (qk - ck * (double)N);
+    cst[4 * k + 3] = qk;
+}
+
+// Rows j in [j0, j0+tj) (one per blockIdx.y) and columns k in [k0, k0+tk),
+// k < j, of the tile.  The products are stored column-major with the k index
+// fastest: X[(j - j0) * ldp + (k - k0)].
+//   no missing genotypes: G = s_j (s_k P - (s_k c_k q_j + c_j w_k))
+//   otherwise:            G = s_j (s_k P - s_k c_k Q1 - c_j s_k Q2 + c_j s_k c_k R)
+__global__ void k_gram_combine(int64_t j0, int64_t k0, int64_t tk, int64_t ldp, const float *__restrict__ P,
+                               const float *__restrict__ Q1, const float *__restrict__ Q2,
+                               const float *__restrict__ R, const double *__restrict__ cst,
+                               const double *__restrict__ scale, double *__restrict__ G)
+{
+    const int64_t a = blockIdx.y;
+    const int64_t j = j0 + a;
+    const int64_t kend = j - k0 < tk ? j - k0 : tk;
+    if (kend <= 0)
+        return;
+    const double sj = scale[2 * j], cj = scale[2 * j + 1];
+    const double qj = cst[4 * j + 3];
+    const float *Prow = P + a * ldp;
+    double *Grow = G + j * (j - 1) / 2 + k0;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < kend; b += (int64_t)gridDim.x * blockDim.x) {
+        const double *ck4 = cst + 4 * (k0 + b);
+        const double sk = ck4[0], skck = ck4[1];
+        double inner;
+        if (Q1) {
+            const int64_t e = a * ldp + b;
+            inner = ((sk * (double)Prow[b] - skck * (double)Q1[e]) - cj * (sk * (double)Q2[e])) +
+                    cj * (skck * (double)R[e]);
+        } else {
+            inner = sk * (double)Prow[b] - fma(skck, qj, cj * ck4[2]);
+        }
+        Grow[b] = sj * inner;
+    }
+}
+
+// Rows [0, M) of the genotype matrix as FP8 E4M3 bytes (row length npad, a
+// multiple of 16, padding zero) and optionally the non-missing indicator; one
+// thread per 16 individuals (four code bytes in, 16 bytes out).
+__global__ void k_decode_fp8(const uint8_t *__restrict__ codes, int64_t col_stride, int64_t N, int64_t npad,
+                             int64_t M, uint8_t *__restrict__ gp, uint8_t *__restrict__ nm)
+{
+    const int64_t groups = npad / 16;
+    const int64_t total = M * groups;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / groups;
+        const int64_t q = e - r * groups;
+        const uint32_t v = *reinterpret_cast<const uint32_t *>(codes + r * col_stride + 4 * q);
+        uint32_t g[4], m[4];
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            uint32_t gw = 0, mw = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const unsigned c = (v >> (8 * w + 2 * k)) & 3u;
+                const bool valid = 16 * q + 4 * w + k < N;
+                // code 0: genotype 2 (E4M3 0x40), code 2: genotype 1 (0x38), code 3: 0, code 1: missing
+                const uint32_t gb = !valid ? 0u : (c == 0u ? 0x40u : (c == 2u ? 0x38u : 0u));
+                const uint32_t mb = (valid && c != 1u) ? 0x38u : 0u;
+                gw |= gb << (8 * k);
+                mw |= mb << (8 * k);
+            }
+            g[w] = gw;
+            m[w] = mw;
+        }
+        reinterpret_cast<uint4 *>(gp + r * npad)[q] = make_uint4(g[0], g[1], g[2], g[3]);
+        if (nm)
+            reinterpret_cast<uint4 *>(nm + r * npad)[q] = make_uint4(m[0], m[1], m[2], m[3]);
+    }
+}
+
+// Rows [0, M) of the genotype matrix as BF16 (row length npad, padding zero),
+// and optionally the non-missing indicator.
+__global__ void k_decode_bf16(const uint8_t *__restrict__ codes, int64_t col_stride, int64_t N, int64_t npad,
+                              int64_t M, __nv_bfloat16 *__restrict__ gp, __nv_bfloat16 *__restrict__ nm)
+{
+    const int64_t total = M * (npad / 4);
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = e / (npad / 4);
         const int64_t b = e - r * (npad / 4);
-        const unsigned v = (4 * b < N) ? codes[(m0 + r) * col_stride + b] : 0x55u;
-        __nv_bfloat16 g4[4], m4[4];
+        const unsigned v = (4 * b < N) ? codes[r * col_stride + b] : 0x55u;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const unsigned c = (v >> (2 * k)) & 3u;
             const bool valid = 4 * b + k < N;
             const float g = (!valid || c == 1u) ? 0.f : (c == 0u ? 2.f : (c == 2u ? 1.f : 0.f));
-            g4[k] = __float2bfloat16(g);
-            m4[k] = __float2bfloat16((valid && c != 1u) ? 1.f : 0.f);
-        }
-        const int64_t o = r * npad + 4 * b;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            gp[o + k] = g4[k];
-        if (nm) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                nm[o + k] = m4[k];
+            gp[r * npad + 4 * b + k] = __float2bfloat16(g);
+            if (nm)
+                nm[r * npad + 4 * b + k] = __float2bfloat16((valid && c != 1u) ? 1.f : 0.f);
         }
     }
 }
 
-// Tile (rows j in [j0, j0+tj), columns k in [k0, k0+tk)) of the products, each
-// stored column-major with the k index fastest: X[(j - j0) * tk + (k - k0)].
-__global__ void k_gram_combine(int64_t j0, int64_t tj, int64_t k0, int64_t tk, const float *__restrict__ P,
-                               const float *__restrict__ Q1, const float *__restrict__ Q2, const float *__restrict__ R,
-                               const double *__restrict__ scale, const int64_t *__restrict__ counts, int64_t N,
-                               double *__restrict__ G)
-{
-    const int64_t total = tj * tk;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t a = e / tk, b = e - a * tk;
-        const int64_t j = j0 + a, k = k0 + b;
-        if (k >= j)
-            continue;
-        const double sj = scale[2 * j], cj = scale[2 * j + 1];
-        const double sk = scale[2 * k], ck = scale[2 * k + 1];
-        double q1, q2, r;
-        if (Q1) {
-            q1 = (double)Q1[e];
-            q2 = (double)Q2[e];
-            r = (double)R[e];
-        } else {
-            q1 = (double)(counts[4 * j + 1] + 2 * counts[4 * j + 2]);
-            q2 = (double)(counts[4 * k + 1] + 2 * counts[4 * k + 2]);
-            r = (double)N;
-        }
-        const double inner = (((double)P[e] - ck * q1) - cj * q2) + (cj * ck) * r;
-        G[j * (j - 1) / 2 + k] = (sj * sk) * inner;
+namespace {
+
+constexpr int64_t kTile = 8192;
+constexpr size_t kLtWorkspace = (size_t)64 << 20;
+
+inline int64_t round16(int64_t x) { return (x + 15) / 16 * 16; }
+
+// FP8 GEMMs through cuBLASLt: out (tk x tj, column-major, k fastest, leading
+// dimension ld) = A(rows k0..) * B(rows j0..)^T over the npad-long rows.
+struct Fp8Gemm {
+    cublasLtHandle_t h = nullptr;
+    cublasLtMatmulDesc_t op = nullptr;
+    cublasLtMatmulPreference_t pref = nullptr;
+    void *ws = nullptr;
+    int64_t npad = 0;
+
+    bool init(int64_t np)
+    {
+        npad = np;
+        const cublasOperation_t ta = CUBLAS_OP_T, tb = CUBLAS_OP_N;
+        size_t wsb = kLtWorkspace;
+        return cublasLtCreate(&h) == CUBLAS_STATUS_SUCCESS &&
+               cublasLtMatmulDescCreate(&op, CUBLAS_COMPUTE_32F, CUDA_R_32F) == CUBLAS_STATUS_SUCCESS &&
+               cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)) ==
+                   CUBLAS_STATUS_SUCCESS &&
+               cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)) ==
+                   CUBLAS_STATUS_SUCCESS &&
+               cublasLtMatmulPreferenceCreate(&pref) == CUBLAS_STATUS_SUCCESS &&
+               cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &wsb,
+                                                    sizeof(wsb)) == CUBLAS_STATUS_SUCCESS &&
+               cudaMalloc(&ws, kLtWorkspace) == cudaSuccess;
     }
-}
+    // 0: done; 1: no algorithm for the shape (nothing launched); -1: error.
+    // With A, B null: only the query for an algorithm.
+    int run(const uint8_t *A, const uint8_t *B, int64_t tk, int64_t tj, int64_t ld, float *out, cudaStream_t st)
+    {
+        cublasLtMatrixLayout_t la = nullptr, lb = nullptr, lc = nullptr;
+        int rc = -1;
+        if (cublasLtMatrixLayoutCreate(&la, CUDA_R_8F_E4M3, npad, tk, npad) == CUBLAS_STATUS_SUCCESS &&
+            cublasLtMatrixLayoutCreate(&lb, CUDA_R_8F_E4M3, npad, tj, npad) == CUBLAS_STATUS_SUCCESS &&
+            cublasLtMatrixLayoutCreate(&lc, CUDA_R_32F, tk, tj, ld) == CUBLAS_STATUS_SUCCESS) {
+            cublasLtMatmulHeuristicResult_t hr{};
+            int n = 0;
+            if (cublasLtMatmulAlgoGetHeuristic(h, op, la, lb, lc, lc, pref, 1, &hr, &n) != CUBLAS_STATUS_SUCCESS ||
+                n < 1) {
+                rc = 1;
+            } else if (!A || !B) {
+                rc = 0;
+            } else {
+                const float one = 1.f, zero = 0.f;
+                rc = cublasLtMatmul(h, op, &one, A, la, B, lb, &zero, out, lc, out, lc, &hr.algo, ws, kLtWorkspace,
+                                    st) == CUBLAS_STATUS_SUCCESS
+                         ? 0
+                         : -1;
+            }
+        }
+        if (la)
+            cublasLtMatrixLayoutDestroy(la);
+        if (lb)
+            cublasLtMatrixLayoutDestroy(lb);
+        if (lc)
+            cublasLtMatrixLayoutDestroy(lc);
+        return rc;
+    }
+    ~Fp8Gemm()
+    {
+        if (pref)
+            cublasLtMatmulPreferenceDestroy(pref);
+        if (op)
+            cublasLtMatmulDescDestroy(op);
+        if (h)
+            cublasLtDestroy(h);
+        cudaFree(ws);
+    }
+};
+
+}  // namespace
 
 cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work)
 {
-    const int64_t npad = ((N + 7) / 8) * 8;
-    const int64_t T = std::min<int64_t>(M, 8192);
+    const int64_t npad = round16(N);
+    const int64_t T = round16(std::min<int64_t>(M, kTile));
     *gram = (size_t)(M * (M - 1) / 2) * sizeof(double);
-    *work = (size_t)M * npad * 2 * (missing ? 2 : 1) + (size_t)T * T * 4 * (missing ? 4 : 1);
+    // the BF16 route's rows (2 bytes per genotype) bound the FP8 route's (1 byte)
+    *work = (size_t)round16(M) * npad * 2 * (missing ? 2 : 1) + (size_t)T * T * 4 * (missing ? 4 : 1) +
+            (size_t)M * 32 + kLtWorkspace;
     return cudaSuccess;
 }
 
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
                const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why, float *device_ms)
 {
-    const int64_t npad = ((N + 7) / 8) * 8;
-    const int64_t T = std::min<int64_t>(M, 8192);
-    __nv_bfloat16 *gp = nullptr, *nm = nullptr;
+    // FP8 rows and tile sides are multiples of 16 (padding rows and columns
+    // are zero and their products are not read)
+    const int64_t npad = round16(N);
+    const int64_t Mp = round16(M);
+    const int64_t T = std::min<int64_t>(M, kTile);
+    const int64_t Tp = round16(T);
+    void *gp = nullptr, *nm = nullptr;
     float *tiles = nullptr;
-    cublasHandle_t h = nullptr;
+    double *cst = nullptr;
     int rc = 0;
     auto cu = [&](cudaError_t e, const char *what) {
         if (e != cudaSuccess && rc == 0) {
@@ -111,39 +246,84 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
             rc = -1;
         }
     };
-    cu(cudaMalloc(&gp, sizeof(__nv_bfloat16) * (size_t)M * npad), "allocation of the BF16 genotypes");
-    if (missing)
-        cu(cudaMalloc(&nm, sizeof(__nv_bfloat16) * (size_t)M * npad), "allocation of the indicators");
-    cu(cudaMalloc(&tiles, sizeof(float) * (size_t)T * T * (missing ? 4 : 1)), "allocation of the product tiles");
-    if (rc == 0 && cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) {
-        why = "cublasCreate failed";
-        rc = -1;
-    }
-    if (rc == 0)
-        cublasSetStream(h, st);
     cudaEvent_t ev[2] = {nullptr, nullptr};
-    if (rc == 0) {
-        cu(cudaEventCreate(&ev[0]), "event");
-        cu(cudaEventCreate(&ev[1]), "event");
-    }
+    cu(cudaEventCreate(&ev[0]), "event");
+    cu(cudaEventCreate(&ev[1]), "event");
+    cu(cudaMalloc(&tiles, sizeof(float) * (size_t)Tp * Tp * (missing ? 4 : 1)), "allocation of the product tiles");
+    cu(cudaMalloc(&cst, sizeof(double) * 4 * (size_t)M), "allocation of the per-marker constants");
+    float *P = tiles, *Q1 = missing ? tiles + (size_t)Tp * Tp : nullptr,
+          *Q2 = missing ? tiles + 2 * (size_t)Tp * Tp : nullptr, *R = missing ? tiles + 3 * (size_t)Tp * Tp : nullptr;
+
+    // the FP8 route when the library has an algorithm for the full tile
+    Fp8Gemm f8;
+    bool fp8 = rc == 0 && f8.init(npad);
     if (rc == 0)
         cu(cudaEventRecord(ev[0], st), "event");
+    if (fp8) {
+        cu(cudaMalloc(&gp, (size_t)Mp * npad), "allocation of the FP8 genotypes");
+        if (missing)
+            cu(cudaMalloc(&nm, (size_t)Mp * npad), "allocation of the FP8 indicators");
+        if (rc == 0) {
+            cu(cudaMemsetAsync(gp, 0, (size_t)Mp * npad, st), "clear");
+            if (nm)
+                cu(cudaMemsetAsync(nm, 0, (size_t)Mp * npad, st), "clear");
+        }
+        // an algorithm for every tile shape of the build: full tiles and the last
+        for (int64_t a = 0; a < 2 && fp8; ++a)
+            for (int64_t b = 0; b < 2 && fp8; ++b) {
+                const int64_t sa = a ? round16(M - (M - 1) / T * T) : Tp, sb = b ? round16(M - (M - 1) / T * T) : Tp;
+                fp8 = f8.run(nullptr, nullptr, sa, sb, Tp, P, st) == 0;
+            }
+        if (!fp8) {
+            cudaFree(gp);
+            cudaFree(nm);
+            gp = nm = nullptr;
+        }
+    }
+    if (!fp8) {
+        cu(cudaMalloc(&gp, sizeof(__nv_bfloat16) * (size_t)Mp * npad), "allocation of the BF16 genotypes");
+        if (missing)
+            cu(cudaMalloc(&nm, sizeof(__nv_bfloat16) * (size_t)Mp * npad), "allocation of the BF16 indicators");
+        if (rc == 0) {
+            cu(cudaMemsetAsync(gp, 0, sizeof(__nv_bfloat16) * (size_t)Mp * npad, st), "clear");
+            if (nm)
+                cu(cudaMemsetAsync(nm, 0, sizeof(__nv_bfloat16) * (size_t)Mp * npad, st), "clear");
+        }
+    }
+    cublasHandle_t hb = nullptr;
+    if (rc == 0 && !fp8) {
+        if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) {
+            why = "cublasCreate failed";
+            rc = -1;
+        } else {
+            cublasSetStream(hb, st);
+        }
+    }
     if (rc == 0) {
-        k_decode_bf16<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, 0, M, gp, nm);
+        if (fp8)
+            k_decode_fp8<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, M, (uint8_t *)gp, (uint8_t *)nm);
+        else
+            k_decode_bf16<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, M, (__nv_bfloat16 *)gp,
+                                                  (__nv_bfloat16 *)nm);
         cu(cudaGetLastError(), "decode");
+        k_gram_consts<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(M, N, scale, counts, cst);
+        cu(cudaGetLastError(), "constants");
     }
     const float one = 1.f, zero = 0.f;
-    float *P = tiles, *Q1 = missing ? tiles + (size_t)T * T : nullptr, *Q2 = missing ? tiles + 2 * (size_t)T * T : nullptr,
-          *R = missing ? tiles + 3 * (size_t)T * T : nullptr;
-    // out (tk x tj, column-major, k fastest) = A(rows k) * B(rows j)^T over the N axis
-    auto gemm = [&](const __nv_bfloat16 *A, const __nv_bfloat16 *B, int64_t k0, int64_t tk, int64_t j0, int64_t tj,
-                    float *out) {
+    auto gemm = [&](const void *A, const void *B, int64_t k0, int64_t tk, int64_t j0, int64_t tj, float *out) {
         if (rc)
             return;
-        const cublasStatus_t s =
-            cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, (int)tk, (int)tj, (int)npad, &one, A + k0 * npad, CUDA_R_16BF,
-                         (int)npad, B + j0 * npad, CUDA_R_16BF, (int)npad, &zero, out, CUDA_R_32F, (int)tk,
-                         CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+        if (fp8) {
+            if (f8.run((const uint8_t *)A + k0 * npad, (const uint8_t *)B + j0 * npad, tk, tj, Tp, out, st) != 0) {
+                why = "cuBLASLt FP8 GEMM failed";
+                rc = -1;
+            }
+            return;
+        }
+        const cublasStatus_t s = cublasGemmEx(hb, CUBLAS_OP_T, CUBLAS_OP_N, (int)tk, (int)tj, (int)npad, &one,
+                                              (const __nv_bfloat16 *)A + k0 * npad, CUDA_R_16BF, (int)npad,
+                                              (const __nv_bfloat16 *)B + j0 * npad, CUDA_R_16BF, (int)npad, &zero,
+                                              out, CUDA_R_32F, (int)Tp, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
         if (s != CUBLAS_STATUS_SUCCESS) {
             why = "cublasGemmEx failed (" + std::to_string((int)s) + ")";
             rc = -1;
@@ -153,14 +333,17 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
         const int64_t tj = std::min<int64_t>(T, M - j0);
         for (int64_t k0 = 0; k0 <= j0 && rc == 0; k0 += T) {
             const int64_t tk = std::min<int64_t>(T, M - k0);
-            gemm(gp, gp, k0, tk, j0, tj, P);            // P[j,k]  = g_j . g_k
+            // FP8 sides rounded up to 16 (rows up to Mp exist and are zero)
+            const int64_t gk = fp8 ? round16(tk) : tk, gj = fp8 ? round16(tj) : tj;
+            gemm(gp, gp, k0, gk, j0, gj, P);             // P[j,k]  = g_j . g_k
             if (missing) {
-                gemm(nm, gp, k0, tk, j0, tj, Q1);       // Q1[j,k] = g_j . m_k
-                gemm(gp, nm, k0, tk, j0, tj, Q2);       // Q2[j,k] = m_j . g_k
-                gemm(nm, nm, k0, tk, j0, tj, R);        // R[j,k]  = m_j . m_k
+                gemm(nm, gp, k0, gk, j0, gj, Q1);        // Q1[j,k] = g_j . m_k
+                gemm(gp, nm, k0, gk, j0, gj, Q2);        // Q2[j,k] = m_j . g_k
+                gemm(nm, nm, k0, gk, j0, gj, R);         // R[j,k]  = m_j . m_k
             }
             if (rc == 0) {
-                k_gram_combine<<<152 * 8, 256, 0, st>>>(j0, tj, k0, tk, P, Q1, Q2, R, scale, counts, N, G);
+                const dim3 grid((unsigned)((tk + 1023) / 1024), (unsigned)tj);
+                k_gram_combine<<<grid, 256, 0, st>>>(j0, k0, tk, Tp, P, Q1, Q2, R, cst, scale, G);
                 cu(cudaGetLastError(), "combine");
             }
         }
@@ -173,11 +356,12 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     for (cudaEvent_t e : ev)
         if (e)
             cudaEventDestroy(e);
-    if (h)
-        cublasDestroy(h);
+    if (hb)
+        cublasDestroy(hb);
     cudaFree(gp);
     cudaFree(nm);
     cudaFree(tiles);
+    cudaFree(cst);
     return rc;
 }
 

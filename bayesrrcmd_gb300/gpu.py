@@ -63,6 +63,7 @@ EXPORTS = [
     "brr_iterate", "brr_sweep", "brr_get_state", "brr_set_state", "brr_refresh_eps", "brr_get_timing", "brr_get_phase_cycles",
     "brr_set_wait_limit", "brr_set_profiling", "brr_xbeta", "brr_synth_bed_device", "brr_xbeta_noalloc",
     "brr_get_gram_info",
+    "brr_get_gram_entries",
     "brr_batch_create", "brr_batch_destroy", "brr_batch_pack_bed", "brr_batch_pack_bed_device",
     "brr_batch_set_groups", "brr_batch_set_phenotypes", "brr_batch_init", "brr_batch_iterate",
     "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_set_profiling",
@@ -108,6 +109,8 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_get_sweep_timeline.argtypes = [P, C.POINTER(C.c_uint64), C.c_int64, C.POINTER(C.c_int32),
                                            C.POINTER(C.c_int32)]
     lib.brr_get_gram_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.brr_get_gram_entries.argtypes = [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int64,
+                                         C.POINTER(C.c_double)]
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
     lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
@@ -356,6 +359,14 @@ class Chain:
         it, ctas = C.c_int32(), C.c_int32()
         self._check(self.lib.brr_get_sweep_timeline(self.h, _ptr(buf, C.c_uint64), n, C.byref(it), C.byref(ctas)))
         return buf[:it.value * ctas.value * ev].reshape(it.value, ctas.value, ev).copy()
+
+    def gram_entries(self, j, k) -> np.ndarray:
+        j = np.ascontiguousarray(j, np.int64)
+        k = np.ascontiguousarray(k, np.int64)
+        out = np.zeros(j.size, np.float64)
+        self._check(self.lib.brr_get_gram_entries(self.h, _ptr(j, C.c_int64), _ptr(k, C.c_int64), j.size,
+                                                  _ptr(out, C.c_double)))
+        return out
 
     def gram_info(self):
         b, ms, n = C.c_int32(), C.c_double(), C.c_int64()

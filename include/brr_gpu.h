@@ -53,6 +53,7 @@
  *                         device, a data source for benchmarks
  *   brr_set_wait_limit,   no counterpart: limits of the device-side waits, the
  *   brr_get_gram_info,    marker Gram of the blocked sweep, and phase counters
+ *   brr_get_gram_entries,
  *   brr_get_phase_cycles, (the device counterpart of the timing log above)
  *   brr_set_profiling
  *   brr_batch_*,          no single counterpart: each chain (instance) is
@@ -239,6 +240,10 @@ int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arriva
  * building the packed marker Gram (ms: decode, GEMMs and combine, without the
  * allocations and the library's initialisation) and its size in bytes. */
 int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes);
+
+/* Entries G[j[i], k[i]] = x_j . x_k (j > k) of the marker Gram of a blocked
+ * chain, for i < n, into out (a check of the build; one copy per entry). */
+int brr_get_gram_entries(brr_ctx *ctx, const int64_t *j, const int64_t *k, int64_t n, double *out);
 
 /* ---- Batched chains on shared genotypes (the C4 batching form) -------------
  * C = 32 or 64 chains with distinct seeds (chain ids cfg.chain .. cfg.chain+C-1)
