@@ -445,6 +445,7 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     a.tline = c->profile && c->timeline && c->G <= c->sms ? c->d_tline : nullptr;
     a.async_batch = cf.async_batch;
     a.cluster = cf.cluster > 0 && c->G > 1 ? c->G : 0;
+    a.pairs = c->pair_rounds ? c->d_acc + kPairOffset : nullptr;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
     a.gram = c->d_gram;
@@ -978,6 +979,19 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     a.slice_max = c.slice_max;
     a.slot_bytes = c.slot_bytes;
     a.cluster = cf.cluster > 0 && c.G > 1 ? c.G : 0;
+    // FP32C ragged markers resolve whole rounds with pair terms when the round
+    // is one warp wide and the slice's code map fits beside the ring
+    c.pair_rounds = cf.form == BRR_FORM_FP32C && c.kind == BRR_KIND_RAGGED && !c.eigen && c.B <= 32 &&
+                    cf.gram >= 0 && a.cluster == 0 && cf.async_batch == 0 && cf.N < (1 << 24);
+    if (c.pair_rounds) {
+        a.pairs = c.d_acc + kPairOffset;
+        const size_t sp = sweep_smem_bytes(cf.form, c.kind, a);
+        const int per = sp <= (size_t)200 * 1024 ? sweep_max_ctas_per_sm(cf.form, c.kind, sp, true) : 0;
+        if (per < 1 || (int64_t)per * c.sms < c.G) {
+            c.pair_rounds = false;
+            a.pairs = nullptr;
+        }
+    }
     const size_t smem = sweep_smem_bytes(cf.form, c.kind, a);
     if (a.cluster > 0) {
         if (sweep_cluster_fits(cf.form, c.kind, c.G, smem) < 1)
@@ -986,7 +1000,7 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
         c.packed = true;
         return BRR_OK;
     }
-    const int per_sm = sweep_max_ctas_per_sm(cf.form, c.kind, smem);
+    const int per_sm = sweep_max_ctas_per_sm(cf.form, c.kind, smem, c.pair_rounds);
     if (per_sm < 1 || (int64_t)per_sm * c.sms < c.G)
         return fail(BRR_ERR_ARG, "the sweep kernel does not fit " + std::to_string(c.G) +
                                      " co-resident CTAs (shared memory " + std::to_string(smem) + " bytes)");
@@ -1367,7 +1381,7 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
     if (!ctx)
         return fail(BRR_ERR_ARG, "null context");
     if (blocked)
-        *blocked = ctx->blocked ? 1 : 0;
+        *blocked = ctx->blocked || ctx->pair_rounds ? 1 : 0;
     if (build_ms)
         *build_ms = ctx->gram_ms;
     if (bytes)

@@ -97,6 +97,9 @@ struct SweepArgs {
     int async_batch;             // restart sweep: 0 synchronous; T > 0 asynchronous batches of T markers
     int cluster;                 // restart sweep: 0 grid-wide exchange; G: the G CTAs are one thread-block
                                  // cluster exchanging through distributed shared memory
+    unsigned long long *pairs;   // pair-resolved ragged rounds: [3][32][32] integer pair terms of the
+                                 // round's markers, A in the low and Bm in the high word (zero at
+                                 // launch), else null
     unsigned long long *tline;   // blocked sweep, counting variant, optional: per-CTA event timeline
                                  // [kTimelineIters][G][kTimelineEvents] of global-timer stamps (ns)
 };
@@ -240,7 +243,7 @@ cudaError_t noalloc_xbeta(cudaStream_t st, int kind, int64_t N, const uint8_t *c
                           const double *table, const uint32_t *idx, const double *b, int64_t n, double *d_out,
                           std::string &why);
 bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string &why);
-int sweep_max_ctas_per_sm(int form, int kind, size_t smem);
+int sweep_max_ctas_per_sm(int form, int kind, size_t smem, bool pair_rounds = false);
 // Clusters of G CTAs of the cluster sweep that can be resident at once (0: none).
 int sweep_cluster_fits(int form, int kind, int G, size_t smem);
 size_t sweep_block_smem_bytes(const SweepArgs &a);

@@ -18,6 +18,15 @@
 // the next round starts right after it.  Every sampled marker therefore sees
 // exactly the residual of the sequential chain.
 //
+// Pair-resolved ragged rounds (FP32C, ragged markers): a round resolves all its
+// B <= 32 markers.  Besides the dot products, every CTA sums over its slice the
+// integer pair terms A[p][t] = sum_i g_p(i) g_t(i) and Bm[p][t] = sum over the
+// individuals missing at p of g_t(i) for p < t, by population counts of the
+// markers' bit masks (ones, twos, missing) over the slice; after a change at marker p the
+// later markers' num move by the exact linear correction these terms give, and
+// every changing marker's residual update is applied in order at the end of the
+// round.
+//
 // The cluster variant runs the same sweep as one thread-block cluster of up to
 // 16 CTAs: each CTA stores its partial sums straight into every CTA's shared
 // memory (distributed shared memory, st.async completing on the receiver's
@@ -186,13 +195,18 @@ struct SmemPlan {
     size_t gcf;             // FP32C: FP32 sampler constants, n_groups x kMaxK x 2 floats
     size_t gtab;            // FP32C dense: 256 float4 + 256 bytes
     size_t xch;             // cluster: [2][cluster][B] exchange records of 32 bytes
+    size_t gmap;            // pair-resolved rounds: [slice_max][32] codes of the round's markers
+    size_t bmask;           // pair-resolved rounds: [3][slice_max / 32][32] bit masks of the round's markers
+    size_t pterm;           // pair-resolved rounds: [32][32] pair terms of the round
+    size_t gdfo;            // pair-resolved rounds: n_groups x kMaxK x {sd_k, 1/den_k} double-float
     size_t total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 __host__ __device__ inline SmemPlan make_plan(int form, int kind, int slice_max, int slot_bytes, int B, int n_groups,
-                                              int cluster = 0, size_t rec_bytes = sizeof(SweepRec))
+                                              int cluster = 0, bool pair_rounds = false,
+                                              size_t rec_bytes = sizeof(SweepRec))
 {
     SmemPlan p;
     const int R = 4 * B;
@@ -223,6 +237,18 @@ __host__ __device__ inline SmemPlan make_plan(int form, int kind, int slice_max,
     o = align16(o);
     p.xch = o;
     o += (size_t)2 * cluster * B * 32;
+    p.gmap = o;
+    if (pair_rounds)
+        o += align16((size_t)slice_max * 32);
+    p.bmask = o;
+    if (pair_rounds)
+        o += align16((size_t)3 * 32 * (slice_max / 32) * sizeof(unsigned));
+    p.pterm = o;
+    if (pair_rounds)
+        o += 32 * 32 * sizeof(unsigned long long);
+    p.gdfo = o;
+    if (pair_rounds)
+        o += align16((size_t)n_groups * kMaxK * 4 * sizeof(float));
     p.total = align16(o);
     return p;
 }
@@ -347,14 +373,19 @@ __device__ __forceinline__ __int128 u128_join(unsigned long long lo, unsigned lo
 // variant that counts phase cycles on the first CTA (the plain variant reads no
 // clock, whose reads would constrain the scheduling of every CTA's code).
 // CL: the G CTAs are one thread-block cluster and exchange the round's partial
-// sums through distributed shared memory (k_sweep_cl).
-template <int FORM, int KIND, int KM, bool PROF, bool CL = false>
+// sums through distributed shared memory (k_sweep_cl).  PR: pair-resolved
+// rounds of FP32C ragged markers (k_sweep_pr).
+template <int FORM, int KIND, int KM, bool PROF, bool CL = false, bool PR = false>
 __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_beta[kMaxSpec];
     __shared__ double s_acum[kMaxSpec];
     __shared__ int s_comp[kMaxSpec];
+    __shared__ int s_chg[kMaxSpec];       // pair-resolved rounds: the marker changes the residual
+    __shared__ float s_pdf[32][6];        // pair-resolved rounds: its residual deltas (ones, twos, missing)
+    __shared__ float s_nf[32][2];         // pair-resolved rounds: the marker's final num (double-float)
+    __shared__ int s_fbd[32];             // pair-resolved rounds: the decision came from the FP64 sampler
     __shared__ int s_first;
     __shared__ int s_abort;
     __shared__ double s_scal[4];          // ragged: shift, epsSum; dense FP32C: residual total
@@ -377,7 +408,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     const int ns = a.slice_lo[sidx + 1] - lo;
     const int nbytes = ((ns + kChunk - 1) / kChunk) * 16;
     const int64_t byte_lo = lo / 4;
-    const SmemPlan plan = make_plan(FORM, KIND, a.slice_max, a.slot_bytes, B, a.n_groups, CL ? a.G : 0);
+    const SmemPlan plan = make_plan(FORM, KIND, a.slice_max, a.slot_bytes, B, a.n_groups, CL ? a.G : 0, PR);
 
     double *eps64 = reinterpret_cast<double *>(smem + plan.eps0);
     float *eh = reinterpret_cast<float *>(smem + plan.eps0);
@@ -393,6 +424,15 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     // cluster exchange records [round parity][source CTA][marker]: the partial
     // sum and the missing-genotype sum, each a 128-bit fixed-point integer
     ulonglong2 *xch = reinterpret_cast<ulonglong2 *>(smem + plan.xch);
+    // pair-resolved rounds: per individual of the slice the codes of the
+    // round's markers (0 absent, 1 or 2 listed genotype, 3 missing), their
+    // bit masks over the slice [ones | twos | missing][word][marker], and the
+    // round's pair terms [p][t] summed over the CTAs (A low, Bm high word)
+    const int mw = a.slice_max / 32;
+    uint8_t *gmap = smem + plan.gmap;
+    unsigned *bmask = reinterpret_cast<unsigned *>(smem + plan.bmask);
+    unsigned long long *s_pt = reinterpret_cast<unsigned long long *>(smem + plan.pterm);
+    float4 *gdf = reinterpret_cast<float4 *>(smem + plan.gdfo);
 
     // ---- prologue: residual slice, constants, tables
     float muh, mul;
@@ -517,7 +557,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     const int team = tid >> lpm_log2;
     const double Nm1 = (double)(a.N - 1);
     const bool prof = PROF && sidx == 0 && tid == 0;
-    long long ph[6] = {0, 0, 0, 0, 0, 0};
+    long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     long long tp = prof ? clock64() : 0;
     auto mark = [&](int k) {
         if (prof) {
@@ -538,6 +578,19 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     };
     for (int i = tid; i < kMaxSpec * 4; i += kThreads)
         s_acc[i] = 0ull;
+    if (PR) {
+        for (int i = tid; i < a.slice_max * 2; i += kThreads)
+            reinterpret_cast<uint4 *>(gmap)[i] = make_uint4(0u, 0u, 0u, 0u);
+        // beta = z sd_k + num / den_k of a non-zero component in double-float
+        for (int i = tid; i < a.n_groups * kMaxK; i += kThreads) {
+            const int k = i % kMaxK;
+            const double *row = a.gconst + (size_t)(i / kMaxK) * kMaxK * 4;
+            float4 v;
+            df_from_double(row[4 * k + 3], v.x, v.y);
+            df_from_double(row[4 * k + 1], v.z, v.w);
+            gdf[i] = v;
+        }
+    }
 
     unsigned start = 0;
     long long r = 0;
@@ -698,11 +751,18 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                     for (int e = ro[0] + tm.lane; e < ro[1]; e += lpm) {
                         const int i = a.ridx[0][e];
                         df_add(h, l, eh[i], el[i]);
+                        if (PR)
+                            gmap[i * 32 + team] = 1;
                     }
                     for (int e = ro[2] + tm.lane; e < ro[3]; e += lpm) {
                         const int i = a.ridx[1][e];
                         df_add(h, l, 2.f * eh[i], 2.f * el[i]);
+                        if (PR)
+                            gmap[i * 32 + team] = 2;
                     }
+                    if (PR)
+                        for (int e = ro[4] + tm.lane; e < ro[5]; e += lpm)
+                            gmap[a.ridx[2][e] * 32 + team] = 3;
                     team_df_sum(h, l, tm, lpm);
                     float mh = 0.f, ml = 0.f;
                     if (a.eigen) {
@@ -735,6 +795,53 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                 atomicCAS(a.err, kDevOk, kDevRange);
         }
         __syncthreads();
+        if (PR) {
+            mark(6);
+            // bit masks of the round's markers over the slice, one thread per
+            // (word, marker): 32 consecutive individuals' codes of the marker
+            const int nwd = (ns + 31) / 32;
+            for (int e = tid; e < nwd * 32; e += kThreads) {
+                const int w = e >> 5, t = e & 31;
+                unsigned m1 = 0u, m2 = 0u, mm = 0u;
+                if (t < nb) {
+                    const int nj = min(32, ns - 32 * w);
+                    const uint8_t *col = gmap + (size_t)32 * w * 32 + t;
+                    for (int j = 0; j < nj; ++j) {
+                        const unsigned c = col[j * 32];
+                        m1 |= (c == 1u ? 1u : 0u) << j;
+                        m2 |= (c == 2u ? 1u : 0u) << j;
+                        mm |= (c == 3u ? 1u : 0u) << j;
+                    }
+                }
+                bmask[w * 32 + t] = m1;
+                bmask[(mw + w) * 32 + t] = m2;
+                bmask[(2 * mw + w) * 32 + t] = mm;
+            }
+            __syncthreads();
+            // pair terms p < t of the round's markers over the slice, a pair
+            // per thread: A[p][t] = sum g_p g_t over individuals listed in
+            // both, Bm[p][t] = sum of g_t over the individuals missing at p;
+            // published as exact integers (ordered before the barrier's
+            // release by the CTA barrier below)
+            unsigned long long *gp = a.pairs + (size_t)rb * 1024;
+            for (int e = tid; e < 1024; e += kThreads) {
+                const int p = e >> 5, t = e & 31;
+                if (p >= t || t >= nb)
+                    continue;
+                unsigned A = 0, Bm = 0;
+                for (int w = 0; w < nwd; ++w) {
+                    const unsigned *m1 = bmask + w * 32, *m2 = bmask + (mw + w) * 32, *mm = bmask + (2 * mw + w) * 32;
+                    const unsigned a1 = m1[p], a2 = m2[p], am = mm[p], b1 = m1[t], b2 = m2[t];
+                    A += __popc(a1 & b1) + 2u * (__popc(a1 & b2) + __popc(a2 & b1)) + 4u * __popc(a2 & b2);
+                    Bm += __popc(am & b1) + 2u * __popc(am & b2);
+                }
+                const unsigned long long v = (unsigned long long)A | ((unsigned long long)Bm << 32);
+                if (v)
+                    red_add_u64(gp + e, v);
+            }
+            __syncthreads();
+            mark(7);
+        }
         mark(1);
 
         // ---- grid barrier: one counter; release orders this CTA's
@@ -770,8 +877,189 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         if (s_abort)
             break;
 
-        // ---- redundant sampling of the round's markers in every CTA, one thread per marker
-        if (tid < nb) {
+        if (PR) {
+            // ---- pair-resolved round, identically in every CTA: lane t
+            // samples marker t; after the first change p the later markers'
+            // num move by dBeta_p isd_p isd_t (A[p][t] + mean_p Bm[p][t]
+            // - mean_t (Zsum_p - mean_p N) - mean_p Zsum_t), the change of
+            // x_t . eps that p's residual update, running sum and pending
+            // shift make (src/raggedbayesrkernel.cpp:10-35), and they are
+            // sampled again
+            const unsigned long long *gp = a.pairs + (size_t)rb * 1024;
+            for (int e = tid; e < 1024; e += kThreads)
+                s_pt[e] = ld_relaxed_u64(gp + e);
+            __syncthreads();
+            if (tid < 32) {
+                const int t = tid;
+                const bool valid = t < nb;
+                const SweepRec &rc = ring_rec[(start + (valid ? t : 0)) & Rm];
+                const double mean = rc.t[0], isd = rc.t[2], Zsum = rc.t[3];
+                double num0 = 0.0;
+                if (valid) {
+                    const unsigned long long *acc = solo ? s_acc + t * 4 : a.acc + (rb * kMaxSpec + t) * 4;
+                    const double tot = solo ? fx_join((long long)acc[0], acc[1])
+                                            : fx_join((long long)ld_relaxed_u64(acc), ld_relaxed_u64(acc + 1));
+                    num0 = (rc.beta_old * ((double)a.N - 1.0) - mean * s_scal[1] * isd) + (tot + s_scal[0] * Zsum) * isd;
+                }
+                // num, the marker constants and the corrections in double-float
+                float nh, nl, mh, ml, ih, il;
+                df_from_double(num0, nh, nl);
+                df_from_double(mean, mh, ml);
+                df_from_double(isd, ih, il);
+                const float Zf = (float)Zsum, Nf = (float)a.N;
+                const int g = valid ? rc.group : 0;
+                const double *gcg = gconst + (size_t)g * kMaxK * 4;
+                const float *gcfg = gcf + (size_t)g * kMaxK * 2;
+                const int K = gk[g];
+                const float uf = __double2float_rn(rc.u);
+                // certified decisions with a stability margin in num^2: a marker
+                // is sampled again only when a correction moves num^2 beyond
+                // its margin (H: the spread of the group's h_k, h_0 = 0
+                // included); decisions the margin sampler cannot certify are
+                // taken by the guarded FP32 sampler, else in FP64
+                float H = 0.f;
+                {
+                    float hmax = 0.f, hmin = 0.f;
+                    for (int k = 1; k < K; ++k) {
+                        hmax = fmaxf(hmax, gcfg[2 * k + 1]);
+                        hmin = fminf(hmin, gcfg[2 * k + 1]);
+                    }
+                    H = (hmax - hmin) * 1.000001f;
+                }
+                bool done = !valid;
+                int comp = -1;
+                float sref = 0.f, wmar = -1.f;
+                bool fbd = false;
+                double fb_beta = rc.beta_old, fb_acum = 0.0;
+                float boh, bol, zh, zl;
+                df_from_double(rc.beta_old, boh, bol);
+                df_from_double(rc.z, zh, zl);
+                const float4 *gdfg = gdf + (size_t)g * kMaxK;
+                for (;;) {
+                    const float sx = __fmaf_rn(nh, nh, 2.f * nh * nl);
+                    const float delta = fabsf(sx - sref) * 1.000001f + 4e-7f * (sx + sref);
+                    if (!done && !(H * delta <= wmar)) {
+                        int cm;
+                        float w;
+                        fbd = false;
+                        if (pick_margin<KM>(sx, uf, gcfg, K, cm, w)) {
+                            comp = cm;
+                            sref = sx;
+                            wmar = w;
+                        } else {
+                            float a0;
+                            wmar = -1.f;
+                            if (!pick_f32<KM>(nh, nl, uf, gcfg, K, comp, a0)) {
+                                const Pick pk = pick_marker<true, KM>((double)nh + (double)nl, rc.u, rc.z, rc.beta_old,
+                                                                      gcg, K);
+                                comp = pk.comp;
+                                fb_beta = pk.beta;
+                                fb_acum = pk.acum0;
+                                fbd = true;
+                            }
+                        }
+                    }
+                    const bool chg = !done && (rc.beta_old != 0.0 || comp > 0);
+                    const unsigned mask = __ballot_sync(0xffffffffu, chg);
+                    const int p = mask ? __ffs(mask) - 1 : 32;
+                    float ch = 0.f, cl = 0.f;
+                    if (!done && t <= p) {
+                        // the decision of marker t is final (src/BayesRBase.cpp:346-366);
+                        // beta, acum and the residual deltas follow after the round
+                        s_nf[t][0] = nh;
+                        s_nf[t][1] = nl;
+                        s_comp[t] = comp;
+                        s_fbd[t] = fbd ? 1 : 0;
+                        s_chg[t] = t == p ? 1 : 0;
+                        if (fbd) {
+                            s_beta[t] = fb_beta;
+                            s_acum[t] = fb_acum;
+                        }
+                        if (t == p) {
+                            // dBeta isd of the change in double-float
+                            float bh = boh, bl = bol;
+                            if (fbd) {
+                                df_from_double(fb_beta, bh, bl);
+                            } else if (comp == 0) {
+                                bh = bl = 0.f;
+                            } else if (comp > 0) {
+                                const float4 k4 = gdfg[comp];
+                                float ah, al, xh, xl;
+                                df_mul(zh, zl, k4.x, k4.y, ah, al);
+                                df_mul(nh, nl, k4.z, k4.w, xh, xl);
+                                df_add(ah, al, xh, xl);
+                                bh = ah;
+                                bl = al;
+                            }
+                            float dh = boh, dl = bol;
+                            df_add(dh, dl, -bh, -bl);
+                            df_mul(dh, dl, ih, il, ch, cl);
+                        }
+                        done = true;
+                    }
+                    if (!mask)
+                        break;
+                    // num_t += dBeta_p isd_p isd_t (A + mean_p Bm - mean_t (Zsum_p
+                    // - mean_p N) - mean_p Zsum_t)
+                    ch = __shfl_sync(0xffffffffu, ch, p);
+                    cl = __shfl_sync(0xffffffffu, cl, p);
+                    const float mph = __shfl_sync(0xffffffffu, mh, p), mpl = __shfl_sync(0xffffffffu, ml, p);
+                    const float Zp = __shfl_sync(0xffffffffu, Zf, p);
+                    if (!done) {
+                        const unsigned long long v = s_pt[p * 32 + t];
+                        const float A = (float)(unsigned)v, Bm = (float)(unsigned)(v >> 32);
+                        float t1h, t1l, t2h, t2l, t3h, t3l, t4h, t4l;
+                        df_mul(mph, mpl, Bm, 0.f, t1h, t1l);
+                        df_add(t1h, t1l, A, 0.f);
+                        df_mul(mph, mpl, Nf, 0.f, t2h, t2l);
+                        t2h = -t2h;
+                        t2l = -t2l;
+                        df_add(t2h, t2l, Zp, 0.f);
+                        df_mul(mh, ml, t2h, t2l, t3h, t3l);
+                        df_mul(mph, mpl, Zf, 0.f, t4h, t4l);
+                        df_add(t1h, t1l, -t3h, -t3l);
+                        df_add(t1h, t1l, -t4h, -t4l);
+                        float kh, kl, xh, xl;
+                        df_mul(ch, cl, ih, il, kh, kl);
+                        df_mul(kh, kl, t1h, t1l, xh, xl);
+                        df_add(nh, nl, xh, xl);
+                    }
+                }
+            }
+            __syncthreads();
+            // beta and acum of every marker at its final num, and the residual
+            // deltas (ones, twos, missing genotypes) of every change, as the
+            // pass per marker forms them
+            if (tid < nb) {
+                const SweepRec &rc = ring_rec[(start + tid) & Rm];
+                if (!s_fbd[tid]) {
+                    const int g = rc.group;
+                    const double *gcg = gconst + (size_t)g * kMaxK * 4;
+                    const int comp = s_comp[tid];
+                    const float nh = s_nf[tid][0], nl = s_nf[tid][1];
+                    double bnew = comp == 0 ? 0.0 : rc.beta_old;
+                    if (comp > 0)
+                        bnew = __dadd_rn(__dmul_rn(rc.z, gcg[4 * comp + 3]),
+                                         __dmul_rn((double)nh + (double)nl, gcg[4 * comp + 1]));
+                    int c2;
+                    float a0;
+                    pick_f32<KM>(nh, nl, __double2float_rn(rc.u), gcf + (size_t)g * kMaxK * 2, gk[g], c2, a0);
+                    s_beta[tid] = bnew;
+                    s_acum[tid] = (double)a0;
+                }
+            }
+            if (tid < nb && s_chg[tid]) {
+                const SweepRec &rc = ring_rec[(start + tid) & Rm];
+                const double dBeta = rc.beta_old - s_beta[tid];
+                const double oneAdj = dBeta * rc.t[2];
+                const double dk[3] = {oneAdj, 2.0 * oneAdj, dBeta * rc.t[0] * rc.t[2]};
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    df_from_double(dk[k], s_pdf[tid][2 * k], s_pdf[tid][2 * k + 1]);
+            }
+            __syncthreads();
+        } else if (tid < nb) {
+            // ---- redundant sampling of the round's markers in every CTA, one thread per marker
             const SweepRec &rc = ring_rec[(start + tid) & Rm];
             const unsigned long long *acc = solo ? s_acc + tid * 4 : a.acc + (rb * kMaxSpec + tid) * 4;
             unsigned long long cw[4] = {0ull, 0ull, 0ull, 0ull};
@@ -842,7 +1130,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         __syncthreads();
         mark(3);
 
-        const int first = a.async_batch > 0 ? nb : s_first;
+        const int first = (a.async_batch > 0 || PR) ? nb : s_first;
         const int last = first < nb ? first : nb - 1;
         if (sidx == 0) {
             // outputs of the resolved markers, only from CTA 0
@@ -859,6 +1147,9 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             // all CTAs have read the accumulators of round r-1: recycle them
             if (!CL && tid < 4 * kMaxSpec)
                 a.acc[((rb + 2) % 3) * kMaxSpec * 4 + tid] = 0ull;
+            if (PR)
+                for (int e = tid; e < 1024; e += kThreads)
+                    a.pairs[(size_t)((rb + 2) % 3) * 1024 + e] = 0ull;
         }
         if (solo)   // the sampling has read this round's sums (barrier above)
             for (int i = tid; i < kMaxSpec * 4; i += kThreads)
@@ -939,7 +1230,52 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                 }
             }
         };
-        if (a.async_batch > 0) {
+        if (PR) {
+            // every changing marker's residual update, in sweep order, by the
+            // owner of each individual from the round's bit masks (the same
+            // operations as a pass per marker, with the deltas the resolve
+            // formed); the pending shift and the running sum in order by one
+            // thread, one without individuals when there is one
+            unsigned chm = 0u;
+            for (int u = 0; u < nb; ++u)
+                chm |= s_chg[u] ? 1u << u : 0u;
+            if (tid == (ns < kThreads ? kThreads - 1 : 0)) {
+                for (unsigned m = chm; m; m &= m - 1u) {
+                    const int u = __ffs(m) - 1;
+                    const SweepRec &rc = ring_rec[(start + u) & Rm];
+                    const double dBeta = rc.beta_old - s_beta[u];
+                    const double mean = rc.t[0], isd = rc.t[2], Zsum = rc.t[3];
+                    s_scal[0] = s_scal[0] - dBeta * mean * isd;
+                    s_scal[1] = s_scal[1] + ((dBeta * Zsum) * isd - ((dBeta * mean) * (double)a.N) * isd);
+                }
+            }
+            if (chm) {
+                for (int i = tid; i < ns; i += kThreads) {
+                    const int w = i >> 5;
+                    const unsigned bit = 1u << (i & 31);
+                    float h = eh[i], l = el[i];
+                    bool any = false;
+                    for (unsigned m = chm; m; m &= m - 1u) {
+                        const int u = __ffs(m) - 1;
+                        const int k = (bmask[w * 32 + u] & bit) ? 0
+                                      : (bmask[(mw + w) * 32 + u] & bit) ? 1
+                                      : (bmask[(2 * mw + w) * 32 + u] & bit) ? 2 : -1;
+                        if (k >= 0) {
+                            df_add(h, l, s_pdf[u][2 * k], s_pdf[u][2 * k + 1]);
+                            any = true;
+                        }
+                    }
+                    if (any) {
+                        eh[i] = h;
+                        el[i] = l;
+                    }
+                }
+            }
+            __syncthreads();
+            // the next round's codes start from zero
+            for (int i = tid; i < ns * 2; i += kThreads)
+                reinterpret_cast<uint4 *>(gmap)[i] = make_uint4(0u, 0u, 0u, 0u);
+        } else if (a.async_batch > 0) {
             for (int u = 0; u < nb; ++u) {
                 if (ring_rec[(start + u) & Rm].beta_old != 0.0 || s_beta[u] != 0.0) {
                     apply_one(u);
@@ -959,6 +1295,8 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
         for (int k = 0; k < 5; ++k)
             a.prof[k] = ph[k];
         a.prof[5] = r;
+        a.prof[6] = ph[6];   // pair-resolved rounds: the dot products (phase 1 is then the publication)
+        a.prof[7] = ph[7];   // pair-resolved rounds: the pair terms
     }
     cp_async_wait_all();
     __syncthreads();
@@ -1017,6 +1355,13 @@ template <int FORM, int KIND, int KM, bool PROF>
 __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
 {
     sweep_body<FORM, KIND, KM, PROF>(a, (int)blockIdx.x);
+}
+
+// Pair-resolved rounds over FP32C ragged markers.
+template <int KM, bool PROF>
+__global__ void __launch_bounds__(kThreads, 1) k_sweep_pr(SweepArgs a)
+{
+    sweep_body<kFormFP32C, kKindRagged, KM, PROF, false, true>(a, (int)blockIdx.x);
 }
 
 // The sweep as one thread-block cluster of G CTAs (the whole grid); the
@@ -1135,7 +1480,7 @@ cudaError_t launch_sweep_stats(int64_t M, const int32_t *group, const int32_t *c
 
 size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a)
 {
-    return make_plan(form, kind, a.slice_max, a.slot_bytes, a.B, a.n_groups, a.cluster).total;
+    return make_plan(form, kind, a.slice_max, a.slot_bytes, a.B, a.n_groups, a.cluster, a.pairs != nullptr).total;
 }
 
 // Clusters above 8 CTAs are a non-portable size, allowed per kernel.
@@ -1183,6 +1528,8 @@ static cudaError_t launch_one(const SweepArgs &a, size_t smem, cudaStream_t st)
     if (a.cluster > 0)
         return launch_one_cl<FORM, KIND, KM>(a, smem, st);
     const void *f = a.prof ? (const void *)k_sweep<FORM, KIND, KM, true> : (const void *)k_sweep<FORM, KIND, KM, false>;
+    if (FORM == kFormFP32C && KIND == kKindRagged && a.pairs)
+        f = a.prof ? (const void *)k_sweep_pr<KM, true> : (const void *)k_sweep_pr<KM, false>;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
@@ -1299,11 +1646,17 @@ cudaError_t launch_sweep_multi(int form, int kmax, const MultiSweepArgs &m, size
     return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
-int sweep_max_ctas_per_sm(int form, int kind, size_t smem)
+int sweep_max_ctas_per_sm(int form, int kind, size_t smem, bool pair_rounds)
 {
     int n = 1 << 30;
     const void *fs[4] = {sweep_fn<4, false>(form, kind), sweep_fn<kMaxK, false>(form, kind),
                          sweep_fn<4, true>(form, kind), sweep_fn<kMaxK, true>(form, kind)};
+    if (pair_rounds) {
+        fs[0] = (const void *)k_sweep_pr<4, false>;
+        fs[1] = (const void *)k_sweep_pr<kMaxK, false>;
+        fs[2] = (const void *)k_sweep_pr<4, true>;
+        fs[3] = (const void *)k_sweep_pr<kMaxK, true>;
+    }
     for (const void *f : fs) {
         int m = 0;
         cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -110,7 +110,9 @@ typedef struct brr_config {
     int32_t grid;              /* CTAs of the persistent sweep (0: one per SM) */
     int32_t device;            /* CUDA device ordinal */
     int32_t gram;              /* FP32C dense: 0 blocked sweep with a precomputed marker Gram when it fits
-                                  in device memory, -1 never, 1 required */
+                                  in device memory, -1 never, 1 required; FP32C ragged (not Eigen):
+                                  0 rounds of up to 32 markers resolved whole with integer pair terms
+                                  of the round's markers when their code map fits, -1 never */
     int32_t async_batch;       /* 0: the synchronous sweep (ppbayes); T in 1..64: the asyncppbayes
                                   schedule of the reference's ParallelGraph with T analysis tokens
                                   (src/parallelgraph.cpp:51-150): the T markers of a batch all read
@@ -236,7 +238,8 @@ int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_
  * than exist, so that tests can exercise the timeout path without a fault. */
 int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arrivals);
 
-/* Whether the chain runs the Gram-blocked FP32C sweep, the device time of
+/* Whether the chain resolves whole blocks per round (the Gram-blocked FP32C
+ * dense sweep, or pair-resolved FP32C ragged rounds), the device time of
  * building the packed marker Gram (ms: decode, GEMMs and combine, without the
  * allocations and the library's initialisation) and its size in bytes. */
 int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes);
