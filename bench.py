@@ -418,10 +418,10 @@ def synth_phenotype(gpu, lib, device, d_bed, N, M, n_causal, h2, seed):
     return y, counts
 
 
-def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed):
+def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed, gram=0):
     """W warm-up and K timed iterations of one chain; the library's CUDA-event
     time of the timed ones."""
-    ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S1, seed=seed,
+    ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S1, seed=seed, gram=gram,
                                    refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device), lib=lib)
     ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
     ch.set_phenotype(y)
@@ -433,6 +433,7 @@ def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed
     ch.close()
     return dict(rate=M * steps / (total_ms / 1e3), ms_per_step=total_ms / steps, sweep_ms=sweep_ms / steps,
                 rounds=rounds / steps, beta=st["beta"], comp=st["comp"], sigmaE=st["sigmaE"])
+
 
 
 def cpu_rate(bed, N, y, kind, iters):
@@ -461,6 +462,8 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
     y, counts = synth_phenotype(gpu, lib, device, d_bed, R_N, R_M, 500, 0.5, SEED + 21)
     f64 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP64, steps, warmup, SEED)
     f32 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED)
+    f32r = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED,
+                      gram=-1)
     # algorithmic bytes of a sweep: 4 bytes per listed genotype (ones, twos, missing)
     idx_bytes = 4.0 * float(counts[:, 1:4].sum())
     hbm, _ = peaks()
@@ -475,12 +478,16 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
     del c1_bed
     torch.cuda.empty_cache()
     out = {
-        "workload": R_WORKLOAD, "value": f32["rate"], "unit": "marker-updates/s", "form": "fp32c (refresh 50)",
-        "steps": steps, "ms_per_step": f32["ms_per_step"], "sweep_ms": f32["sweep_ms"],
+        "workload": R_WORKLOAD, "value": f32["rate"], "unit": "marker-updates/s",
+        "form": "fp32c (refresh 50), pair-resolved rounds of 32 markers",
+        "steps": steps, "ms_per_step": f32["ms_per_step"], "sweep_ms": f32["sweep_ms"], "rounds_per_step": f32["rounds"],
+        "fp32c_restart_rounds": {"value": f32r["rate"], "ms_per_step": f32r["ms_per_step"],
+                                 "rounds_per_step": f32r["rounds"],
+                                 "component_mismatches_vs_pair_rounds": int(np.count_nonzero(f32r["comp"] != f32["comp"]))},
         "plain_fp64": {"value": f64["rate"], "ms_per_step": f64["ms_per_step"], "rounds_per_step": f64["rounds"]},
         "speedup_fp32c_vs_plain": f32["rate"] / f64["rate"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "k_sweep (ragged, FP32C)",
+                     "traffic": None, "kernel": "k_sweep_pr (ragged, FP32C, pair-resolved rounds)",
                      "algorithmic_bytes_per_launch": idx_bytes,
                      "note": "4 bytes per listed genotype (ones, twos, missing) per sweep"},
         "matched_error": {"beta_max_abs_diff_vs_plain": float(np.abs(f32["beta"] - f64["beta"]).max()),
