@@ -59,7 +59,8 @@ struct brr_ctx {
     brr::BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
     float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)
     bool blocked = false;
-    bool pair_rounds = false;   // FP32C ragged: pair-resolved rounds (pair terms in d_acc + kPairOffset)
+    bool pair_rounds = false;   // FP32C ragged: pair-resolved rounds available (pair terms in d_acc + kPairOffset)
+    int64_t last_nnz = -1;      // markers in a non-zero component after the last sweep (-1: not known)
     bool has_missing = false;
     int kind = BRR_KIND_DENSE;          // storage: dense codes, or ragged lists (Ragged and Eigen markers)
     bool eigen = false;                 // Eigen sparse markers (BRR_KIND_EIGEN)

@@ -385,6 +385,7 @@ def run_uneven(lib, gpu, torch, device, steps, tune_rounds, scale=1.0):
 # genotypes, 500 causal markers with beta ~ N(0, 0.5/500), h2 = 0.5; the plain
 # FP64 form against the FP32C form with the FP64 refresh every 50 sweeps.
 R_N, R_M, R_RARE = 20_000, 50_000, 35_000
+R_LATE = 190   # untimed iterations between the burn-in and the stationary timing
 R_WORKLOAD = ("ragged sparse BayesR, N=20,000 x M=50,000, 70% rare p~U(0.001,0.05), rest p~U(0.05,0.5), 1% missing, "
               "500 causal, h2=0.5, S=0.01,0.001,0.0001")
 # The plain dense configuration C1 (CPU-runnable): N = 2,000 x M = 5,000,
@@ -418,9 +419,10 @@ def synth_phenotype(gpu, lib, device, d_bed, N, M, n_causal, h2, seed):
     return y, counts
 
 
-def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed, gram=0):
+def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed, gram=0, late=0):
     """W warm-up and K timed iterations of one chain; the library's CUDA-event
-    time of the timed ones."""
+    time of the timed ones.  late > 0: then `late` more untimed iterations and
+    K timed again (the chain's stationary phase)."""
     ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S1, seed=seed, gram=gram,
                                    refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device), lib=lib)
     ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
@@ -430,9 +432,17 @@ def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed
     ch.iterate(steps)
     sweep_ms, total_ms, rounds = ch.timing()
     st = ch.state()
+    out = dict(rate=M * steps / (total_ms / 1e3), ms_per_step=total_ms / steps, sweep_ms=sweep_ms / steps,
+               rounds=rounds / steps, beta=st["beta"], comp=st["comp"], sigmaE=st["sigmaE"])
+    if late:
+        ch.iterate(late)
+        ch.iterate(steps)
+        _, lt, lr = ch.timing()
+        out["late"] = {"after_iterations": warmup + steps + late, "rate": M * steps / (lt / 1e3),
+                       "ms_per_step": lt / steps, "rounds_per_step": lr / steps,
+                       "nonzero_effects": int(np.count_nonzero(ch.state()["beta"]))}
     ch.close()
-    return dict(rate=M * steps / (total_ms / 1e3), ms_per_step=total_ms / steps, sweep_ms=sweep_ms / steps,
-                rounds=rounds / steps, beta=st["beta"], comp=st["comp"], sigmaE=st["sigmaE"])
+    return out
 
 
 
@@ -461,9 +471,12 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
                         0.01)
     y, counts = synth_phenotype(gpu, lib, device, d_bed, R_N, R_M, 500, 0.5, SEED + 21)
     f64 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP64, steps, warmup, SEED)
-    f32 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED)
+    # the first timed iterations lie in the chain's burn-in, where about one
+    # marker in six changes its effect; the late ones in its stationary phase
+    f32 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED,
+                     late=R_LATE)
     f32r = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED,
-                      gram=-1)
+                      gram=-1, late=R_LATE)
     # algorithmic bytes of a sweep: 4 bytes per listed genotype (ones, twos, missing)
     idx_bytes = 4.0 * float(counts[:, 1:4].sum())
     hbm, _ = peaks()
@@ -479,10 +492,13 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
     torch.cuda.empty_cache()
     out = {
         "workload": R_WORKLOAD, "value": f32["rate"], "unit": "marker-updates/s",
-        "form": "fp32c (refresh 50), pair-resolved rounds of 32 markers",
+        "form": "fp32c (refresh 50); pair-resolved rounds of 32 markers while more than M/40 effects are non-zero, "
+                "restart rounds otherwise",
+        "timed_iterations": f"{warmup + 1}..{warmup + steps} (burn-in)",
         "steps": steps, "ms_per_step": f32["ms_per_step"], "sweep_ms": f32["sweep_ms"], "rounds_per_step": f32["rounds"],
+        "stationary": f32["late"],
         "fp32c_restart_rounds": {"value": f32r["rate"], "ms_per_step": f32r["ms_per_step"],
-                                 "rounds_per_step": f32r["rounds"],
+                                 "rounds_per_step": f32r["rounds"], "stationary": f32r["late"],
                                  "component_mismatches_vs_pair_rounds": int(np.count_nonzero(f32r["comp"] != f32["comp"]))},
         "plain_fp64": {"value": f64["rate"], "ms_per_step": f64["ms_per_step"], "rounds_per_step": f64["rounds"]},
         "speedup_fp32c_vs_plain": f32["rate"] / f64["rate"],
@@ -762,6 +778,8 @@ def main():
     ap.add_argument("--uneven-only", action="store_true", help="only the uneven-batch leg; --uneven-scale shrinks it")
     ap.add_argument("--uneven-scale", type=float, default=1.0)
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged (C2) and C1 measurements")
+    ap.add_argument("--ragged-only", action="store_true",
+                    help="only the ragged (C2) and C1 measurements (--no-cpu skips their CPU rates)")
     ap.add_argument("--sample-writer", action="store_true",
                     help="only the sample-file measurement: brr at the benchmark workload with and without rows")
     ap.add_argument("--matched-chains", action="store_true",
@@ -812,6 +830,11 @@ def main():
         sw = run_sample_writer(lib, gpu, torch, device, int(os.environ.get("BRR_SW_ITERS", "60")))
         if rank == 0:
             print(json.dumps({"sample_writer": sw}))
+        return
+    if args.ragged_only:
+        rr = run_ragged(lib, gpu, torch, device, args.steps, args.warmup, cpu=not args.no_cpu)
+        if rank == 0:
+            print(json.dumps({"ragged_only": True, **rr}))
         return
     if args.cluster_compare:
         cc = run_cluster_compare(lib, gpu, torch, device, args.steps, args.warmup)

@@ -111,8 +111,10 @@ typedef struct brr_config {
     int32_t device;            /* CUDA device ordinal */
     int32_t gram;              /* FP32C dense: 0 blocked sweep with a precomputed marker Gram when it fits
                                   in device memory, -1 never, 1 required; FP32C ragged (not Eigen):
-                                  0 rounds of up to 32 markers resolved whole with integer pair terms
-                                  of the round's markers when their code map fits, -1 never */
+                                  rounds of up to 32 markers resolved whole with integer pair terms
+                                  of the round's markers, 0 in the sweeps that follow one with more
+                                  than M/40 non-zero effects (and the first), 1 in every sweep,
+                                  -1 never */
     int32_t async_batch;       /* 0: the synchronous sweep (ppbayes); T in 1..64: the asyncppbayes
                                   schedule of the reference's ParallelGraph with T analysis tokens
                                   (src/parallelgraph.cpp:51-150): the T markers of a batch all read

@@ -3,7 +3,9 @@ against the FP32C restart sweep, through the C ABI.
 
 A round resolves all its markers: after a change at marker p the later
 markers' num move by the exact linear change of x_t . eps that p's residual
-update makes, built from integer pair terms summed over the slices.  Only
+update makes, built from integer pair terms summed over the slices.  With
+gram = 1 every sweep takes pair-resolved rounds, with gram = 0 (the default)
+the sweeps that follow one with more than M/40 non-zero effects.  Only
 rounding separates the result from the restart sweep, which samples every
 marker against the residual itself, so the bars are the FP32C form's:
 components identical, beta within 1e-7 relative of the FP64 oracle, the
@@ -27,10 +29,10 @@ def problem(N, M, seed, miss, p_lo=0.01, p_hi=0.5, n_causal=None):
     return bed, y
 
 
-def make(bed, N, y, S, group=None, seed=1, **kw):
+def make(bed, N, y, S, group=None, seed=1, gram=1, **kw):
     M = bed.shape[0]
     ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=gpu.KIND_RAGGED, form=gpu.FORM_FP32C, S=S, seed=seed,
-                                   refresh_every=4, **kw))
+                                   refresh_every=4, gram=gram, **kw))
     ch.pack_bed(bed)
     if group is not None:
         ch.set_groups(group)
@@ -103,6 +105,32 @@ def test_pair_rounds_and_restart_rounds_agree(gpu_lib):
     assert a.timing()[2] * 2 < b.timing()[2]
 
 
+def test_automatic_choice_follows_the_number_of_effects(gpu_lib):
+    """gram = 0: pair-resolved rounds in the first sweep and after any sweep
+    that leaves more than M/40 non-zero effects, restart rounds otherwise; both
+    give the chain of the restart rounds up to rounding."""
+    N, M = 4000, 1200
+    bed, y = problem(N, M, seed=31, miss=0.01, n_causal=6)
+    auto = make(bed, N, y, S1, seed=4, gram=0)
+    restart = make(bed, N, y, S1, seed=4, gram=-1)
+    modes = []
+    for it in range(8):
+        auto.iterate(1)
+        restart.iterate(1)
+        sa, sb = auto.state(), restart.state()
+        np.testing.assert_array_equal(sa["comp"], sb["comp"])
+        nz = sb["beta"] != 0
+        np.testing.assert_allclose(sa["beta"][nz], sb["beta"][nz], rtol=1e-9, atol=1e-13)
+        modes.append((auto.timing()[2], restart.timing()[2], int(np.count_nonzero(sb["beta"]))))
+    assert modes[0][0] == -(-M // 32)
+    for k in range(1, len(modes)):
+        prev_nnz = modes[k - 1][2]
+        if prev_nnz * 40 > M:
+            assert modes[k][0] == -(-M // 32), modes
+        else:
+            assert modes[k][0] == modes[k][1], modes
+
+
 def test_pair_rounds_are_not_used_where_they_do_not_apply(gpu_lib):
     N, M = 1000, 100
     bed, y = problem(N, M, seed=9, miss=0.01)
@@ -114,6 +142,14 @@ def test_pair_rounds_are_not_used_where_they_do_not_apply(gpu_lib):
         ch.init()
         assert not ch.gram_info()["blocked"], kw
         ch.close()
+        # and cannot be required there
+        if "cluster" not in kw:
+            ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=gpu.FORM_FP32C, S=S1, seed=1, gram=1, **kw))
+            ch.pack_bed(bed)
+            ch.set_phenotype(y)
+            with pytest.raises(gpu.BrrError):
+                ch.init()
+            ch.close()
 
 
 def test_pair_rounds_wait_limit_returns_timeout_and_context_recovers(gpu_lib):
