@@ -402,12 +402,17 @@ int brr::sweep_enqueue_inputs(brr_ctx *c, double eps_total, cudaStream_t st)
 // markers (N = 20,000, M = 50,000) the pair-resolved sweep is faster while more
 // than about one marker in forty carries a non-zero effect, so the choice
 // follows the chain's state after the last sweep (a deterministic function of
-// the chain, which keeps it reproducible); gram = 1 always takes them.
+// the chain, which keeps it reproducible).  Dense pair terms (population counts
+// over every code word of the slice for each pair) grow with the square of the
+// round width and cost more than the dot products on large slices, so dense
+// markers take them only when asked (pair_rounds = 1, as every kind does).
 static bool use_pair_rounds(const brr_ctx *c)
 {
-    if (!c->pair_rounds)
+    if (!c->pair_rounds || c->blocked)
         return false;
-    return c->cfg.gram > 0 || c->last_nnz < 0 || c->last_nnz * 40 > c->cfg.M;
+    if (c->cfg.pair_rounds > 0)
+        return true;
+    return c->kind != BRR_KIND_DENSE && (c->last_nnz < 0 || c->last_nnz * 40 > c->cfg.M);
 }
 
 // The sweep kernel's arguments and shared memory.
@@ -459,6 +464,7 @@ void brr::sweep_args(brr_ctx *c, double mu_new, double eps_total, SweepArgs &a, 
     a.async_batch = cf.async_batch;
     a.cluster = cf.cluster > 0 && c->G > 1 ? c->G : 0;
     a.pairs = use_pair_rounds(c) ? c->d_acc + kPairOffset : nullptr;
+    c->last_pair = a.pairs != nullptr;
     a.timeout_ns = c->wait_limit_ns;
     a.phantom = c->phantom;
     a.gram = c->d_gram;
@@ -629,11 +635,13 @@ void schedule_permutation(brr_ctx *c, uint32_t it)
 int prepare_blocked(brr_ctx *c)
 {
     const brr_config &cf = c->cfg;
-    if (cf.form == BRR_FORM_FP32C && cf.kind != BRR_KIND_DENSE) {
+    if (cf.pair_rounds > 0 && !c->pair_rounds)
+        return fail(BRR_ERR_ARG, "pair_rounds = 1 needs the FP32C form, ragged (not Eigen) or dense markers, at most "
+                                 "32 markers per round, no cluster and slices whose pair data fit shared memory");
+    if (cf.pair_rounds > 0 && cf.kind == BRR_KIND_DENSE && cf.gram > 0)
+        return fail(BRR_ERR_ARG, "pair_rounds = 1 takes the restart sweep, gram = 1 the Gram-blocked one");
+    if (cf.pair_rounds > 0 && cf.kind == BRR_KIND_DENSE) {
         c->blocked = false;
-        if (cf.gram > 0 && !c->pair_rounds)
-            return fail(BRR_ERR_ARG, "gram = 1 with sparse markers needs the pair-resolved rounds: ragged (not Eigen) "
-                                     "markers, at most 32 markers per round, no cluster, slices whose code map fits");
         return BRR_OK;
     }
     if (cf.form != BRR_FORM_FP32C || cf.kind != BRR_KIND_DENSE || cf.gram < 0 || cf.M < 2 || cf.cluster > 0) {
@@ -1004,10 +1012,10 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     a.slice_max = c.slice_max;
     a.slot_bytes = c.slot_bytes;
     a.cluster = cf.cluster > 0 && c.G > 1 ? c.G : 0;
-    // FP32C ragged markers resolve whole rounds with pair terms when the round
-    // is one warp wide and the slice's code map fits beside the ring
-    c.pair_rounds = cf.form == BRR_FORM_FP32C && c.kind == BRR_KIND_RAGGED && !c.eigen && c.B <= 32 &&
-                    cf.gram >= 0 && a.cluster == 0 && cf.async_batch == 0 && cf.N < (1 << 24);
+    // FP32C restart sweeps resolve whole rounds with pair terms when the round
+    // is one warp wide and the slice's code map or masks fit beside the ring
+    c.pair_rounds = cf.form == BRR_FORM_FP32C && !c.eigen && c.B <= 32 && cf.pair_rounds >= 0 && a.cluster == 0 &&
+                    cf.async_batch == 0 && cf.N < (1 << 24);
     if (c.pair_rounds) {
         a.pairs = c.d_acc + kPairOffset;
         const size_t sp = sweep_smem_bytes(cf.form, c.kind, a);
@@ -1025,7 +1033,7 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
         c.packed = true;
         return BRR_OK;
     }
-    const int per_sm = sweep_max_ctas_per_sm(cf.form, c.kind, smem, c.pair_rounds);
+    const int per_sm = sweep_max_ctas_per_sm(cf.form, c.kind, smem);
     if (per_sm < 1 || (int64_t)per_sm * c.sms < c.G)
         return fail(BRR_ERR_ARG, "the sweep kernel does not fit " + std::to_string(c.G) +
                                      " co-resident CTAs (shared memory " + std::to_string(smem) + " bytes)");
@@ -1408,11 +1416,22 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
     if (!ctx)
         return fail(BRR_ERR_ARG, "null context");
     if (blocked)
-        *blocked = ctx->blocked || ctx->pair_rounds ? 1 : 0;
+        *blocked = ctx->blocked ? 1 : 0;
     if (build_ms)
         *build_ms = ctx->gram_ms;
     if (bytes)
         *bytes = ctx->d_gram ? (int64_t)(ctx->cfg.M * (ctx->cfg.M - 1) / 2) * (int64_t)sizeof(double) : 0;
+    return BRR_OK;
+}
+
+int brr_get_round_info(brr_ctx *ctx, int32_t *pair_rounds, int32_t *last_sweep_pair_rounds)
+{
+    if (!ctx)
+        return fail(BRR_ERR_ARG, "null context");
+    if (pair_rounds)
+        *pair_rounds = ctx->pair_rounds && !ctx->blocked ? 1 : 0;
+    if (last_sweep_pair_rounds)
+        *last_sweep_pair_rounds = ctx->last_pair ? 1 : 0;
     return BRR_OK;
 }
 

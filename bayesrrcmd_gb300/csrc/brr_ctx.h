@@ -59,7 +59,9 @@ struct brr_ctx {
     brr::BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
     float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)
     bool blocked = false;
-    bool pair_rounds = false;   // FP32C ragged: pair-resolved rounds available (pair terms in d_acc + kPairOffset)
+    bool pair_rounds = false;   // FP32C restart sweep: pair-resolved rounds available (pair terms in
+                                // d_acc + kPairOffset)
+    bool last_pair = false;     // the last sweep took pair-resolved rounds
     int64_t last_nnz = -1;      // markers in a non-zero component after the last sweep (-1: not known)
     bool has_missing = false;
     int kind = BRR_KIND_DENSE;          // storage: dense codes, or ragged lists (Ragged and Eigen markers)
@@ -108,9 +110,9 @@ namespace brr {
 constexpr size_t kAccWords = 8 * 8 * kMaxSpec * 4;
 constexpr size_t kCounterWords = 2 * 8 * 16;
 // The restart sweep's accumulators take the first 3 x kMaxSpec x 4 words; the
-// pair terms of pair-resolved ragged rounds (3 x 1024 words) follow.
+// pair terms of pair-resolved rounds (3 x 2048 words) follow.
 constexpr size_t kPairOffset = 4096;
-static_assert(kPairOffset + 3 * 1024 <= kAccWords, "pair terms must fit the accumulator block");
+static_assert(kPairOffset + 3 * 2048 <= kAccWords, "pair terms must fit the accumulator block");
 constexpr int kPartBlocks = 608;   // 4 x 152 SMs for the updateMu reduction
 
 // Phases of one iteration of a chain (BayesRBase::runGibbs loop body,

@@ -281,6 +281,7 @@ int brr_multi_create(const brr_config *cfgs, int32_t n, brr_multi **out)
         brr_config c = cfgs[i];
         c.grid = 0;
         c.gram = -1;
+        c.pair_rounds = -1;
         brr_ctx *x = nullptr;
         const int rc = brr_ctx_create(&c, &x);
         if (rc)

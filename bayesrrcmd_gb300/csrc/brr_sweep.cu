@@ -195,9 +195,9 @@ struct SmemPlan {
     size_t gcf;             // FP32C: FP32 sampler constants, n_groups x kMaxK x 2 floats
     size_t gtab;            // FP32C dense: 256 float4 + 256 bytes
     size_t xch;             // cluster: [2][cluster][B] exchange records of 32 bytes
-    size_t gmap;            // pair-resolved rounds: [slice_max][32] codes of the round's markers
-    size_t bmask;           // pair-resolved rounds: [3][slice_max / 32][32] bit masks of the round's markers
-    size_t pterm;           // pair-resolved rounds: [32][32] pair terms of the round
+    size_t gmap;            // pair-resolved ragged rounds: [slice_max][32] codes of the round's markers
+    size_t bmask;           // pair-resolved rounds: [3][words][32] bit masks of the round's markers
+    size_t pterm;           // pair-resolved rounds: [2][32][32] pair terms of the round
     size_t gdfo;            // pair-resolved rounds: n_groups x kMaxK x {sd_k, 1/den_k} double-float
     size_t total;
 };
@@ -238,14 +238,15 @@ __host__ __device__ inline SmemPlan make_plan(int form, int kind, int slice_max,
     p.xch = o;
     o += (size_t)2 * cluster * B * 32;
     p.gmap = o;
-    if (pair_rounds)
+    if (pair_rounds && kind == kKindRagged)
         o += align16((size_t)slice_max * 32);
     p.bmask = o;
+    // ragged: a word holds 32 individuals; dense: a 32-bit code word, 16
     if (pair_rounds)
-        o += align16((size_t)3 * 32 * (slice_max / 32) * sizeof(unsigned));
+        o += align16((size_t)3 * 32 * (kind == kKindRagged ? slice_max / 32 : slot_bytes / 4) * sizeof(unsigned));
     p.pterm = o;
     if (pair_rounds)
-        o += 32 * 32 * sizeof(unsigned long long);
+        o += 2 * 32 * 32 * sizeof(unsigned long long);
     p.gdfo = o;
     if (pair_rounds)
         o += align16((size_t)n_groups * kMaxK * 4 * sizeof(float));
@@ -383,7 +384,8 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     __shared__ double s_acum[kMaxSpec];
     __shared__ int s_comp[kMaxSpec];
     __shared__ int s_chg[kMaxSpec];       // pair-resolved rounds: the marker changes the residual
-    __shared__ float s_pdf[32][6];        // pair-resolved rounds: its residual deltas (ones, twos, missing)
+    __shared__ float s_pdf[32][8];        // pair-resolved rounds: its residual deltas (ragged: ones, twos,
+                                          // missing; dense: per 2-bit code)
     __shared__ float s_nf[32][2];         // pair-resolved rounds: the marker's final num (double-float)
     __shared__ int s_fbd[32];             // pair-resolved rounds: the decision came from the FP64 sampler
     __shared__ int s_first;
@@ -424,11 +426,15 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     // cluster exchange records [round parity][source CTA][marker]: the partial
     // sum and the missing-genotype sum, each a 128-bit fixed-point integer
     ulonglong2 *xch = reinterpret_cast<ulonglong2 *>(smem + plan.xch);
-    // pair-resolved rounds: per individual of the slice the codes of the
-    // round's markers (0 absent, 1 or 2 listed genotype, 3 missing), their
-    // bit masks over the slice [ones | twos | missing][word][marker], and the
-    // round's pair terms [p][t] summed over the CTAs (A low, Bm high word)
-    const int mw = a.slice_max / 32;
+    // pair-resolved rounds.  Ragged: per individual of the slice the codes of
+    // the round's markers (0 absent, 1 or 2 listed genotype, 3 missing) and
+    // their bit masks over the slice [ones | twos | missing][word][marker];
+    // the round's pair terms [p][t] summed over the CTAs (A low, Bm high
+    // word).  Dense: bit masks of the code words [genotype >= 1 | genotype 2
+    // | missing][word][marker] at the even bit of each individual, and two
+    // words of pair terms [P | MM][p][t], [Gmp | Gmt][p][t], the diagonal
+    // holding each marker's genotype sum and missing count.
+    const int mw = KIND == kKindRagged ? a.slice_max / 32 : a.slot_bytes / 4;
     uint8_t *gmap = smem + plan.gmap;
     unsigned *bmask = reinterpret_cast<unsigned *>(smem + plan.bmask);
     unsigned long long *s_pt = reinterpret_cast<unsigned long long *>(smem + plan.pterm);
@@ -579,8 +585,9 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
     for (int i = tid; i < kMaxSpec * 4; i += kThreads)
         s_acc[i] = 0ull;
     if (PR) {
-        for (int i = tid; i < a.slice_max * 2; i += kThreads)
-            reinterpret_cast<uint4 *>(gmap)[i] = make_uint4(0u, 0u, 0u, 0u);
+        if (KIND == kKindRagged)
+            for (int i = tid; i < a.slice_max * 2; i += kThreads)
+                reinterpret_cast<uint4 *>(gmap)[i] = make_uint4(0u, 0u, 0u, 0u);
         // beta = z sd_k + num / den_k of a non-zero component in double-float
         for (int i = tid; i < a.n_groups * kMaxK; i += kThreads) {
             const int k = i % kMaxK;
@@ -795,7 +802,67 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                 atomicCAS(a.err, kDevOk, kDevRange);
         }
         __syncthreads();
-        if (PR) {
+        if (PR && KIND == kKindDense) {
+            mark(6);
+            // bit masks of the round's markers from their code words (16
+            // individuals each, code 0: genotype 2, 1: missing, 2: genotype 1,
+            // 3: genotype 0; individuals past the slice masked), one thread per
+            // (word, marker)
+            const int nwd = (ns + 15) / 16;
+            for (int e = tid; e < nwd * 32; e += kThreads) {
+                const int w = e >> 5, t = e & 31;
+                unsigned h = 0u, d = 0u, m = 0u;
+                if (t < nb) {
+                    const unsigned cw =
+                        reinterpret_cast<const unsigned *>(ring_codes + ((start + t) & Rm) * a.slot_bytes)[w];
+                    const int nv = ns - 16 * w;
+                    const unsigned vm = nv >= 16 ? 0x55555555u : (0x55555555u & ((1u << (2 * nv)) - 1u));
+                    h = ~cw & vm;
+                    d = ~cw & ~(cw >> 1) & vm;
+                    m = cw & ~(cw >> 1) & vm;
+                }
+                bmask[w * 32 + t] = h;
+                bmask[(mw + w) * 32 + t] = d;
+                bmask[(2 * mw + w) * 32 + t] = m;
+            }
+            __syncthreads();
+            // pair terms p <= t, a pair per thread: P = sum g_p g_t, MM =
+            // individuals missing at both, Gmp = sum of g_t over the
+            // individuals missing at p, Gmt = sum of g_p over those missing at
+            // t; on the diagonal the marker's genotype sum and missing count
+            // (g = [genotype >= 1] + [genotype 2])
+            unsigned long long *gp = a.pairs + (size_t)rb * 2048;
+            for (int e = tid; e < 1024; e += kThreads) {
+                const int p = e >> 5, t = e & 31;
+                if (p > t || t >= nb)
+                    continue;
+                unsigned w0a = 0u, w0b = 0u, w1a = 0u, w1b = 0u;
+                for (int w = 0; w < nwd; ++w) {
+                    const unsigned *hh = bmask + w * 32, *dd = bmask + (mw + w) * 32, *mm = bmask + (2 * mw + w) * 32;
+                    const unsigned hp = hh[p], dp = dd[p], mp = mm[p];
+                    if (p == t) {
+                        w0a += __popc(hp) + __popc(dp);
+                        w0b += __popc(mp);
+                    } else {
+                        const unsigned ht = hh[t], dt = dd[t], mt = mm[t];
+                        w0a += __popc(hp & ht) + __popc(hp & dt) + __popc(dp & ht) + __popc(dp & dt);
+                        if (a.has_missing) {
+                            w0b += __popc(mp & mt);
+                            w1a += __popc(mp & ht) + __popc(mp & dt);
+                            w1b += __popc(mt & hp) + __popc(mt & dp);
+                        }
+                    }
+                }
+                const unsigned long long v0 = (unsigned long long)w0a | ((unsigned long long)w0b << 32);
+                const unsigned long long v1 = (unsigned long long)w1a | ((unsigned long long)w1b << 32);
+                if (v0)
+                    red_add_u64(gp + e, v0);
+                if (v1)
+                    red_add_u64(gp + 1024 + e, v1);
+            }
+            __syncthreads();
+            mark(7);
+        } else if (PR) {
             mark(6);
             // bit masks of the round's markers over the slice, one thread per
             // (word, marker): 32 consecutive individuals' codes of the marker
@@ -823,7 +890,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             // both, Bm[p][t] = sum of g_t over the individuals missing at p;
             // published as exact integers (ordered before the barrier's
             // release by the CTA barrier below)
-            unsigned long long *gp = a.pairs + (size_t)rb * 1024;
+            unsigned long long *gp = a.pairs + (size_t)rb * 2048;
             for (int e = tid; e < 1024; e += kThreads) {
                 const int p = e >> 5, t = e & 31;
                 if (p >= t || t >= nb)
@@ -885,28 +952,52 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             // x_t . eps that p's residual update, running sum and pending
             // shift make (src/raggedbayesrkernel.cpp:10-35), and they are
             // sampled again
-            const unsigned long long *gp = a.pairs + (size_t)rb * 1024;
-            for (int e = tid; e < 1024; e += kThreads)
+            const unsigned long long *gp = a.pairs + (size_t)rb * 2048;
+            for (int e = tid; e < (KIND == kKindDense ? 2048 : 1024); e += kThreads)
                 s_pt[e] = ld_relaxed_u64(gp + e);
             __syncthreads();
             if (tid < 32) {
                 const int t = tid;
                 const bool valid = t < nb;
                 const SweepRec &rc = ring_rec[(start + (valid ? t : 0)) & Rm];
+                // ragged: mean, 1/sd, sum of listed genotypes; dense: sigma,
+                // column mean, value of a missing genotype, sum of the column
                 const double mean = rc.t[0], isd = rc.t[2], Zsum = rc.t[3];
                 double num0 = 0.0;
                 if (valid) {
                     const unsigned long long *acc = solo ? s_acc + t * 4 : a.acc + (rb * kMaxSpec + t) * 4;
-                    const double tot = solo ? fx_join((long long)acc[0], acc[1])
-                                            : fx_join((long long)ld_relaxed_u64(acc), ld_relaxed_u64(acc + 1));
-                    num0 = (rc.beta_old * ((double)a.N - 1.0) - mean * s_scal[1] * isd) + (tot + s_scal[0] * Zsum) * isd;
+                    auto ldw = [&](int k) -> unsigned long long { return solo ? acc[k] : ld_relaxed_u64(acc + k); };
+                    const double tot = fx_join((long long)ldw(0), ldw(1));
+                    if (KIND == kKindDense) {
+                        const double sm = fx_join((long long)ldw(2), ldw(3));
+                        num0 = (rc.t[0] * (tot - rc.t[1] * (s_scal[2] - sm)) + rc.t[2] * sm) +
+                               rc.beta_old * ((double)a.N - 1.0);
+                    } else {
+                        num0 = (rc.beta_old * ((double)a.N - 1.0) - mean * s_scal[1] * isd) + (tot + s_scal[0] * Zsum) * isd;
+                    }
                 }
                 // num, the marker constants and the corrections in double-float
                 float nh, nl, mh, ml, ih, il;
                 df_from_double(num0, nh, nl);
-                df_from_double(mean, mh, ml);
-                df_from_double(isd, ih, il);
+                df_from_double(mean, mh, ml);     // dense: sigma
+                df_from_double(isd, ih, il);      // dense: value of a missing genotype
                 const float Zf = (float)Zsum, Nf = (float)a.N;
+                // dense: column mean, sum of the column, sigma * colmean and
+                // sigma * colmean + the missing value, the marker's genotype sum
+                // and missing count (the diagonal of the pair terms)
+                float cmh = 0.f, cml = 0.f, csh = 0.f, csl = 0.f, sch = 0.f, scl = 0.f, sxh = 0.f, sxl = 0.f;
+                float Sg = 0.f, Nm = 0.f;
+                if (KIND == kKindDense) {
+                    df_from_double(rc.t[1], cmh, cml);
+                    df_from_double(rc.t[3], csh, csl);
+                    df_mul(mh, ml, cmh, cml, sch, scl);
+                    sxh = sch;
+                    sxl = scl;
+                    df_add(sxh, sxl, ih, il);
+                    const unsigned long long dg = s_pt[t * 32 + t];
+                    Sg = (float)(unsigned)dg;
+                    Nm = (float)(unsigned)(dg >> 32);
+                }
                 const int g = valid ? rc.group : 0;
                 const double *gcg = gconst + (size_t)g * kMaxK * 4;
                 const float *gcfg = gcf + (size_t)g * kMaxK * 2;
@@ -993,12 +1084,64 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                             }
                             float dh = boh, dl = bol;
                             df_add(dh, dl, -bh, -bl);
-                            df_mul(dh, dl, ih, il, ch, cl);
+                            if (KIND == kKindDense) {
+                                ch = dh;
+                                cl = dl;
+                            } else {
+                                df_mul(dh, dl, ih, il, ch, cl);
+                            }
                         }
                         done = true;
                     }
                     if (!mask)
                         break;
+                    if (KIND == kKindDense) {
+                        // x_p . x_t moves num_t by dBeta_p (sigma_t dT - sigma_t cm_t dE
+                        // + (sigma_t cm_t + xm_t) dSm): dT the change of the sum of
+                        // g_t eps over t's genotypes, dE of the residual total, dSm of
+                        // the residual over t's missing genotypes
+                        ch = __shfl_sync(0xffffffffu, ch, p);
+                        cl = __shfl_sync(0xffffffffu, cl, p);
+                        const float sph = __shfl_sync(0xffffffffu, mh, p), spl = __shfl_sync(0xffffffffu, ml, p);
+                        const float cph = __shfl_sync(0xffffffffu, cmh, p), cpl = __shfl_sync(0xffffffffu, cml, p);
+                        const float xph = __shfl_sync(0xffffffffu, ih, p), xpl = __shfl_sync(0xffffffffu, il, p);
+                        const float eph = __shfl_sync(0xffffffffu, csh, p), epl = __shfl_sync(0xffffffffu, csl, p);
+                        if (!done) {
+                            const unsigned long long v0 = s_pt[p * 32 + t], v1 = s_pt[1024 + p * 32 + t];
+                            const float P = (float)(unsigned)v0, MM = (float)(unsigned)(v0 >> 32);
+                            const float Gmp = (float)(unsigned)v1, Gmt = (float)(unsigned)(v1 >> 32);
+                            // dT = sigma_p (P - cm_p (S_t - Gmp)) + xm_p Gmp
+                            float th, tl, uh, ul;
+                            df_mul(cph, cpl, Sg - Gmp, 0.f, th, tl);
+                            th = -th;
+                            tl = -tl;
+                            df_add(th, tl, P, 0.f);
+                            df_mul(sph, spl, th, tl, uh, ul);
+                            df_mul(xph, xpl, Gmp, 0.f, th, tl);
+                            df_add(uh, ul, th, tl);
+                            // sigma_t dT - sigma_t cm_t dE
+                            float rh, rl, qh, ql;
+                            df_mul(mh, ml, uh, ul, rh, rl);
+                            df_mul(sch, scl, eph, epl, qh, ql);
+                            df_add(rh, rl, -qh, -ql);
+                            if (a.has_missing) {
+                                // dSm = sigma_p (Gmt - cm_p (nmiss_t - MM)) + xm_p MM
+                                df_mul(cph, cpl, Nm - MM, 0.f, th, tl);
+                                th = -th;
+                                tl = -tl;
+                                df_add(th, tl, Gmt, 0.f);
+                                df_mul(sph, spl, th, tl, uh, ul);
+                                df_mul(xph, xpl, MM, 0.f, th, tl);
+                                df_add(uh, ul, th, tl);
+                                df_mul(sxh, sxl, uh, ul, qh, ql);
+                                df_add(rh, rl, qh, ql);
+                            }
+                            float xh2, xl2;
+                            df_mul(ch, cl, rh, rl, xh2, xl2);
+                            df_add(nh, nl, xh2, xl2);
+                        }
+                        continue;
+                    }
                     // num_t += dBeta_p isd_p isd_t (A + mean_p Bm - mean_t (Zsum_p
                     // - mean_p N) - mean_p Zsum_t)
                     ch = __shfl_sync(0xffffffffu, ch, p);
@@ -1051,11 +1194,21 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             if (tid < nb && s_chg[tid]) {
                 const SweepRec &rc = ring_rec[(start + tid) & Rm];
                 const double dBeta = rc.beta_old - s_beta[tid];
-                const double oneAdj = dBeta * rc.t[2];
-                const double dk[3] = {oneAdj, 2.0 * oneAdj, dBeta * rc.t[0] * rc.t[2]};
+                if (KIND == kKindDense) {
+                    // delta per 2-bit code: dBeta (g - colmean) sigma, a missing genotype dBeta xm
 #pragma unroll
-                for (int k = 0; k < 3; ++k)
-                    df_from_double(dk[k], s_pdf[tid][2 * k], s_pdf[tid][2 * k + 1]);
+                    for (int c = 0; c < 4; ++c) {
+                        const double gv = c == 0 ? 2.0 : (c == 2 ? 1.0 : 0.0);
+                        const double d = c == 1 ? dBeta * rc.t[2] : dBeta * ((gv - rc.t[1]) * rc.t[0]);
+                        df_from_double(d, s_pdf[tid][2 * c], s_pdf[tid][2 * c + 1]);
+                    }
+                } else {
+                    const double oneAdj = dBeta * rc.t[2];
+                    const double dk[3] = {oneAdj, 2.0 * oneAdj, dBeta * rc.t[0] * rc.t[2]};
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        df_from_double(dk[k], s_pdf[tid][2 * k], s_pdf[tid][2 * k + 1]);
+                }
             }
             __syncthreads();
         } else if (tid < nb) {
@@ -1148,8 +1301,8 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             if (!CL && tid < 4 * kMaxSpec)
                 a.acc[((rb + 2) % 3) * kMaxSpec * 4 + tid] = 0ull;
             if (PR)
-                for (int e = tid; e < 1024; e += kThreads)
-                    a.pairs[(size_t)((rb + 2) % 3) * 1024 + e] = 0ull;
+                for (int e = tid; e < 2048; e += kThreads)
+                    a.pairs[(size_t)((rb + 2) % 3) * 2048 + e] = 0ull;
         }
         if (solo)   // the sampling has read this round's sums (barrier above)
             for (int i = tid; i < kMaxSpec * 4; i += kThreads)
@@ -1244,12 +1397,30 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
                     const int u = __ffs(m) - 1;
                     const SweepRec &rc = ring_rec[(start + u) & Rm];
                     const double dBeta = rc.beta_old - s_beta[u];
-                    const double mean = rc.t[0], isd = rc.t[2], Zsum = rc.t[3];
-                    s_scal[0] = s_scal[0] - dBeta * mean * isd;
-                    s_scal[1] = s_scal[1] + ((dBeta * Zsum) * isd - ((dBeta * mean) * (double)a.N) * isd);
+                    if (KIND == kKindDense) {
+                        // the residual total moves by dBeta times the column sum
+                        s_scal[2] = s_scal[2] + dBeta * rc.t[3];
+                    } else {
+                        const double mean = rc.t[0], isd = rc.t[2], Zsum = rc.t[3];
+                        s_scal[0] = s_scal[0] - dBeta * mean * isd;
+                        s_scal[1] = s_scal[1] + ((dBeta * Zsum) * isd - ((dBeta * mean) * (double)a.N) * isd);
+                    }
                 }
             }
-            if (chm) {
+            if (chm && KIND == kKindDense) {
+                // every individual of the slice moves with every change: the
+                // delta of its code, marker by marker in sweep order
+                for (int i = tid; i < ns; i += kThreads) {
+                    float h = eh[i], l = el[i];
+                    for (unsigned m = chm; m; m &= m - 1u) {
+                        const int u = __ffs(m) - 1;
+                        const unsigned c = (ring_codes[((start + u) & Rm) * a.slot_bytes + (i >> 2)] >> (2 * (i & 3))) & 3u;
+                        df_add(h, l, s_pdf[u][2 * c], s_pdf[u][2 * c + 1]);
+                    }
+                    eh[i] = h;
+                    el[i] = l;
+                }
+            } else if (chm) {
                 for (int i = tid; i < ns; i += kThreads) {
                     const int w = i >> 5;
                     const unsigned bit = 1u << (i & 31);
@@ -1273,8 +1444,9 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, const int sidx)
             }
             __syncthreads();
             // the next round's codes start from zero
-            for (int i = tid; i < ns * 2; i += kThreads)
-                reinterpret_cast<uint4 *>(gmap)[i] = make_uint4(0u, 0u, 0u, 0u);
+            if (KIND == kKindRagged)
+                for (int i = tid; i < ns * 2; i += kThreads)
+                    reinterpret_cast<uint4 *>(gmap)[i] = make_uint4(0u, 0u, 0u, 0u);
         } else if (a.async_batch > 0) {
             for (int u = 0; u < nb; ++u) {
                 if (ring_rec[(start + u) & Rm].beta_old != 0.0 || s_beta[u] != 0.0) {
@@ -1357,11 +1529,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_sweep(SweepArgs a)
     sweep_body<FORM, KIND, KM, PROF>(a, (int)blockIdx.x);
 }
 
-// Pair-resolved rounds over FP32C ragged markers.
-template <int KM, bool PROF>
+// Pair-resolved rounds over FP32C dense or ragged markers.
+template <int KIND, int KM, bool PROF>
 __global__ void __launch_bounds__(kThreads, 1) k_sweep_pr(SweepArgs a)
 {
-    sweep_body<kFormFP32C, kKindRagged, KM, PROF, false, true>(a, (int)blockIdx.x);
+    sweep_body<kFormFP32C, KIND, KM, PROF, false, true>(a, (int)blockIdx.x);
 }
 
 // The sweep as one thread-block cluster of G CTAs (the whole grid); the
@@ -1528,8 +1700,8 @@ static cudaError_t launch_one(const SweepArgs &a, size_t smem, cudaStream_t st)
     if (a.cluster > 0)
         return launch_one_cl<FORM, KIND, KM>(a, smem, st);
     const void *f = a.prof ? (const void *)k_sweep<FORM, KIND, KM, true> : (const void *)k_sweep<FORM, KIND, KM, false>;
-    if (FORM == kFormFP32C && KIND == kKindRagged && a.pairs)
-        f = a.prof ? (const void *)k_sweep_pr<KM, true> : (const void *)k_sweep_pr<KM, false>;
+    if (FORM == kFormFP32C && a.pairs)
+        f = a.prof ? (const void *)k_sweep_pr<KIND, KM, true> : (const void *)k_sweep_pr<KIND, KM, false>;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
@@ -1651,11 +1823,16 @@ int sweep_max_ctas_per_sm(int form, int kind, size_t smem, bool pair_rounds)
     int n = 1 << 30;
     const void *fs[4] = {sweep_fn<4, false>(form, kind), sweep_fn<kMaxK, false>(form, kind),
                          sweep_fn<4, true>(form, kind), sweep_fn<kMaxK, true>(form, kind)};
-    if (pair_rounds) {
-        fs[0] = (const void *)k_sweep_pr<4, false>;
-        fs[1] = (const void *)k_sweep_pr<kMaxK, false>;
-        fs[2] = (const void *)k_sweep_pr<4, true>;
-        fs[3] = (const void *)k_sweep_pr<kMaxK, true>;
+    if (pair_rounds && kind == kKindDense) {
+        fs[0] = (const void *)k_sweep_pr<kKindDense, 4, false>;
+        fs[1] = (const void *)k_sweep_pr<kKindDense, kMaxK, false>;
+        fs[2] = (const void *)k_sweep_pr<kKindDense, 4, true>;
+        fs[3] = (const void *)k_sweep_pr<kKindDense, kMaxK, true>;
+    } else if (pair_rounds) {
+        fs[0] = (const void *)k_sweep_pr<kKindRagged, 4, false>;
+        fs[1] = (const void *)k_sweep_pr<kKindRagged, kMaxK, false>;
+        fs[2] = (const void *)k_sweep_pr<kKindRagged, 4, true>;
+        fs[3] = (const void *)k_sweep_pr<kKindRagged, kMaxK, true>;
     }
     for (const void *f : fs) {
         int m = 0;

@@ -35,7 +35,7 @@ class BrrConfig(C.Structure):
         ("seed", C.c_uint32), ("chain", C.c_uint32),
         ("v0E", C.c_double), ("s02E", C.c_double), ("v0G", C.c_double), ("s02G", C.c_double),
         ("refresh_every", C.c_int32), ("spec_width", C.c_int32), ("grid", C.c_int32), ("device", C.c_int32),
-        ("gram", C.c_int32), ("async_batch", C.c_int32), ("cluster", C.c_int32),
+        ("gram", C.c_int32), ("async_batch", C.c_int32), ("cluster", C.c_int32), ("pair_rounds", C.c_int32),
     ]
 
 
@@ -64,6 +64,7 @@ EXPORTS = [
     "brr_set_wait_limit", "brr_set_profiling", "brr_xbeta", "brr_synth_bed_device", "brr_xbeta_noalloc",
     "brr_get_gram_info",
     "brr_get_gram_entries",
+    "brr_get_round_info",
     "brr_batch_create", "brr_batch_destroy", "brr_batch_pack_bed", "brr_batch_pack_bed_device",
     "brr_batch_set_groups", "brr_batch_set_phenotypes", "brr_batch_init", "brr_batch_iterate",
     "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_set_profiling",
@@ -111,6 +112,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_get_gram_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.brr_get_gram_entries.argtypes = [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int64,
                                          C.POINTER(C.c_double)]
+    lib.brr_get_round_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
     lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
@@ -199,6 +201,7 @@ class ChainConfig:
     gram: int = 0
     async_batch: int = 0
     cluster: int = 0
+    pair_rounds: int = 0
 
     def to_c(self) -> BrrConfig:
         c = BrrConfig()
@@ -214,6 +217,7 @@ class ChainConfig:
         c.gram = self.gram
         c.async_batch = self.async_batch
         c.cluster = self.cluster
+        c.pair_rounds = self.pair_rounds
         return c
 
 
@@ -367,6 +371,11 @@ class Chain:
         self._check(self.lib.brr_get_gram_entries(self.h, _ptr(j, C.c_int64), _ptr(k, C.c_int64), j.size,
                                                   _ptr(out, C.c_double)))
         return out
+
+    def round_info(self):
+        pr, last = C.c_int32(), C.c_int32()
+        self._check(self.lib.brr_get_round_info(self.h, C.byref(pr), C.byref(last)))
+        return dict(pair_rounds=bool(pr.value), last_sweep_pair_rounds=bool(last.value))
 
     def gram_info(self):
         b, ms, n = C.c_int32(), C.c_double(), C.c_int64()

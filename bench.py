@@ -419,11 +419,12 @@ def synth_phenotype(gpu, lib, device, d_bed, N, M, n_causal, h2, seed):
     return y, counts
 
 
-def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed, gram=0, late=0):
+def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed, gram=0, late=0, phases=False,
+               pair_rounds=0):
     """W warm-up and K timed iterations of one chain; the library's CUDA-event
     time of the timed ones.  late > 0: then `late` more untimed iterations and
     K timed again (the chain's stationary phase)."""
-    ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S1, seed=seed, gram=gram,
+    ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S1, seed=seed, gram=gram, pair_rounds=pair_rounds,
                                    refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, device=device), lib=lib)
     ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())
     ch.set_phenotype(y)
@@ -434,6 +435,21 @@ def time_chain(gpu, lib, device, d_bed, N, M, y, kind, form, steps, warmup, seed
     st = ch.state()
     out = dict(rate=M * steps / (total_ms / 1e3), ms_per_step=total_ms / steps, sweep_ms=sweep_ms / steps,
                rounds=rounds / steps, beta=st["beta"], comp=st["comp"], sigmaE=st["sigmaE"])
+    if phases:
+        # one further iteration of the phase-counting variant: cycles per round on CTA 0
+        ch.set_profiling(1)
+        ch.iterate(1)
+        ph = ch.phase_cycles()
+        ch.set_profiling(0)
+        n = max(int(ph[5]), 1)
+        names = ("ring", "dot_products", "exchange_wait", "sampling", "update")
+        out["phase_cycles_per_round"] = {k: round(float(ph[i]) / n) for i, k in enumerate(names)}
+        if ph[6] or ph[7]:
+            out["phase_cycles_per_round"]["dot_products"] = round(float(ph[6]) / n)
+            out["phase_cycles_per_round"]["pair_terms"] = round(float(ph[7]) / n)
+            out["phase_cycles_per_round"]["publication"] = round(float(ph[1]) / n)
+        out["phase_iteration"] = warmup + steps + 1
+        warmup += 1
     if late:
         ch.iterate(late)
         ch.iterate(steps)
@@ -474,9 +490,9 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
     # the first timed iterations lie in the chain's burn-in, where about one
     # marker in six changes its effect; the late ones in its stationary phase
     f32 = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED,
-                     late=R_LATE)
+                     late=R_LATE, phases=True)
     f32r = time_chain(gpu, lib, device, d_bed, R_N, R_M, y, gpu.KIND_RAGGED, gpu.FORM_FP32C, steps, warmup, SEED,
-                      gram=-1, late=R_LATE)
+                      pair_rounds=-1, late=R_LATE)
     # algorithmic bytes of a sweep: 4 bytes per listed genotype (ones, twos, missing)
     idx_bytes = 4.0 * float(counts[:, 1:4].sum())
     hbm, _ = peaks()
@@ -497,6 +513,7 @@ def run_ragged(lib, gpu, torch, device, steps, warmup, cpu=True):
         "timed_iterations": f"{warmup + 1}..{warmup + steps} (burn-in)",
         "steps": steps, "ms_per_step": f32["ms_per_step"], "sweep_ms": f32["sweep_ms"], "rounds_per_step": f32["rounds"],
         "stationary": f32["late"],
+        "phase_cycles_per_round": f32["phase_cycles_per_round"], "phase_iteration": f32["phase_iteration"],
         "fp32c_restart_rounds": {"value": f32r["rate"], "ms_per_step": f32r["ms_per_step"],
                                  "rounds_per_step": f32r["rounds"], "stationary": f32r["late"],
                                  "component_mismatches_vs_pair_rounds": int(np.count_nonzero(f32r["comp"] != f32["comp"]))},
@@ -623,7 +640,7 @@ def run_cluster_compare(lib, gpu, torch, device, steps, warmup):
     two iterations (grid-wide restart sweep against a cluster of 16)."""
     def one(d_bed, N, M, y, kind, form, cluster, group=None, S=S1, n_steps=steps, n_warm=warmup, spec=0):
         ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=form, S=S, seed=SEED, device=device, gram=-1,
-                                       spec_width=spec,
+                                       pair_rounds=-1, spec_width=spec,
                                        refresh_every=REFRESH if form == gpu.FORM_FP32C else 0, cluster=cluster),
                        lib=lib)
         ch.pack_bed_device(d_bed.data_ptr(), d_bed.numel())

@@ -54,6 +54,7 @@
  *   brr_set_wait_limit,   no counterpart: limits of the device-side waits, the
  *   brr_get_gram_info,    marker Gram of the blocked sweep, and phase counters
  *   brr_get_gram_entries,
+ *   brr_get_round_info,
  *   brr_get_phase_cycles, (the device counterpart of the timing log above)
  *   brr_set_profiling
  *   brr_batch_*,          no single counterpart: each chain (instance) is
@@ -110,11 +111,7 @@ typedef struct brr_config {
     int32_t grid;              /* CTAs of the persistent sweep (0: one per SM) */
     int32_t device;            /* CUDA device ordinal */
     int32_t gram;              /* FP32C dense: 0 blocked sweep with a precomputed marker Gram when it fits
-                                  in device memory, -1 never, 1 required; FP32C ragged (not Eigen):
-                                  rounds of up to 32 markers resolved whole with integer pair terms
-                                  of the round's markers, 0 in the sweeps that follow one with more
-                                  than M/40 non-zero effects (and the first), 1 in every sweep,
-                                  -1 never */
+                                  in device memory, -1 never, 1 required */
     int32_t async_batch;       /* 0: the synchronous sweep (ppbayes); T in 1..64: the asyncppbayes
                                   schedule of the reference's ParallelGraph with T analysis tokens
                                   (src/parallelgraph.cpp:51-150): the T markers of a batch all read
@@ -125,6 +122,12 @@ typedef struct brr_config {
                                   one thread-block cluster of C CTAs, each holding its slice of the
                                   residual in shared memory and storing its partial sums into every
                                   CTA's shared memory (no Gram-blocked form; gram must not be 1) */
+    int32_t pair_rounds;       /* FP32C restart sweep (ragged markers other than Eigen, and dense markers
+                                  without the Gram-blocked sweep): rounds of up to 32 markers resolved
+                                  whole with exact integer pair terms of the round's markers.  0: ragged
+                                  markers in the first sweep and after any sweep that leaves more than
+                                  M/40 non-zero effects, dense markers never; 1: in every sweep;
+                                  -1: never */
 } brr_config;
 
 /* Chain state; arrays are caller-owned, sized M (beta, comp, acum) and N (eps).
@@ -240,11 +243,14 @@ int brr_xbeta_noalloc(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_
  * than exist, so that tests can exercise the timeout path without a fault. */
 int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arrivals);
 
-/* Whether the chain resolves whole blocks per round (the Gram-blocked FP32C
- * dense sweep, or pair-resolved FP32C ragged rounds), the device time of
+/* Whether the chain runs the Gram-blocked FP32C dense sweep, the device time of
  * building the packed marker Gram (ms: decode, GEMMs and combine, without the
  * allocations and the library's initialisation) and its size in bytes. */
 int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes);
+
+/* Whether the chain can take pair-resolved rounds, and whether its last sweep
+ * took them. */
+int brr_get_round_info(brr_ctx *ctx, int32_t *pair_rounds, int32_t *last_sweep_pair_rounds);
 
 /* Entries G[j[i], k[i]] = x_j . x_k (j > k) of the marker Gram of a blocked
  * chain, for i < n, into out (a check of the build; one copy per entry). */

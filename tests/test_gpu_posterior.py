@@ -62,22 +62,24 @@ def dataset(N, M, seed, miss=0.0, p_lo=0.05):
     return g, bed, y
 
 
-@pytest.mark.parametrize("kind,miss,refresh,gram", [
-    (gpu.KIND_DENSE, 0.0, 50, 1),      # Gram-blocked FP32C dense sweep
-    (gpu.KIND_RAGGED, 0.01, 5, -1),    # FP32C restart sweep, ragged markers, refresh every 5 sweeps
-    (gpu.KIND_RAGGED, 0.01, 5, 0),     # FP32C pair-resolved rounds, ragged markers
+@pytest.mark.parametrize("kind,miss,refresh,gram,pair_rounds", [
+    (gpu.KIND_DENSE, 0.0, 50, 1, 0),      # Gram-blocked FP32C dense sweep
+    (gpu.KIND_RAGGED, 0.01, 5, -1, -1),   # FP32C restart rounds, ragged markers, refresh every 5 sweeps
+    (gpu.KIND_RAGGED, 0.01, 5, -1, 1),    # FP32C pair-resolved rounds, ragged markers
+    (gpu.KIND_DENSE, 0.01, 5, -1, 1),     # FP32C pair-resolved rounds, dense markers
 ])
-def test_fp32c_posterior_means_match_fp64_oracle(gpu_lib, kind, miss, refresh, gram):
+def test_fp32c_posterior_means_match_fp64_oracle(gpu_lib, kind, miss, refresh, gram, pair_rounds):
     N, M, iters, burn = 3000, 700, 40, 10
     _, bed, y = dataset(N, M, seed=131, miss=miss, p_lo=0.01)
     group = (np.arange(M) % 2).astype(np.int32)
     ch = gpu.Chain(gpu.ChainConfig(N=N, M=M, kind=kind, form=gpu.FORM_FP32C, S=S2, seed=17,
-                                   refresh_every=refresh, gram=gram))
+                                   refresh_every=refresh, gram=gram, pair_rounds=pair_rounds))
     ch.pack_bed(bed)
     ch.set_groups(group)
     ch.set_phenotype(y)
     ch.init()
-    assert ch.gram_info()["blocked"] == (gram >= 0)
+    assert ch.gram_info()["blocked"] == (gram == 1)
+    assert ch.round_info()["pair_rounds"] == (pair_rounds == 1)
     oc = O.OracleChain(bed, N, y, S2, kind=kind, group=group, seed=17)
     pg, po = Posterior(M, 2), Posterior(M, 2)
     for it in range(iters):
