@@ -701,6 +701,7 @@ int prepare_blocked(brr_ctx *c)
         return fail(BRR_ERR_CUDA, "building the marker Gram failed: " + why);
     }
     c->gram_ms = ms;
+    c->gram_bits = gram_route_bits();
     c->blocked = true;
     return BRR_OK;
 }
@@ -1421,6 +1422,14 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
         *build_ms = ctx->gram_ms;
     if (bytes)
         *bytes = ctx->d_gram ? (int64_t)(ctx->cfg.M * (ctx->cfg.M - 1) / 2) * (int64_t)sizeof(double) : 0;
+    return BRR_OK;
+}
+
+int brr_get_gram_bits(brr_ctx *ctx, int32_t *bits)
+{
+    if (!ctx || !bits)
+        return fail(BRR_ERR_ARG, "null argument");
+    *bits = ctx->d_gram ? ctx->gram_bits : 0;
     return BRR_OK;
 }
 

@@ -62,6 +62,7 @@ struct brr_ctx {
     bool pair_rounds = false;   // FP32C restart sweep: pair-resolved rounds available (pair terms in
                                 // d_acc + kPairOffset)
     bool last_pair = false;     // the last sweep took pair-resolved rounds
+    int gram_bits = 0;          // element bits of the marker Gram's GEMM operands (FP4, FP8 or BF16)
     int64_t last_nnz = -1;      // markers in a non-zero component after the last sweep (-1: not known)
     bool has_missing = false;
     int kind = BRR_KIND_DENSE;          // storage: dense codes, or ragged lists (Ragged and Eigen markers)

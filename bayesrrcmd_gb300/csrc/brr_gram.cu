@@ -10,11 +10,12 @@
 //   P = g_j . g_k,  Q_jk = g_j . m_k,  R = m_j . m_k
 // (missing genotypes take the value (mean - colmean) * sigma, which is zero up
 // to the rounding of the two means and is left out).  P, Q, R are integer
-// sums below 2^24.  They come from FP8 (E4M3, in which 0, 1 and 2 are exact)
-// GEMMs with FP32 accumulation on tiles of 8,192 markers (cuBLASLt, a plain
-// library GEMM); every product and partial sum is an integer below 2^24, so
-// the FP32 results are exact.  Where the library offers no FP8 algorithm for
-// the shapes the build uses BF16 GEMMs instead.  The FP64 combination runs in
+// sums below 2^24.  They come from FP4 (E2M1, block scales all 1) or FP8
+// (E4M3) GEMMs with FP32 accumulation on tiles of 8,192 markers (cuBLASLt, a
+// plain library GEMM); 0, 1 and 2 are exact in both, every product and partial
+// sum is an integer below 2^24, so the FP32 results are exact.  The build takes
+// the first of FP4, FP8 and BF16 for which the library has an algorithm for
+// every tile shape.  The FP64 combination runs in
 // k_gram_combine, one CTA row per marker j of the tile.
 #include <cublasLt.h>
 #include <cublas_v2.h>
@@ -115,6 +116,40 @@ __global__ void k_decode_fp8(const uint8_t *__restrict__ codes, int64_t col_stri
     }
 }
 
+// Rows [0, M) of the genotype matrix as FP4 E2M1 (two individuals per byte,
+// the first in the low half; row length npad, a multiple of 128, padding zero)
+// and optionally the non-missing indicator; one thread per 16 individuals.
+__global__ void k_decode_fp4(const uint8_t *__restrict__ codes, int64_t col_stride, int64_t N, int64_t npad,
+                             int64_t M, uint8_t *__restrict__ gp, uint8_t *__restrict__ nm)
+{
+    const int64_t groups = npad / 16;
+    const int64_t total = M * groups;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / groups;
+        const int64_t q = e - r * groups;
+        // the code bytes of individuals past the column's stored bytes are not read
+        const int64_t b0 = 4 * q;
+        uint32_t v = 0x55555555u;
+        if (b0 + 4 <= col_stride)
+            v = *reinterpret_cast<const uint32_t *>(codes + r * col_stride + b0);
+        uint32_t g[2] = {0u, 0u}, m[2] = {0u, 0u};
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const unsigned c = (v >> (2 * k)) & 3u;
+            const bool valid = 16 * q + k < N;
+            // code 0: genotype 2 (E2M1 0x4), code 2: genotype 1 (0x2), code 3: 0, code 1: missing
+            const uint32_t gb = !valid ? 0u : (c == 0u ? 0x4u : (c == 2u ? 0x2u : 0u));
+            const uint32_t mb = (valid && c != 1u) ? 0x2u : 0u;
+            g[k >> 3] |= gb << (4 * (k & 7));
+            m[k >> 3] |= mb << (4 * (k & 7));
+        }
+        reinterpret_cast<uint2 *>(gp + r * (npad / 2))[q] = make_uint2(g[0], g[1]);
+        if (nm)
+            reinterpret_cast<uint2 *>(nm + r * (npad / 2))[q] = make_uint2(m[0], m[1]);
+    }
+}
+
 // Rows [0, M) of the genotype matrix as BF16 (row length npad, padding zero),
 // and optionally the non-missing indicator.
 __global__ void k_decode_bf16(const uint8_t *__restrict__ codes, int64_t col_stride, int64_t N, int64_t npad,
@@ -144,31 +179,49 @@ constexpr int64_t kTile = 8192;
 constexpr size_t kLtWorkspace = (size_t)64 << 20;
 
 inline int64_t round16(int64_t x) { return (x + 15) / 16 * 16; }
+inline int64_t round128(int64_t x) { return (x + 127) / 128 * 128; }
+int g_route_bits = 0;   // element bits of the last Gram build's GEMM operands
 
-// FP8 GEMMs through cuBLASLt: out (tk x tj, column-major, k fastest, leading
-// dimension ld) = A(rows k0..) * B(rows j0..)^T over the npad-long rows.
-struct Fp8Gemm {
+// FP4 or FP8 GEMMs through cuBLASLt: out (tk x tj, column-major, k fastest,
+// leading dimension ld) = A(rows k0..) * B(rows j0..)^T over the npad-long
+// rows.  FP4 operands carry a UE4M3 scale per 16 elements along a row, all 1.0
+// here (`scales`, sized for the largest operand of the build).
+struct LtGemm {
     cublasLtHandle_t h = nullptr;
     cublasLtMatmulDesc_t op = nullptr;
     cublasLtMatmulPreference_t pref = nullptr;
     void *ws = nullptr;
     int64_t npad = 0;
+    cudaDataType_t type = CUDA_R_8F_E4M3;
 
-    bool init(int64_t np)
+    bool init(int64_t np, cudaDataType_t t, const void *scales)
     {
         npad = np;
+        type = t;
         const cublasOperation_t ta = CUBLAS_OP_T, tb = CUBLAS_OP_N;
         size_t wsb = kLtWorkspace;
-        return cublasLtCreate(&h) == CUBLAS_STATUS_SUCCESS &&
-               cublasLtMatmulDescCreate(&op, CUBLAS_COMPUTE_32F, CUDA_R_32F) == CUBLAS_STATUS_SUCCESS &&
-               cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)) ==
-                   CUBLAS_STATUS_SUCCESS &&
-               cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)) ==
-                   CUBLAS_STATUS_SUCCESS &&
-               cublasLtMatmulPreferenceCreate(&pref) == CUBLAS_STATUS_SUCCESS &&
-               cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &wsb,
-                                                    sizeof(wsb)) == CUBLAS_STATUS_SUCCESS &&
-               cudaMalloc(&ws, kLtWorkspace) == cudaSuccess;
+        bool ok = cublasLtCreate(&h) == CUBLAS_STATUS_SUCCESS &&
+                  cublasLtMatmulDescCreate(&op, CUBLAS_COMPUTE_32F, CUDA_R_32F) == CUBLAS_STATUS_SUCCESS &&
+                  cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)) ==
+                      CUBLAS_STATUS_SUCCESS &&
+                  cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)) ==
+                      CUBLAS_STATUS_SUCCESS &&
+                  cublasLtMatmulPreferenceCreate(&pref) == CUBLAS_STATUS_SUCCESS &&
+                  cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &wsb,
+                                                       sizeof(wsb)) == CUBLAS_STATUS_SUCCESS &&
+                  cudaMalloc(&ws, kLtWorkspace) == cudaSuccess;
+        if (ok && t == CUDA_R_4F_E2M1) {
+            const int32_t mode = CUBLASLT_MATMUL_MATRIX_SCALE_VEC16_UE4M3;
+            ok = cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_A_SCALE_MODE, &mode, sizeof(mode)) ==
+                     CUBLAS_STATUS_SUCCESS &&
+                 cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_B_SCALE_MODE, &mode, sizeof(mode)) ==
+                     CUBLAS_STATUS_SUCCESS &&
+                 cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_A_SCALE_POINTER, &scales, sizeof(scales)) ==
+                     CUBLAS_STATUS_SUCCESS &&
+                 cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_B_SCALE_POINTER, &scales, sizeof(scales)) ==
+                     CUBLAS_STATUS_SUCCESS;
+        }
+        return ok;
     }
     // 0: done; 1: no algorithm for the shape (nothing launched); -1: error.
     // With A, B null: only the query for an algorithm.
@@ -176,8 +229,8 @@ struct Fp8Gemm {
     {
         cublasLtMatrixLayout_t la = nullptr, lb = nullptr, lc = nullptr;
         int rc = -1;
-        if (cublasLtMatrixLayoutCreate(&la, CUDA_R_8F_E4M3, npad, tk, npad) == CUBLAS_STATUS_SUCCESS &&
-            cublasLtMatrixLayoutCreate(&lb, CUDA_R_8F_E4M3, npad, tj, npad) == CUBLAS_STATUS_SUCCESS &&
+        if (cublasLtMatrixLayoutCreate(&la, type, npad, tk, npad) == CUBLAS_STATUS_SUCCESS &&
+            cublasLtMatrixLayoutCreate(&lb, type, npad, tj, npad) == CUBLAS_STATUS_SUCCESS &&
             cublasLtMatrixLayoutCreate(&lc, CUDA_R_32F, tk, tj, ld) == CUBLAS_STATUS_SUCCESS) {
             cublasLtMatmulHeuristicResult_t hr{};
             int n = 0;
@@ -202,7 +255,7 @@ struct Fp8Gemm {
             cublasLtMatrixLayoutDestroy(lc);
         return rc;
     }
-    ~Fp8Gemm()
+    ~LtGemm()
     {
         if (pref)
             cublasLtMatmulPreferenceDestroy(pref);
@@ -219,7 +272,7 @@ struct Fp8Gemm {
 cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work)
 {
     const int64_t npad = round16(N);
-    const int64_t T = round16(std::min<int64_t>(M, kTile));
+    const int64_t T = round128(std::min<int64_t>(M, kTile));
     *gram = (size_t)(M * (M - 1) / 2) * sizeof(double);
     // the BF16 route's rows (2 bytes per genotype) bound the FP8 route's (1 byte)
     *work = (size_t)round16(M) * npad * 2 * (missing ? 2 : 1) + (size_t)T * T * 4 * (missing ? 4 : 1) +
@@ -230,13 +283,12 @@ cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, 
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
                const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why, float *device_ms)
 {
-    // FP8 rows and tile sides are multiples of 16 (padding rows and columns
-    // are zero and their products are not read)
-    const int64_t npad = round16(N);
-    const int64_t Mp = round16(M);
+    // FP4 rows are multiples of 128 elements, FP8 and BF16 rows of 16; tile
+    // sides are multiples of 128 (FP4) or 16 (padding rows and columns are
+    // zero and their products are not read)
     const int64_t T = std::min<int64_t>(M, kTile);
-    const int64_t Tp = round16(T);
-    void *gp = nullptr, *nm = nullptr;
+    const int64_t Tp = round128(T);
+    void *gp = nullptr, *nm = nullptr, *scales = nullptr;
     float *tiles = nullptr;
     double *cst = nullptr;
     int rc = 0;
@@ -253,45 +305,64 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     cu(cudaMalloc(&cst, sizeof(double) * 4 * (size_t)M), "allocation of the per-marker constants");
     float *P = tiles, *Q1 = missing ? tiles + (size_t)Tp * Tp : nullptr,
           *Q2 = missing ? tiles + 2 * (size_t)Tp * Tp : nullptr, *R = missing ? tiles + 3 * (size_t)Tp * Tp : nullptr;
-
-    // the FP8 route when the library has an algorithm for the full tile
-    Fp8Gemm f8;
-    bool fp8 = rc == 0 && f8.init(npad);
     if (rc == 0)
         cu(cudaEventRecord(ev[0], st), "event");
-    if (fp8) {
-        cu(cudaMalloc(&gp, (size_t)Mp * npad), "allocation of the FP8 genotypes");
-        if (missing)
-            cu(cudaMalloc(&nm, (size_t)Mp * npad), "allocation of the FP8 indicators");
-        if (rc == 0) {
-            cu(cudaMemsetAsync(gp, 0, (size_t)Mp * npad, st), "clear");
-            if (nm)
-                cu(cudaMemsetAsync(nm, 0, (size_t)Mp * npad, st), "clear");
+
+    // the first route with an algorithm for every tile shape of the build: full
+    // tiles and the last one
+    const int64_t last = M - (M - 1) / T * T;
+    int bits = 0;          // 4, 8 (cuBLASLt) or 16 (BF16 cublasGemmEx)
+    int64_t npad = 0, Mp = 0;
+    LtGemm lt;
+    for (int cand : {4, 8}) {
+        if (rc)
+            break;
+        const int64_t np = cand == 4 ? round128(N) : round16(N);
+        const int64_t side = cand == 4 ? 128 : 16;
+        if (cand == 4) {
+            // UE4M3 scale 1.0 (0x38) for every 16 elements of the largest operand
+            const size_t sbytes = (size_t)Tp * (size_t)(((np / 16) + 3) / 4 * 4);
+            cu(cudaMalloc(&scales, sbytes), "allocation of the FP4 block scales");
+            if (rc == 0)
+                cu(cudaMemsetAsync(scales, 0x38, sbytes, st), "scales");
         }
-        // an algorithm for every tile shape of the build: full tiles and the last
-        for (int64_t a = 0; a < 2 && fp8; ++a)
-            for (int64_t b = 0; b < 2 && fp8; ++b) {
-                const int64_t sa = a ? round16(M - (M - 1) / T * T) : Tp, sb = b ? round16(M - (M - 1) / T * T) : Tp;
-                fp8 = f8.run(nullptr, nullptr, sa, sb, Tp, P, st) == 0;
+        LtGemm trial;
+        bool ok = rc == 0 && trial.init(np, cand == 4 ? CUDA_R_4F_E2M1 : CUDA_R_8F_E4M3, scales);
+        for (int a = 0; a < 2 && ok; ++a)
+            for (int b = 0; b < 2 && ok; ++b) {
+                const int64_t sa = a ? (last + side - 1) / side * side : Tp;
+                const int64_t sb = b ? (last + side - 1) / side * side : Tp;
+                ok = trial.run(nullptr, nullptr, sa, sb, Tp, P, st) == 0;
             }
-        if (!fp8) {
-            cudaFree(gp);
-            cudaFree(nm);
-            gp = nm = nullptr;
+        if (ok) {
+            bits = cand;
+            npad = np;
+            Mp = (M + side - 1) / side * side + (Tp - T);
+            lt.init(np, cand == 4 ? CUDA_R_4F_E2M1 : CUDA_R_8F_E4M3, scales);
+            break;
+        }
+        if (cand == 4) {
+            cudaFree(scales);
+            scales = nullptr;
         }
     }
-    if (!fp8) {
-        cu(cudaMalloc(&gp, sizeof(__nv_bfloat16) * (size_t)Mp * npad), "allocation of the BF16 genotypes");
-        if (missing)
-            cu(cudaMalloc(&nm, sizeof(__nv_bfloat16) * (size_t)Mp * npad), "allocation of the BF16 indicators");
-        if (rc == 0) {
-            cu(cudaMemsetAsync(gp, 0, sizeof(__nv_bfloat16) * (size_t)Mp * npad, st), "clear");
-            if (nm)
-                cu(cudaMemsetAsync(nm, 0, sizeof(__nv_bfloat16) * (size_t)Mp * npad, st), "clear");
-        }
+    if (bits == 0) {
+        bits = 16;
+        npad = round16(N);
+        Mp = round16(M);
+    }
+    // genotype and indicator rows: half a byte, a byte or two bytes per individual
+    const size_t row_bytes = bits == 4 ? (size_t)npad / 2 : (size_t)npad * (bits / 8);
+    cu(cudaMalloc(&gp, (size_t)Mp * row_bytes), "allocation of the decoded genotypes");
+    if (missing)
+        cu(cudaMalloc(&nm, (size_t)Mp * row_bytes), "allocation of the decoded indicators");
+    if (rc == 0) {
+        cu(cudaMemsetAsync(gp, 0, (size_t)Mp * row_bytes, st), "clear");
+        if (nm)
+            cu(cudaMemsetAsync(nm, 0, (size_t)Mp * row_bytes, st), "clear");
     }
     cublasHandle_t hb = nullptr;
-    if (rc == 0 && !fp8) {
+    if (rc == 0 && bits == 16) {
         if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) {
             why = "cublasCreate failed";
             rc = -1;
@@ -300,7 +371,9 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
         }
     }
     if (rc == 0) {
-        if (fp8)
+        if (bits == 4)
+            k_decode_fp4<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, M, (uint8_t *)gp, (uint8_t *)nm);
+        else if (bits == 8)
             k_decode_fp8<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, M, (uint8_t *)gp, (uint8_t *)nm);
         else
             k_decode_bf16<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, M, (__nv_bfloat16 *)gp,
@@ -313,9 +386,10 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     auto gemm = [&](const void *A, const void *B, int64_t k0, int64_t tk, int64_t j0, int64_t tj, float *out) {
         if (rc)
             return;
-        if (fp8) {
-            if (f8.run((const uint8_t *)A + k0 * npad, (const uint8_t *)B + j0 * npad, tk, tj, Tp, out, st) != 0) {
-                why = "cuBLASLt FP8 GEMM failed";
+        if (bits != 16) {
+            if (lt.run((const uint8_t *)A + k0 * row_bytes, (const uint8_t *)B + j0 * row_bytes, tk, tj, Tp, out,
+                       st) != 0) {
+                why = "cuBLASLt low-precision GEMM failed";
                 rc = -1;
             }
             return;
@@ -329,12 +403,14 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
             rc = -1;
         }
     };
+    const int64_t side = bits == 4 ? 128 : 16;
     for (int64_t j0 = 0; j0 < M && rc == 0; j0 += T) {
         const int64_t tj = std::min<int64_t>(T, M - j0);
         for (int64_t k0 = 0; k0 <= j0 && rc == 0; k0 += T) {
             const int64_t tk = std::min<int64_t>(T, M - k0);
-            // FP8 sides rounded up to 16 (rows up to Mp exist and are zero)
-            const int64_t gk = fp8 ? round16(tk) : tk, gj = fp8 ? round16(tj) : tj;
+            // low-precision tile sides rounded up (those rows exist and are zero)
+            const int64_t gk = bits != 16 ? (tk + side - 1) / side * side : tk;
+            const int64_t gj = bits != 16 ? (tj + side - 1) / side * side : tj;
             gemm(gp, gp, k0, gk, j0, gj, P);             // P[j,k]  = g_j . g_k
             if (missing) {
                 gemm(nm, gp, k0, gk, j0, gj, Q1);        // Q1[j,k] = g_j . m_k
@@ -360,9 +436,13 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
         cublasDestroy(hb);
     cudaFree(gp);
     cudaFree(nm);
+    cudaFree(scales);
     cudaFree(tiles);
     cudaFree(cst);
+    g_route_bits = rc == 0 ? bits : 0;
     return rc;
 }
+
+int gram_route_bits() { return g_route_bits; }
 
 }  // namespace brr

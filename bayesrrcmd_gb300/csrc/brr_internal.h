@@ -260,5 +260,7 @@ cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, 
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
                const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why,
                float *device_ms);
+// Element bits of the last successful Gram build's GEMM operands (4, 8 or 16).
+int gram_route_bits();
 
 }  // namespace brr

@@ -65,6 +65,7 @@ EXPORTS = [
     "brr_get_gram_info",
     "brr_get_gram_entries",
     "brr_get_round_info",
+    "brr_get_gram_bits",
     "brr_batch_create", "brr_batch_destroy", "brr_batch_pack_bed", "brr_batch_pack_bed_device",
     "brr_batch_set_groups", "brr_batch_set_phenotypes", "brr_batch_init", "brr_batch_iterate",
     "brr_batch_get_chain_state", "brr_batch_get_timing", "brr_batch_set_wait_limit", "brr_batch_set_profiling",
@@ -113,6 +114,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
     lib.brr_get_gram_entries.argtypes = [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int64,
                                          C.POINTER(C.c_double)]
     lib.brr_get_round_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.brr_get_gram_bits.argtypes = [P, C.POINTER(C.c_int32)]
     lib.brr_xbeta.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
     lib.brr_xbeta_noalloc.argtypes = [P, C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_int64, P]
     lib.brr_synth_bed_device.argtypes = [P, C.c_int64, C.c_int64, C.c_uint32, C.c_double, C.c_double, C.c_double]
@@ -378,9 +380,10 @@ class Chain:
         return dict(pair_rounds=bool(pr.value), last_sweep_pair_rounds=bool(last.value))
 
     def gram_info(self):
-        b, ms, n = C.c_int32(), C.c_double(), C.c_int64()
+        b, ms, n, bits = C.c_int32(), C.c_double(), C.c_int64(), C.c_int32()
         self._check(self.lib.brr_get_gram_info(self.h, C.byref(b), C.byref(ms), C.byref(n)))
-        return dict(blocked=bool(b.value), build_ms=ms.value, bytes=n.value)
+        self._check(self.lib.brr_get_gram_bits(self.h, C.byref(bits)))
+        return dict(blocked=bool(b.value), build_ms=ms.value, bytes=n.value, operand_bits=bits.value)
 
     def phase_cycles(self) -> np.ndarray:
         out = np.zeros(16, np.int64)

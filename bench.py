@@ -997,6 +997,7 @@ def main():
         "fp64_fallbacks_per_step": fp32c["phases"][8] / PROFILE_STEPS,
         "rounds_per_step": fp32c["rounds"] / args.steps,
         "gram": {"blocked_sweep": fp32c["gram"]["blocked"], "build_ms": fp32c["gram"]["build_ms"],
+                 "gemm_operand_bits": fp32c["gram"].get("operand_bits"),
                  "bytes": fp32c["gram"]["bytes"]},
         "gpu_launches": 5 * args.steps + (args.steps + args.warmup) // REFRESH,
         "clocks": clk.summary(),

@@ -55,6 +55,7 @@
  *   brr_get_gram_info,    marker Gram of the blocked sweep, and phase counters
  *   brr_get_gram_entries,
  *   brr_get_round_info,
+ *   brr_get_gram_bits,
  *   brr_get_phase_cycles, (the device counterpart of the timing log above)
  *   brr_set_profiling
  *   brr_batch_*,          no single counterpart: each chain (instance) is
@@ -247,6 +248,10 @@ int brr_set_wait_limit(brr_ctx *ctx, uint64_t timeout_ns, int32_t phantom_arriva
  * building the packed marker Gram (ms: decode, GEMMs and combine, without the
  * allocations and the library's initialisation) and its size in bytes. */
 int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t *bytes);
+
+/* Element bits of the GEMM operands the marker Gram was built from: 4 (FP4
+ * E2M1), 8 (FP8 E4M3) or 16 (BF16); 0 without a Gram. */
+int brr_get_gram_bits(brr_ctx *ctx, int32_t *bits);
 
 /* Whether the chain can take pair-resolved rounds, and whether its last sweep
  * took them. */

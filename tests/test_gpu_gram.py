@@ -3,8 +3,9 @@ evaluation, through the C ABI.
 
 G[j,k] = x_j . x_k with x_j(i) = sigma_j (g_j(i) - colmean_j) for a genotype
 that is present and 0 for a missing one (the dense table's value of each code).
-The build forms the integer sums P, Q, R with low-precision GEMMs whose
-products and partial sums are integers below 2^24, so they are exact; a unit
+The build forms the integer sums P, Q, R with FP4, FP8 or BF16 GEMMs (the first
+the library has algorithms for) whose products and partial sums are integers
+below 2^24, so they are exact; a unit
 error in any of them moves G by sigma_j sigma_k >= 2, far above the bar
 (absolute 1e-8, against entries up to N).  Cases: N = 100,000 with markers of
 allele frequency 0.6-0.99 (P up to 4N), N = 100,000 with 1 % missing genotypes
@@ -26,7 +27,8 @@ def chain_with_gram(g):
     y = np.linspace(-1.0, 1.0, N).astype(np.float32)
     ch.set_phenotype(y)
     ch.init()
-    assert ch.gram_info()["blocked"]
+    info = ch.gram_info()
+    assert info["blocked"] and info["operand_bits"] in (4, 8, 16)
     return ch
 
 
