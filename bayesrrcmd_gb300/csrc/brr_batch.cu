@@ -44,6 +44,7 @@ namespace {
 
 constexpr int kBT = 256;               // threads per CTA
 constexpr int kBW = kBT / 32;
+static_assert(kBW == 8, "the update pass deals tiles to two groups of four warps");
 constexpr int kTmemCols = 512;
 constexpr int kCounterGap = 32;        // words between the two barrier counters
 constexpr long long kLimbHalf = 1024;  // balanced limbs in [-1024, 1023]
@@ -686,11 +687,14 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
             }
             ++mphase;
             tc_fence_after();
-            const int it = warp >> 2, q4 = warp & 3;
-            if (it < nt) {
+            // the pass's tiles dealt to the two groups of four warps in pairs;
+            // an odd last tile split between them by chains (both groups read
+            // the same TMEM lanes, the warp's quarter, at other columns)
+            const int q4 = warp & 3, wg = warp >> 2;
+            auto update_tile = [&](int it, int ck0, int ck1) {
                 const int i = (t0p + it) * 128 + q4 * 32 + lane;
                 bool ok = true;
-                for (int ck = 0; ck < R / 32; ++ck) {
+                for (int ck = ck0; ck < ck1; ++ck) {
                     float f[32];
                     tmem_ld32(tmem + ((unsigned)(q4 * 32) << 16) + (unsigned)(it * R + ck * 32), f);
                     if (i < ns) {
@@ -729,7 +733,11 @@ __global__ void __launch_bounds__(kBT, 1) k_sweep_batch(BatchArgs a)
                 }
                 if (!ok)
                     atomicCAS(a.err, kDevOk, kDevRange);
-            }
+            };
+            for (int it = wg; it < (nt & ~1); it += 2)
+                update_tile(it, 0, R / 32);
+            if (nt & 1)
+                update_tile(nt - 1, wg * (R / 64), (wg + 1) * (R / 64));
             fence_async_smem();
             tc_fence_before();
             __syncthreads();

@@ -70,6 +70,22 @@ def test_batch_matches_oracle_each_iteration(gpu_lib, N, M, C, chains_checked):
             compare(b.state(c), oc.state(), f"iteration {it} chain {c}")
 
 
+@pytest.mark.parametrize("N,C,grid,chains_checked", [
+    (3200, 32, 8, [0, 5, 31]),     # 400 individuals per slice: four update tiles in one TMEM pass
+    (4800, 64, 16, [0, 33, 63]),   # 300 per slice: three tiles, the last split by chains
+])
+def test_batch_update_tiles_of_large_slices(gpu_lib, N, C, grid, chains_checked):
+    M = 96
+    bed, ys = problem(N, M, C, seed=N % 89 + C)
+    b = make_batch(bed, N, ys, S1, C, seed=7, chain0=3, grid=grid)
+    oracles = {c: O.OracleChain(bed, N, ys[c], S1, seed=7, chain=3 + c, perm_chain=3) for c in chains_checked}
+    for it in range(3):
+        b.iterate(1)
+        for c, oc in oracles.items():
+            oc.iterate(it)
+            compare(b.state(c), oc.state(), f"iteration {it} chain {c}")
+
+
 def test_batch_two_groups(gpu_lib):
     N, M, C = 1500, 200, 32
     bed, ys = problem(N, M, C, seed=3)
