@@ -654,6 +654,13 @@ int prepare_blocked(brr_ctx *c)
         c->blocked = true;
         return BRR_OK;
     }
+    // the combination's 64-bit numerators hold 16 N^3
+    if (cf.N > 800000) {
+        if (cf.gram > 0)
+            return fail(BRR_ERR_ARG, "the marker Gram needs N <= 800,000");
+        c->blocked = false;
+        return BRR_OK;
+    }
     size_t gram_bytes = 0, work = 0, free_b = 0, total_b = 0;
     gram_bytes_needed(cf.N, cf.M, c->has_missing, &gram_bytes, &work);
     BRR_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -1421,7 +1428,7 @@ int brr_get_gram_info(brr_ctx *ctx, int32_t *blocked, double *build_ms, int64_t 
     if (build_ms)
         *build_ms = ctx->gram_ms;
     if (bytes)
-        *bytes = ctx->d_gram ? (int64_t)(ctx->cfg.M * (ctx->cfg.M - 1) / 2) * (int64_t)sizeof(double) : 0;
+        *bytes = ctx->d_gram ? (int64_t)(ctx->cfg.M * (ctx->cfg.M - 1) / 2) * (int64_t)sizeof(float2) : 0;
     return BRR_OK;
 }
 
@@ -1456,9 +1463,11 @@ int brr_get_gram_entries(brr_ctx *ctx, const int64_t *j, const int64_t *k, int64
             return fail(BRR_ERR_ARG, "Gram entries need M > j > k >= 0");
     BRR_CUDA(cudaSetDevice(ctx->dev));
     BRR_CUDA(cudaStreamSynchronize(ctx->st));
-    for (int64_t i = 0; i < n; ++i)
-        BRR_CUDA(cudaMemcpy(out + i, ctx->d_gram + j[i] * (j[i] - 1) / 2 + k[i], sizeof(double),
-                            cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < n; ++i) {
+        float2 v;
+        BRR_CUDA(cudaMemcpy(&v, ctx->d_gram + j[i] * (j[i] - 1) / 2 + k[i], sizeof(float2), cudaMemcpyDeviceToHost));
+        out[i] = (double)v.x + (double)v.y;
+    }
     return BRR_OK;
 }
 

@@ -679,9 +679,9 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     // signal before the barrier arrival (more than kGather entries per lane, on
     // grids below 80 CTAs, are loaded when stored).
     constexpr int kGather = 4;
-    double gval[kGather] = {0.0, 0.0, 0.0, 0.0};
+    float2 gval[kGather];
     int gent_mine[kGather] = {-1, -1, -1, -1};
-    auto gram_entry = [&](int q, unsigned e, double *out) -> bool {
+    auto gram_entry = [&](int q, unsigned e, float2 *out) -> bool {
         const unsigned q0 = (unsigned)q * Bu;
         const int nbq = nb_of(q);
         unsigned pa, pb, qa;
@@ -718,22 +718,17 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
                 gent_mine[k] = (int)e;
         }
     };
-    auto split2 = [](double v) {
-        float h, l;
-        df_from_double(v, h, l);
-        return make_float2(h, l);
-    };
     auto gather_store = [&](int q) {
         float2 *slot = gstage + (size_t)(q % kStageSlots) * gst;
 #pragma unroll
         for (int k = 0; k < kGather; ++k)
             if (gent_mine[k] >= 0)
-                slot[gent_mine[k]] = split2(gval[k]);
+                slot[gent_mine[k]] = gval[k];
         for (unsigned e = (unsigned)sidx + (unsigned)(lane + 32 * kGather) * (unsigned)a.G; e < gst;
              e += 32u * (unsigned)a.G) {
-            double v;
+            float2 v;
             if (gram_entry(q, e, &v))
-                slot[e] = split2(v);
+                slot[e] = v;
         }
     };
 

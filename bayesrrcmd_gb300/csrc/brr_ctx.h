@@ -54,7 +54,7 @@ struct brr_ctx {
     long long *d_prof = nullptr;        // per-phase cycles of the last sweep (CTA 0)
     uint32_t *d_nzj = nullptr;
     double *d_nzb = nullptr;
-    double *d_gram = nullptr;           // blocked FP32C: packed marker Gram
+    float2 *d_gram = nullptr;           // blocked FP32C: packed marker Gram (double-float entries)
     double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries (8 blocks)
     brr::BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
     float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)

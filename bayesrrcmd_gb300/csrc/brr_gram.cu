@@ -1,6 +1,6 @@
 // Marker Gram matrix G[j,k] = x_j . x_k of the standardised dense columns,
-// stored as a packed lower triangle (entry (j, k), j > k, at j(j-1)/2 + k) in
-// FP64.  The blocked FP32C sweep uses it to resolve several markers per grid
+// stored as a packed lower triangle (entry (j, k), j > k, at j(j-1)/2 + k) as
+// double-float pairs.  The blocked FP32C sweep uses it to resolve several markers per grid
 // round exactly: after marker p changes the residual by dBeta_p * x_p, the
 // dot product of a later marker t moves by dBeta_p * G[p, t].
 //
@@ -15,8 +15,8 @@
 // plain library GEMM); 0, 1 and 2 are exact in both, every product and partial
 // sum is an integer below 2^24, so the FP32 results are exact.  The build takes
 // the first of FP4, FP8 and BF16 for which the library has an algorithm for
-// every tile shape.  The FP64 combination runs in
-// k_gram_combine, one CTA row per marker j of the tile.
+// every tile shape.  k_gram_combine forms the entries from exact 64-bit
+// integer numerators (see there), one CTA row per marker j of the tile.
 #include <cublasLt.h>
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
@@ -30,53 +30,64 @@
 namespace brr {
 
 
-// Per-marker constants of the combination: s_k, s_k c_k and, without missing
-// genotypes, w_k = s_k (q_k - c_k N) with q_k = sum of g_k; q_k itself.
+// Per-marker constants of the combination: a_k = s_k / n_k as a double-float
+// pair, and the marker's genotype sum q_k and count of present genotypes n_k.
 __global__ void k_gram_consts(int64_t M, int64_t N, const double *__restrict__ scale,
-                              const int64_t *__restrict__ counts, double *__restrict__ cst)
+                              const int64_t *__restrict__ counts, float2 *__restrict__ af,
+                              longlong2 *__restrict__ qn)
 {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M)
         return;
-    const double sk = scale[2 * k], ck = scale[2 * k + 1];
-    const double qk = (double)(counts[4 * k + 1] + 2 * counts[4 * k + 2]);
-    cst[4 * k] = sk;
-    cst[4 * k + 1] = sk * ck;
-    cst[4 * k + 2] = sk * (qk - ck * (double)N);
-    cst[4 * k + 3] = qk;
+    const long long n = (long long)(N - counts[4 * k + 3]);
+    const long long q = (long long)(counts[4 * k + 1] + 2 * counts[4 * k + 2]);
+    float h, l;
+    df_from_double(scale[2 * k] / (double)n, h, l);
+    af[k] = make_float2(h, l);
+    qn[k] = make_longlong2(q, n);
 }
 
 // Rows j in [j0, j0+tj) (one per blockIdx.y) and columns k in [k0, k0+tk),
 // k < j, of the tile.  The products are stored column-major with the k index
-// fastest: X[(j - j0) * ldp + (k - k0)].
-//   no missing genotypes: G = s_j (s_k P - (s_k c_k q_j + c_j w_k))
-//   otherwise:            G = s_j (s_k P - s_k c_k Q1 - c_j s_k Q2 + c_j s_k c_k R)
-__global__ void k_gram_combine(int64_t j0, int64_t k0, int64_t tk, int64_t ldp, const float *__restrict__ P,
-                               const float *__restrict__ Q1, const float *__restrict__ Q2,
-                               const float *__restrict__ R, const double *__restrict__ cst,
-                               const double *__restrict__ scale, double *__restrict__ G)
+// fastest: X[(j - j0) * ldp + (k - k0)].  With the column means c = q / n,
+//   G = s_j s_k (P - c_k Q1 - c_j Q2 + c_j c_k R)
+//     = a_j a_k (n_j n_k P - n_j q_k Q1 - q_j n_k Q2 + q_j q_k R),
+// the second factor an exact 64-bit integer (|terms| < 4 N^3; without missing
+// genotypes Q1 = q_j, Q2 = q_k, R = N), so the centred sum has no cancellation
+// error; it is split into a double-float pair and multiplied by a_j a_k.
+__global__ void k_gram_combine(int64_t j0, int64_t k0, int64_t tk, int64_t ldp, int64_t N,
+                               const float *__restrict__ P, const float *__restrict__ Q1,
+                               const float *__restrict__ Q2, const float *__restrict__ R,
+                               const float2 *__restrict__ af, const longlong2 *__restrict__ qn,
+                               float2 *__restrict__ G)
 {
     const int64_t a = blockIdx.y;
     const int64_t j = j0 + a;
     const int64_t kend = j - k0 < tk ? j - k0 : tk;
     if (kend <= 0)
         return;
-    const double sj = scale[2 * j], cj = scale[2 * j + 1];
-    const double qj = cst[4 * j + 3];
+    const float2 aj = af[j];
+    const longlong2 qnj = qn[j];
     const float *Prow = P + a * ldp;
-    double *Grow = G + j * (j - 1) / 2 + k0;
+    float2 *Grow = G + j * (j - 1) / 2 + k0;
     for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < kend; b += (int64_t)gridDim.x * blockDim.x) {
-        const double *ck4 = cst + 4 * (k0 + b);
-        const double sk = ck4[0], skck = ck4[1];
-        double inner;
+        const float2 ak = af[k0 + b];
+        const longlong2 qnk = qn[k0 + b];
+        const long long p = (long long)Prow[b];
+        long long q1 = qnj.x, q2 = qnk.x, r = N;
         if (Q1) {
             const int64_t e = a * ldp + b;
-            inner = ((sk * (double)Prow[b] - skck * (double)Q1[e]) - cj * (sk * (double)Q2[e])) +
-                    cj * (skck * (double)R[e]);
-        } else {
-            inner = sk * (double)Prow[b] - fma(skck, qj, cj * ck4[2]);
+            q1 = (long long)Q1[e];
+            q2 = (long long)Q2[e];
+            r = (long long)R[e];
         }
-        Grow[b] = sj * inner;
+        const long long num = qnj.y * qnk.y * p - qnj.y * qnk.x * q1 - qnj.x * qnk.y * q2 + qnj.x * qnk.x * r;
+        const float nh = __ll2float_rn(num);
+        const float nl = __ll2float_rn(num - __float2ll_rn(nh));
+        float sh, sl, gh, gl;
+        df_mul(aj.x, aj.y, ak.x, ak.y, sh, sl);
+        df_mul(sh, sl, nh, nl, gh, gl);
+        Grow[b] = make_float2(gh, gl);
     }
 }
 
@@ -273,15 +284,15 @@ cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, 
 {
     const int64_t npad = round16(N);
     const int64_t T = round128(std::min<int64_t>(M, kTile));
-    *gram = (size_t)(M * (M - 1) / 2) * sizeof(double);
+    *gram = (size_t)(M * (M - 1) / 2) * sizeof(float2);
     // the BF16 route's rows (2 bytes per genotype) bound the FP8 route's (1 byte)
     *work = (size_t)round16(M) * npad * 2 * (missing ? 2 : 1) + (size_t)T * T * 4 * (missing ? 4 : 1) +
-            (size_t)M * 32 + kLtWorkspace;
+            (size_t)M * 24 + kLtWorkspace;
     return cudaSuccess;
 }
 
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
-               const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why, float *device_ms)
+               const int64_t *counts, bool missing, float2 *G, cudaStream_t st, std::string &why, float *device_ms)
 {
     // FP4 rows are multiples of 128 elements, FP8 and BF16 rows of 16; tile
     // sides are multiples of 128 (FP4) or 16 (padding rows and columns are
@@ -290,7 +301,8 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     const int64_t Tp = round128(T);
     void *gp = nullptr, *nm = nullptr, *scales = nullptr;
     float *tiles = nullptr;
-    double *cst = nullptr;
+    float2 *af = nullptr;
+    longlong2 *qn = nullptr;
     int rc = 0;
     auto cu = [&](cudaError_t e, const char *what) {
         if (e != cudaSuccess && rc == 0) {
@@ -302,7 +314,8 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     cu(cudaEventCreate(&ev[0]), "event");
     cu(cudaEventCreate(&ev[1]), "event");
     cu(cudaMalloc(&tiles, sizeof(float) * (size_t)Tp * Tp * (missing ? 4 : 1)), "allocation of the product tiles");
-    cu(cudaMalloc(&cst, sizeof(double) * 4 * (size_t)M), "allocation of the per-marker constants");
+    cu(cudaMalloc(&af, sizeof(float2) * (size_t)M), "allocation of the per-marker constants");
+    cu(cudaMalloc(&qn, sizeof(longlong2) * (size_t)M), "allocation of the per-marker counts");
     float *P = tiles, *Q1 = missing ? tiles + (size_t)Tp * Tp : nullptr,
           *Q2 = missing ? tiles + 2 * (size_t)Tp * Tp : nullptr, *R = missing ? tiles + 3 * (size_t)Tp * Tp : nullptr;
     if (rc == 0)
@@ -379,7 +392,7 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
             k_decode_bf16<<<152 * 8, 256, 0, st>>>(codes, col_stride, N, npad, M, (__nv_bfloat16 *)gp,
                                                   (__nv_bfloat16 *)nm);
         cu(cudaGetLastError(), "decode");
-        k_gram_consts<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(M, N, scale, counts, cst);
+        k_gram_consts<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(M, N, scale, counts, af, qn);
         cu(cudaGetLastError(), "constants");
     }
     const float one = 1.f, zero = 0.f;
@@ -419,7 +432,7 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
             }
             if (rc == 0) {
                 const dim3 grid((unsigned)((tk + 1023) / 1024), (unsigned)tj);
-                k_gram_combine<<<grid, 256, 0, st>>>(j0, k0, tk, Tp, P, Q1, Q2, R, cst, scale, G);
+                k_gram_combine<<<grid, 256, 0, st>>>(j0, k0, tk, Tp, N, P, Q1, Q2, R, af, qn, G);
                 cu(cudaGetLastError(), "combine");
             }
         }
@@ -438,7 +451,8 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     cudaFree(nm);
     cudaFree(scales);
     cudaFree(tiles);
-    cudaFree(cst);
+    cudaFree(af);
+    cudaFree(qn);
     g_route_bits = rc == 0 ? bits : 0;
     return rc;
 }

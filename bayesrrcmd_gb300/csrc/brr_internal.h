@@ -84,7 +84,7 @@ struct SweepArgs {
     long long *prof;             // optional: cycles per round phase of CTA 0 (diagnostics), or null
     uint64_t timeout_ns;         // limit of any single wait
     int phantom;                 // extra arrivals the barrier waits for (tests of the timeout path)
-    const double *gram;          // blocked FP32C sweep: packed lower-triangle marker Gram (FP64)
+    const float2 *gram;          // blocked FP32C sweep: packed lower-triangle marker Gram (double-float)
     double *gstage;              // blocked FP32C sweep: staged Gram entries (sweep_block_stage_bytes)
     int has_missing;             // any missing genotype in the packed markers
     const BlockRec *brec;        // blocked FP32C sweep: M records in sweep order
@@ -258,7 +258,7 @@ int sweep_block_threads();
 int sweep_block_max_ctas_per_sm(size_t smem, std::string *why = nullptr);
 cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, size_t *work);
 int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, const double *scale,
-               const int64_t *counts, bool missing, double *G, cudaStream_t st, std::string &why,
+               const int64_t *counts, bool missing, float2 *G, cudaStream_t st, std::string &why,
                float *device_ms);
 // Element bits of the last successful Gram build's GEMM operands (4, 8 or 16).
 int gram_route_bits();
