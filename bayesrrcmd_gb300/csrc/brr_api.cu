@@ -157,6 +157,7 @@ void free_all(brr_ctx *c)
     cudaFree(c->d_comp);
     cudaFree(c->d_acum);
     cudaFree(c->d_eps);
+    cudaFree(c->d_eps_dl);
     cudaFree(c->d_eps_hi);
     cudaFree(c->d_eps_lo);
     cudaFree(c->d_order);
@@ -261,11 +262,14 @@ int download_eps(brr_ctx *c, double *eps_host)
     if (c->cfg.form == BRR_FORM_FP64) {
         BRR_CUDA(cudaMemcpy(eps_host, c->d_eps, sizeof(double) * N, cudaMemcpyDeviceToHost));
     } else {
-        std::vector<float> h(N), l(N);
-        BRR_CUDA(cudaMemcpy(h.data(), c->d_eps_hi, sizeof(float) * N, cudaMemcpyDeviceToHost));
-        BRR_CUDA(cudaMemcpy(l.data(), c->d_eps_lo, sizeof(float) * N, cudaMemcpyDeviceToHost));
-        for (int64_t i = 0; i < N; ++i)
-            eps_host[i] = (double)h[i] + (double)l[i];
+        // hi + lo formed on the device, one copy of N doubles
+        if (!c->d_eps_dl && cudaMalloc((void **)&c->d_eps_dl, sizeof(double) * N) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(BRR_ERR_OOM, "device allocation failed");
+        }
+        BRR_CUDA(launch_df_to_double(N, c->d_eps_hi, c->d_eps_lo, c->d_eps_dl, c->st));
+        BRR_CUDA(cudaMemcpyAsync(eps_host, c->d_eps_dl, sizeof(double) * N, cudaMemcpyDeviceToHost, c->st));
+        BRR_CUDA(cudaStreamSynchronize(c->st));
     }
     return BRR_OK;
 }

@@ -55,6 +55,7 @@ struct brr_ctx {
     uint32_t *d_nzj = nullptr;
     double *d_nzb = nullptr;
     float2 *d_gram = nullptr;           // blocked FP32C: packed marker Gram (double-float entries)
+    double *d_eps_dl = nullptr;         // FP32C: the residual as doubles for its read-back (allocated on use)
     double *d_gstage = nullptr;         // blocked FP32C: staged Gram entries (8 blocks)
     brr::BlockRec *d_brec = nullptr;         // blocked FP32C: records in sweep order
     float2 *d_bdf = nullptr;            // blocked FP32C: [2][M] new beta, acum (double-float)

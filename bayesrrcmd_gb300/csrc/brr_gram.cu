@@ -204,6 +204,13 @@ struct LtGemm {
     void *ws = nullptr;
     int64_t npad = 0;
     cudaDataType_t type = CUDA_R_8F_E4M3;
+    // the algorithm chosen for each tile shape of the build (at most four)
+    struct Choice {
+        int64_t tk, tj;
+        cublasLtMatmulAlgo_t algo;
+    };
+    Choice chosen[4];
+    int n_chosen = 0;
 
     bool init(int64_t np, cudaDataType_t t, const void *scales)
     {
@@ -243,16 +250,27 @@ struct LtGemm {
         if (cublasLtMatrixLayoutCreate(&la, type, npad, tk, npad) == CUBLAS_STATUS_SUCCESS &&
             cublasLtMatrixLayoutCreate(&lb, type, npad, tj, npad) == CUBLAS_STATUS_SUCCESS &&
             cublasLtMatrixLayoutCreate(&lc, CUDA_R_32F, tk, tj, ld) == CUBLAS_STATUS_SUCCESS) {
+            const cublasLtMatmulAlgo_t *algo = nullptr;
+            for (int c = 0; c < n_chosen; ++c)
+                if (chosen[c].tk == tk && chosen[c].tj == tj)
+                    algo = &chosen[c].algo;
             cublasLtMatmulHeuristicResult_t hr{};
             int n = 0;
-            if (cublasLtMatmulAlgoGetHeuristic(h, op, la, lb, lc, lc, pref, 1, &hr, &n) != CUBLAS_STATUS_SUCCESS ||
-                n < 1) {
+            if (!algo) {
+                if (cublasLtMatmulAlgoGetHeuristic(h, op, la, lb, lc, lc, pref, 1, &hr, &n) == CUBLAS_STATUS_SUCCESS &&
+                    n >= 1) {
+                    algo = &hr.algo;
+                    if (n_chosen < 4)
+                        chosen[n_chosen++] = Choice{tk, tj, hr.algo};
+                }
+            }
+            if (!algo) {
                 rc = 1;
             } else if (!A || !B) {
                 rc = 0;
             } else {
                 const float one = 1.f, zero = 0.f;
-                rc = cublasLtMatmul(h, op, &one, A, la, B, lb, &zero, out, lc, out, lc, &hr.algo, ws, kLtWorkspace,
+                rc = cublasLtMatmul(h, op, &one, A, la, B, lb, &zero, out, lc, out, lc, algo, ws, kLtWorkspace,
                                     st) == CUBLAS_STATUS_SUCCESS
                          ? 0
                          : -1;
@@ -286,7 +304,7 @@ cudaError_t gram_bytes_needed(int64_t N, int64_t M, bool missing, size_t *gram, 
     const int64_t T = round128(std::min<int64_t>(M, kTile));
     *gram = (size_t)(M * (M - 1) / 2) * sizeof(float2);
     // the BF16 route's rows (2 bytes per genotype) bound the FP8 route's (1 byte)
-    *work = (size_t)round16(M) * npad * 2 * (missing ? 2 : 1) + (size_t)T * T * 4 * (missing ? 4 : 1) +
+    *work = (size_t)round16(M) * npad * 2 * (missing ? 2 : 1) + (size_t)T * T * 4 * (missing ? 4 : 1) * 2 +
             (size_t)M * 24 + kLtWorkspace;
     return cudaSuccess;
 }
@@ -313,11 +331,20 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cu(cudaEventCreate(&ev[0]), "event");
     cu(cudaEventCreate(&ev[1]), "event");
-    cu(cudaMalloc(&tiles, sizeof(float) * (size_t)Tp * Tp * (missing ? 4 : 1)), "allocation of the product tiles");
+    // two sets of product tiles: the combination of one tile runs on a second
+    // stream while the tensor cores form the next
+    const size_t set_floats = (size_t)Tp * Tp * (missing ? 4 : 1);
+    cu(cudaMalloc(&tiles, sizeof(float) * set_floats * 2), "allocation of the product tiles");
+    cudaStream_t sc = nullptr;
+    cudaEvent_t ev_gemm[2] = {nullptr, nullptr}, ev_comb[2] = {nullptr, nullptr};
+    cu(cudaStreamCreateWithFlags(&sc, cudaStreamNonBlocking), "stream");
+    for (int b = 0; b < 2; ++b) {
+        cu(cudaEventCreateWithFlags(&ev_gemm[b], cudaEventDisableTiming), "event");
+        cu(cudaEventCreateWithFlags(&ev_comb[b], cudaEventDisableTiming), "event");
+    }
     cu(cudaMalloc(&af, sizeof(float2) * (size_t)M), "allocation of the per-marker constants");
     cu(cudaMalloc(&qn, sizeof(longlong2) * (size_t)M), "allocation of the per-marker counts");
-    float *P = tiles, *Q1 = missing ? tiles + (size_t)Tp * Tp : nullptr,
-          *Q2 = missing ? tiles + 2 * (size_t)Tp * Tp : nullptr, *R = missing ? tiles + 3 * (size_t)Tp * Tp : nullptr;
+    float *P = tiles;   // the first set, for the choice of the route
     if (rc == 0)
         cu(cudaEventRecord(ev[0], st), "event");
 
@@ -417,34 +444,59 @@ int build_gram(const uint8_t *codes, int64_t col_stride, int64_t N, int64_t M, c
         }
     };
     const int64_t side = bits == 4 ? 128 : 16;
+    int64_t tile = 0;
     for (int64_t j0 = 0; j0 < M && rc == 0; j0 += T) {
         const int64_t tj = std::min<int64_t>(T, M - j0);
-        for (int64_t k0 = 0; k0 <= j0 && rc == 0; k0 += T) {
+        for (int64_t k0 = 0; k0 <= j0 && rc == 0; k0 += T, ++tile) {
             const int64_t tk = std::min<int64_t>(T, M - k0);
+            const int b = (int)(tile & 1);
+            float *Pb = tiles + (size_t)b * set_floats;
+            float *Q1b = missing ? Pb + (size_t)Tp * Tp : nullptr, *Q2b = missing ? Pb + 2 * (size_t)Tp * Tp : nullptr,
+                  *Rb = missing ? Pb + 3 * (size_t)Tp * Tp : nullptr;
+            // the set is free once the combination of two tiles back is done
+            if (tile >= 2)
+                cu(cudaStreamWaitEvent(st, ev_comb[b], 0), "wait");
             // low-precision tile sides rounded up (those rows exist and are zero)
             const int64_t gk = bits != 16 ? (tk + side - 1) / side * side : tk;
             const int64_t gj = bits != 16 ? (tj + side - 1) / side * side : tj;
-            gemm(gp, gp, k0, gk, j0, gj, P);             // P[j,k]  = g_j . g_k
+            gemm(gp, gp, k0, gk, j0, gj, Pb);            // P[j,k]  = g_j . g_k
             if (missing) {
-                gemm(nm, gp, k0, gk, j0, gj, Q1);        // Q1[j,k] = g_j . m_k
-                gemm(gp, nm, k0, gk, j0, gj, Q2);        // Q2[j,k] = m_j . g_k
-                gemm(nm, nm, k0, gk, j0, gj, R);         // R[j,k]  = m_j . m_k
+                gemm(nm, gp, k0, gk, j0, gj, Q1b);       // Q1[j,k] = g_j . m_k
+                gemm(gp, nm, k0, gk, j0, gj, Q2b);       // Q2[j,k] = m_j . g_k
+                gemm(nm, nm, k0, gk, j0, gj, Rb);        // R[j,k]  = m_j . m_k
             }
             if (rc == 0) {
+                cu(cudaEventRecord(ev_gemm[b], st), "event");
+                cu(cudaStreamWaitEvent(sc, ev_gemm[b], 0), "wait");
                 const dim3 grid((unsigned)((tk + 1023) / 1024), (unsigned)tj);
-                k_gram_combine<<<grid, 256, 0, st>>>(j0, k0, tk, Tp, N, P, Q1, Q2, R, af, qn, G);
+                k_gram_combine<<<grid, 256, 0, sc>>>(j0, k0, tk, Tp, N, Pb, Q1b, Q2b, Rb, af, qn, G);
                 cu(cudaGetLastError(), "combine");
+                cu(cudaEventRecord(ev_comb[b], sc), "event");
             }
         }
     }
+    // the build ends when the last combinations have
+    for (int b = 0; b < 2 && rc == 0; ++b)
+        if (tile > b)
+            cu(cudaStreamWaitEvent(st, ev_comb[b], 0), "wait");
     if (rc == 0)
         cu(cudaEventRecord(ev[1], st), "event");
     cu(cudaStreamSynchronize(st), "Gram build");
+    if (sc)
+        cu(cudaStreamSynchronize(sc), "Gram build");
     if (rc == 0 && device_ms)
         cu(cudaEventElapsedTime(device_ms, ev[0], ev[1]), "event");
     for (cudaEvent_t e : ev)
         if (e)
             cudaEventDestroy(e);
+    for (int b = 0; b < 2; ++b) {
+        if (ev_gemm[b])
+            cudaEventDestroy(ev_gemm[b]);
+        if (ev_comb[b])
+            cudaEventDestroy(ev_comb[b]);
+    }
+    if (sc)
+        cudaStreamDestroy(sc);
     if (hb)
         cublasDestroy(hb);
     cudaFree(gp);

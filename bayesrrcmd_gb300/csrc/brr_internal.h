@@ -239,6 +239,7 @@ cudaError_t launch_synth_bed(uint8_t *out, int64_t N, int64_t M, uint32_t seed, 
                              double miss, cudaStream_t st, double beta_a = 0.0, double beta_b = 0.0);
 cudaError_t launch_sweep(int form, int kind, const SweepArgs &a, size_t smem, cudaStream_t st);
 size_t sweep_smem_bytes(int form, int kind, const SweepArgs &a);
+cudaError_t launch_df_to_double(int64_t N, const float *hi, const float *lo, double *out, cudaStream_t st);
 cudaError_t noalloc_xbeta(cudaStream_t st, int kind, int64_t N, const uint8_t *codes, int64_t col_stride,
                           const double *table, const uint32_t *idx, const double *b, int64_t n, double *d_out,
                           std::string &why);

@@ -1639,6 +1639,20 @@ cudaError_t launch_refresh(int form, int kind, int64_t N, const double *ystd, do
     return cudaGetLastError();
 }
 
+// The double-float residual as doubles (hi + lo), for the state read-back.
+__global__ void k_df_to_double(int64_t N, const float *__restrict__ hi, const float *__restrict__ lo, double *out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N)
+        out[i] = (double)hi[i] + (double)lo[i];
+}
+
+cudaError_t launch_df_to_double(int64_t N, const float *hi, const float *lo, double *out, cudaStream_t st)
+{
+    k_df_to_double<<<(unsigned)((N + kThreads - 1) / kThreads), kThreads, 0, st>>>(N, hi, lo, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sweep_stats(int64_t M, const int32_t *group, const int32_t *comp, const uint8_t *chosen,
                                const double *beta, int n_groups, unsigned long long *out, cudaStream_t st)
 {

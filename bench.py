@@ -216,7 +216,9 @@ def run_e2e(lib, gpu, torch, device, host_bed, y, group, steps, chain_id):
     ch.pack_bed(host_bed)
     ch.set_groups(group)
     ch.set_phenotype(y)
+    t1 = time.perf_counter()
     ch.init()
+    t2 = time.perf_counter()
     d2h = 0
     for _ in range(steps):
         ch.iterate(1)
@@ -224,9 +226,15 @@ def run_e2e(lib, gpu, torch, device, host_bed, y, group, steps, chain_id):
         d2h += st["beta"].nbytes + st["comp"].nbytes + st["acum"].nbytes + st["eps"].nbytes
     torch.cuda.synchronize(device)
     wall = time.perf_counter() - t0
+    gram_ms = ch.gram_info()["build_ms"]
     ch.close()
     h2d = host_bed.nbytes + y.nbytes + group.nbytes
-    return dict(wall=wall, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps)
+    # where the end-to-end time goes (host clock): upload and packing, the
+    # chain's set-up (marker Gram: allocation and device build), the iterations
+    # with their read-backs
+    parts = {"upload_and_pack_s": t1 - t0, "init_s": t2 - t1, "gram_build_device_s": gram_ms / 1e3,
+             "iterations_s": wall - (t2 - t0)}
+    return dict(wall=wall, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps, parts=parts)
 
 
 # Batching form: 64 chains (distinct seeds, one phenotype each) on shared
@@ -909,7 +917,8 @@ def main():
                "unit": "marker-updates/s",
                "h2d_bytes_per_step": int(e["h2d_per_step"]), "d2h_bytes_per_step": int(e["d2h_per_step"]),
                "includes": f"chain of {e2e_steps} iterations: pinned-host BED upload + device packing + "
-                           f"marker Gram + init, then per iteration the sample read-back"}
+                           f"marker Gram + init, then per iteration the sample read-back",
+               "parts_s": e["parts"]}
     batched = None
     if not args.no_batch and not args.small:
         bsteps = int(os.environ.get("BRR_BATCH_STEPS", "3"))
