@@ -100,19 +100,22 @@ namespace brr {
 
 namespace {
 
-// Roles by warp.  Warp w issues from sub-partition w % 4, so the resolve warp
-// (the latency-bound sampling chain) is placed on sub-partition 3 with the
-// input warp alone; the eight dot warps are 0-2, 4-6, 8 and 9.
+// Roles by warp.  Warp w issues from sub-partition w % 4: the eight dot warps
+// 0-7 put two on every sub-partition (their dot products and updates are the
+// longest role), and the resolve, input and chore warps 8-10 take the third
+// slot of sub-partitions 0-2.  Measured against the resolve warp alone with
+// the input warp on sub-partition 3 (three dot warps on sub-partitions 0 and
+// 1): 3 % more marker-updates/s at N = M = 100,000 although the resolve warp
+// now shares its sub-partition with two dot warps.
 constexpr int kDotWarps = 8;
-constexpr int kResolveWarp = 3;    // samples the blocks
-constexpr int kInputWarp = 7;      // grid barrier, inputs of the next block
+constexpr int kResolveWarp = 8;    // samples the blocks
+constexpr int kInputWarp = 9;      // grid barrier, inputs of the next block
 constexpr int kChoreWarp = 10;     // Gram copies and gathers, outputs
 constexpr int kBlockThreads = (kDotWarps + 3) * 32;
 // index 0..7 of a dot warp, -1 for the other roles
-__host__ __device__ constexpr int dot_index(int w)
-{
-    return (w == kResolveWarp || w == kInputWarp || w == kChoreWarp) ? -1 : w - (w > 3) - (w > 7);
-}
+__host__ __device__ constexpr int dot_index(int w) { return w < kDotWarps ? w : -1; }
+static_assert(kResolveWarp >= kDotWarps && kInputWarp >= kDotWarps && kChoreWarp >= kDotWarps,
+              "the dot warps are warps 0..7");
 constexpr int kAccBufs = 8;
 constexpr int kAccCopies = 8;   // CTA s adds into copy s % 8: 19 atomics per address and block, not 152
 constexpr int kAccBufWords = kAccCopies * kMaxSpec * 4;
@@ -279,6 +282,18 @@ constexpr int kFrac = 50;
 constexpr long long kFixMax = 1ll << 62;
 
 __device__ __forceinline__ int sext16(unsigned w) { return (int)(w << 16) >> 16; }
+
+// A code byte (4 individuals, 2 bits each) as the byte selector of __byte_perm:
+// code k of the byte in bits 4k..4k+1 of the result.  Selecting from
+// kGenoBytes gives the 4 genotype bytes (code 0: 2, 2: 1, 1 and 3: 0), from
+// kMissBytes the 4 missing-indicator bytes (code 1), with no table lookup.
+constexpr unsigned kGenoBytes = 0x00010002u;
+constexpr unsigned kMissBytes = 0x00000100u;
+__device__ __forceinline__ unsigned code_nibbles(unsigned v)
+{
+    const unsigned x = (v | (v << 4)) & 0x0F0Fu;
+    return (x | (x << 2)) & 0x3333u;
+}
 
 __device__ __forceinline__ void split_limbs(long long E, int (&l)[4])
 {
@@ -501,9 +516,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
     __shared__ float s_H[kMaxGroups];
     __shared__ int32_t s_gk[kMaxGroups];
     __shared__ BlockOut s_out[2];
-    __shared__ uint32_t s_glut[256];         // code byte -> 4 genotype bytes (code 0: 2, 2: 1, 1 and 3: 0)
-    __shared__ uint32_t s_mlut[256];         // code byte -> 4 missing-indicator bytes (code 1)
     __shared__ long long s_D[kMaxSpec][4];   // residual change per update and code, fixed point
+    __shared__ unsigned s_uoff[kMaxSpec];    // offset of each update's codes in the ring
     // marker ids of blocks q (slot q % kIdSlots), copied from the sweep order
     // one iteration before they are read: blocks r+1 .. r+4 are resident in
     // iteration r while block r+5's ids are in flight
@@ -572,17 +586,6 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             reinterpret_cast<longlong2 *>(fix)[2 * b] = make_longlong2(E[0], E[1]);
             reinterpret_cast<longlong2 *>(fix)[2 * b + 1] = make_longlong2(E[2], E[3]);
         }
-    }
-    for (int v = tid; v < 256; v += kBlockThreads) {
-        uint32_t g = 0, m = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const unsigned c = (v >> (2 * k)) & 3u;
-            g |= (c == 0u ? 2u : (c == 2u ? 1u : 0u)) << (8 * k);
-            m |= (c == 1u ? 1u : 0u) << (8 * k);
-        }
-        s_glut[v] = g;
-        s_mlut[v] = m;
     }
     for (int i = tid; i < a.n_groups; i += kBlockThreads) {
         s_gk[i] = a.gK[i];
@@ -774,14 +777,15 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
 #pragma unroll
             for (int k = 0; k < MPW; ++k) {
                 const unsigned v = ring_codes[cofs[k] + b];
-                const int g = (int)s_glut[v];
+                const unsigned sel = code_nibbles(v);
+                const int g = (int)__byte_perm(kGenoBytes, 0u, sel);
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     A[4 * k + t] = __dp2a_lo(wv[2 * t], g, A[4 * k + t]);
                     A[4 * k + t] = __dp2a_hi(wv[2 * t + 1], g, A[4 * k + t]);
                 }
                 if (MISS) {
-                    const int mm = (int)s_mlut[v];
+                    const int mm = (int)__byte_perm(kMissBytes, 0u, sel);
 #pragma unroll
                     for (int t = 0; t < 4; ++t) {
                         Mx[4 * k + t] = __dp2a_lo(wv[2 * t], mm, Mx[4 * k + t]);
@@ -875,6 +879,8 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             if (!df_to_fix(dh, dl, D))
                 atomicCAS(a.err, kDevOk, kDevRange);
             s_D[u][code] = D;
+            if (code == 0)
+                s_uoff[u] = ((qb + (unsigned)s_upd[par][u]) & Rm) * (unsigned)a.slot_bytes;
         }
         if (tid == 0)
             stamp(q + 1, 12);
@@ -888,8 +894,21 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             const longlong2 e01 = reinterpret_cast<const longlong2 *>(fix)[2 * b];
             const longlong2 e23 = reinterpret_cast<const longlong2 *>(fix)[2 * b + 1];
             long long E[4] = {e01.x, e01.y, e23.x, e23.y};
-            for (int u = 0; u < U; ++u) {
-                const unsigned v = ring_codes[((qb + s_upd[par][u]) & Rm) * a.slot_bytes + b];
+            // four updates' code bytes loaded at a time
+            int u = 0;
+            for (; u + 4 <= U; u += 4) {
+                unsigned v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    v[k] = ring_codes[s_uoff[u + k] + b];
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        E[i] += s_D[u + k][(v[k] >> (2 * i)) & 3u];
+            }
+            for (; u < U; ++u) {
+                const unsigned v = ring_codes[s_uoff[u] + b];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
                     E[i] += s_D[u][(v >> (2 * i)) & 3u];
