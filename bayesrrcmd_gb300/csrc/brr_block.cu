@@ -281,8 +281,6 @@ __device__ __forceinline__ float2 ld_relaxed_f2(const float2 *p)
 constexpr int kFrac = 50;
 constexpr long long kFixMax = 1ll << 62;
 
-__device__ __forceinline__ int sext16(unsigned w) { return (int)(w << 16) >> 16; }
-
 // A code byte (4 individuals, 2 bits each) as the byte selector of __byte_perm:
 // code k of the byte in bits 4k..4k+1 of the result.  Selecting from
 // kGenoBytes gives the 4 genotype bytes (code 0: 2, 2: 1, 1 and 3: 0), from
@@ -332,6 +330,22 @@ __device__ __forceinline__ bool df_to_fix(float h, float l, long long &E)
         return false;
     E = (long long)x;
     return true;
+}
+
+// Double-float value times 2^kFrac to the nearest integer by the hardware
+// conversions, for the residual changes of the update: the scaled high part is
+// an integer whenever it reaches 2^23, and then the sum is the nearest integer
+// to the scaled value; below that it is within one unit of it.  False when out
+// of range or not a number.  The exact df_to_fix (two 128-bit shifts) stays for
+// the residual itself.
+static_assert(kFrac == 50, "df_to_fix_near scales by 2^50");
+__device__ __forceinline__ bool df_to_fix_near(float h, float l, long long &E)
+{
+    const float sh = h * 0x1p50f, sl = l * 0x1p50f;
+    if (!(fabsf(sh) < 0x1p61f) || !(fabsf(sl) < 0x1p61f))
+        return false;
+    E = __float2ll_rn(sh) + __float2ll_rn(sl);
+    return E < kFixMax && E > -kFixMax;
 }
 
 __device__ __forceinline__ void fix_to_df(long long E, float &h, float &l)
@@ -861,7 +875,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
 
     // ---- rank-U residual update of block q (dot warps, run at the start of the
     // next iteration while the resolve warp works on block q+1):
-    // E += round(dBeta_u * x_u(code) * 2^kFrac)
+    // E += round(dBeta_u * x_u(code) * 2^kFrac) (df_to_fix_near)
     auto apply_update = [&](int q) {
         const int par = q & 1;
         const int U = s_nupd[par];
@@ -876,7 +890,7 @@ __global__ void __launch_bounds__(12 * 32, 1) k_sweep_block(SweepArgs a)
             float dh, dl;
             df_mul(dB.x, dB.y, xh, xl, dh, dl);
             long long D = 0;
-            if (!df_to_fix(dh, dl, D))
+            if (!df_to_fix_near(dh, dl, D))
                 atomicCAS(a.err, kDevOk, kDevRange);
             s_D[u][code] = D;
             if (code == 0)
