@@ -937,6 +937,12 @@ int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes)
     if (nbytes != cf.M * ((cf.N + 3) / 4))
         return fail(BRR_ERR_ARG, "BED payload size does not match M*ceil(N/4)");
     BRR_CUDA(cudaSetDevice(c.dev));
+    {
+        // the packer reads nbytes from d_bed: refuse a buffer it would overrun
+        std::string why;
+        if (!device_range_check(c.dev, d_bed, (size_t)nbytes, "d_bed", why))
+            return fail(BRR_ERR_ARG, why);
+    }
     const int64_t M = cf.M;
     if (!c.d_codes) {
         if (dalloc(&c.d_codes, (size_t)(M * c.col_stride)) != cudaSuccess || dalloc(&c.d_counts, (size_t)M * 4) ||
@@ -1336,6 +1342,14 @@ int brr_synth_bed_device(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, do
     if (!d_bed || N < 2 || M < 1 || !(p_lo > 0.0) || !(p_hi <= 0.5) || !(p_lo <= p_hi) || !(missing >= 0.0) ||
         !(missing < 0.5))
         return fail(BRR_ERR_ARG, "invalid synthetic genotype parameters");
+    {
+        // the generator writes M * ceil(N/4) bytes to d_bed on the current device
+        int dev = 0;
+        BRR_CUDA(cudaGetDevice(&dev));
+        std::string why;
+        if (!device_range_check(dev, d_bed, (size_t)(M * ((N + 3) / 4)), "d_bed", why))
+            return fail(BRR_ERR_ARG, why);
+    }
     BRR_CUDA(launch_synth_bed(d_bed, N, M, seed, p_lo, p_hi, missing, 0));
     BRR_CUDA(cudaDeviceSynchronize());
     return BRR_OK;
@@ -1347,6 +1361,14 @@ int brr_synth_bed_device_beta(uint8_t *d_bed, int64_t N, int64_t M, uint32_t see
     if (!d_bed || N < 2 || M < 1 || !(a > 0.0) || !(b > 0.0) || !(p_lo > 0.0) || !(p_hi <= 0.5) ||
         !(p_lo <= p_hi) || !(missing >= 0.0) || !(missing < 0.5))
         return fail(BRR_ERR_ARG, "invalid synthetic genotype parameters");
+    {
+        // the generator writes M * ceil(N/4) bytes to d_bed on the current device
+        int dev = 0;
+        BRR_CUDA(cudaGetDevice(&dev));
+        std::string why;
+        if (!device_range_check(dev, d_bed, (size_t)(M * ((N + 3) / 4)), "d_bed", why))
+            return fail(BRR_ERR_ARG, why);
+    }
     BRR_CUDA(launch_synth_bed(d_bed, N, M, seed, p_lo, p_hi, missing, 0, a, b));
     BRR_CUDA(cudaDeviceSynchronize());
     return BRR_OK;

@@ -331,6 +331,12 @@ int brr_batch_pack_bed_device(brr_batch *b, const uint8_t *d_bed, int64_t nbytes
     if (nbytes != M * ((cf.N + 3) / 4))
         return api_fail(BRR_ERR_ARG, "BED payload size does not match M*ceil(N/4)");
     BATCH_CUDA(cudaSetDevice(b->dev));
+    {
+        // the packer reads nbytes from d_bed: refuse a buffer it would overrun
+        std::string why;
+        if (!device_range_check(b->dev, d_bed, (size_t)nbytes, "d_bed", why))
+            return api_fail(BRR_ERR_ARG, why);
+    }
     if (!b->d_codes) {
         if (balloc(&b->d_codes, (size_t)(M * b->col_stride)) || balloc(&b->d_counts, (size_t)M * 4) ||
             balloc(&b->d_lut, (size_t)M * 4) || balloc(&b->d_scale, (size_t)M * 2) || balloc(&b->d_colsum, (size_t)M) ||

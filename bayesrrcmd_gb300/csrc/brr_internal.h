@@ -244,6 +244,9 @@ cudaError_t noalloc_xbeta(cudaStream_t st, int kind, int64_t N, const uint8_t *c
                           const double *table, const uint32_t *idx, const double *b, int64_t n, double *d_out,
                           std::string &why);
 bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string &why);
+// Whether p is device or managed memory of device dev with `bytes` bytes to the
+// end of its allocation (no allocation, no launch); the message names `name`.
+bool device_range_check(int dev, const void *p, size_t bytes, const char *name, std::string &why);
 int sweep_max_ctas_per_sm(int form, int kind, size_t smem, bool pair_rounds = false);
 // Clusters of G CTAs of the cluster sweep that can be resident at once (0: none).
 int sweep_cluster_fits(int form, int kind, int G, size_t smem);

@@ -171,27 +171,25 @@ cudaError_t terms_address(NoallocTerms **out, std::string &why)
 
 }  // namespace
 
-// Whether d_out is device (or managed) memory of device `dev` with at least
-// `bytes` bytes from d_out to the end of its allocation.  Allocates nothing.
-bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string &why)
+// Whether p is device (or managed) memory of device `dev` with at least `bytes`
+// bytes from p to the end of its allocation; `name` names the argument in the
+// message.  Allocates nothing and launches nothing, so a caller can refuse a
+// buffer that a kernel would read or write out of bounds.
+bool device_range_check(int dev, const void *p, size_t bytes, const char *name, std::string &why)
 {
-    if ((uintptr_t)d_out % alignof(double) != 0) {
-        why = "d_out must be aligned to 8 bytes";
-        return false;
-    }
     cudaPointerAttributes a{};
-    cudaError_t e = cudaPointerGetAttributes(&a, d_out);
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        why = std::string("d_out is not a CUDA pointer: ") + cudaGetErrorString(e);
+        why = std::string(name) + " is not a CUDA pointer: " + cudaGetErrorString(e);
         return false;
     }
     if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) {
-        why = "d_out must be device or managed memory (got host or unregistered memory)";
+        why = std::string(name) + " must be device or managed memory (got host or unregistered memory)";
         return false;
     }
     if (a.device != dev) {
-        why = "d_out belongs to device " + std::to_string(a.device) + ", the context runs on device " +
+        why = std::string(name) + " belongs to device " + std::to_string(a.device) + ", the call runs on device " +
               std::to_string(dev);
         return false;
     }
@@ -202,17 +200,28 @@ bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string 
     }
     CUdeviceptr base = 0;
     size_t size = 0;
-    if (g_mem_get_address_range(&base, &size, (CUdeviceptr)d_out) != CUDA_SUCCESS) {
-        why = "the allocation holding d_out could not be found";
+    if (g_mem_get_address_range(&base, &size, (CUdeviceptr)p) != CUDA_SUCCESS) {
+        why = std::string("the allocation holding ") + name + " could not be found";
         return false;
     }
-    const size_t left = (size_t)(base + size - (CUdeviceptr)d_out);
+    const size_t left = (size_t)(base + size - (CUdeviceptr)p);
     if (left < bytes) {
-        why = "d_out has " + std::to_string(left) + " bytes to the end of its allocation; " + std::to_string(bytes) +
-              " (N doubles) are needed";
+        why = std::string(name) + " has " + std::to_string(left) + " bytes to the end of its allocation; " +
+              std::to_string(bytes) + " are needed";
         return false;
     }
     return true;
+}
+
+// The output of brr_xbeta_noalloc: N doubles, 8-byte aligned, in device (or
+// managed) memory of device `dev`.
+bool noalloc_check_output(int dev, const void *d_out, size_t bytes, std::string &why)
+{
+    if ((uintptr_t)d_out % alignof(double) != 0) {
+        why = "d_out must be aligned to 8 bytes";
+        return false;
+    }
+    return device_range_check(dev, d_out, bytes, "d_out", why);
 }
 
 cudaError_t noalloc_xbeta(cudaStream_t st, int kind, int64_t N, const uint8_t *codes, int64_t col_stride,
