@@ -166,7 +166,8 @@ int brr_ctx_destroy(brr_ctx *ctx);
  * magic header already removed) from host memory; the decode, genotype counts,
  * standardisation or ragged index lists all run on the device. */
 int brr_pack_bed(brr_ctx *ctx, const uint8_t *bed, int64_t nbytes);
-/* Same, from a device pointer. */
+/* Same, from a device pointer: device or managed memory of the context's GPU
+ * with nbytes to the end of its allocation, else BRR_ERR_ARG before any launch. */
 int brr_pack_bed_device(brr_ctx *ctx, const uint8_t *d_bed, int64_t nbytes);
 
 /* Per-marker table, M x 4 doubles.  Dense: the standardised value of each
@@ -211,7 +212,9 @@ int brr_xbeta(brr_ctx *ctx, const uint32_t *idx, const double *b, int64_t n, dou
 /* Seeded synthetic genotypes written as a BED payload (M x ceil(N/4) bytes,
  * no header) into a device buffer: allele frequency of marker j uniform in
  * [p_lo, p_hi], genotypes Binomial(2, p_j), missing at rate `missing`.  A data
- * source for benchmarks at sizes where host generation is too slow. */
+ * source for benchmarks at sizes where host generation is too slow.  d_bed must
+ * be device or managed memory of the current GPU with M x ceil(N/4) bytes to the
+ * end of its allocation, else BRR_ERR_ARG before any launch. */
 int brr_synth_bed_device(uint8_t *d_bed, int64_t N, int64_t M, uint32_t seed, double p_lo, double p_hi,
                          double missing);
 /* The same with allele frequencies p_j ~ Beta(a, b) clipped to [p_lo, p_hi]. */
@@ -274,6 +277,8 @@ typedef struct brr_batch brr_batch;
 int brr_batch_create(const brr_config *cfg, int32_t chains, brr_batch **out);
 int brr_batch_destroy(brr_batch *b);
 int brr_batch_pack_bed(brr_batch *b, const uint8_t *bed, int64_t nbytes);
+/* d_bed: device or managed memory of the batch's GPU with nbytes to the end of
+ * its allocation, else BRR_ERR_ARG before any launch. */
 int brr_batch_pack_bed_device(brr_batch *b, const uint8_t *d_bed, int64_t nbytes);
 int brr_batch_set_groups(brr_batch *b, const int32_t *group);
 /* chains x N phenotype values, chain-major */
